@@ -1,0 +1,229 @@
+/*
+ * obte.h — C ABI of the GB300 (sm_103a) phonon-BTE transport library.
+ *
+ * The reference (romanodev/OpenBTE) is pure Python; its transport path is the
+ * pair of functions
+ *     BTE_RTA(geo, mat, bcs, fourier, effective_thermal_conductivity, ...)   openbte/bte.py:19-271
+ *     Fourier(geometry, thermal_conductivity, boundary_conditions, ...)      openbte/fourier.py:15-185
+ * A Python FFI for that path (ctypes / cffi) binds the functions below; the
+ * package's ``openbte_gb300.BTE_RTA`` / ``Fourier`` wrappers are exactly that
+ * binding.
+ *
+ * Conventions
+ *   - every call returns an obte_status; obte_status_string() names it;
+ *   - "host" arrays are read during the call only; "device" arrays are
+ *     caller-owned CUDA device pointers (e.g. torch tensors) on the
+ *     context's device; the library owns only its plans and scratch;
+ *   - all work is issued on the stream given to obte_context_create and the
+ *     call returns after that stream has finished the work it issued;
+ *   - indices are 0-based int64, floating point is IEEE binary64 at the boundary.
+ */
+#ifndef OBTE_H
+#define OBTE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  OBTE_OK = 0,
+  OBTE_ERR_BAD_ARG = 1,           /* invalid size, index or pointer            */
+  OBTE_ERR_OOM = 2,               /* device allocation failed                  */
+  OBTE_ERR_ADMISSION = 3,         /* request exceeds the admitted HBM budget   */
+  OBTE_ERR_NOT_CONVERGED = 4,     /* iteration cap reached before tolerance    */
+  OBTE_ERR_CUDA = 5,              /* a CUDA runtime call failed                */
+  OBTE_ERR_CYCLE = 6,             /* upwind graph has a cycle besides periodic */
+  OBTE_ERR_UNSUPPORTED = 7        /* input outside what the kernels implement  */
+} obte_status;
+
+typedef struct obte_context_s* obte_context;
+typedef struct obte_plan_s* obte_plan;
+typedef struct obte_fourier_plan_s* obte_fourier_plan;
+
+/* Sweep precision. */
+enum { OBTE_FP64 = 0, OBTE_FP32_REFINE = 1, OBTE_FP32 = 2 };
+
+/* Contact kinds for kappa_eff (openbte/bte.py:132-158). */
+enum { OBTE_CONTACT_NONE = 0, OBTE_CONTACT_PERIODIC = 1, OBTE_CONTACT_MIXED = 2, OBTE_CONTACT_NANOWIRE = 3 };
+
+/*
+ * Problem description: the Mesh fields the transport path reads
+ * (openbte/objects.py:244-268), with boundary-condition names already
+ * resolved to side lists (openbte/objects.py:220-241).  All host arrays.
+ */
+typedef struct {
+  int32_t dim;                    /* 2 or 3                                       */
+  int64_t n_elems;
+  int64_t n_sides;
+  int32_t elem_nv;                /* sides per element (3 triangle, 4 tetrahedron) */
+  const int64_t* side_elem_map;   /* [n_sides, 2]                                 */
+  const double* normal_areas;     /* [n_sides, dim], outward from side_elem_map[:,0] */
+  const double* elem_volumes;     /* [n_elems]                                    */
+  const double* side_areas;       /* [n_sides]                                    */
+  int64_t n_internal;
+  const int64_t* internal;        /* [n_internal] sides coupling two elements (incl. kept periodic) */
+  int64_t n_periodic;
+  const int64_t* periodic_sides;  /* [n_periodic] kept periodic sides            */
+  const double* periodic_jump;    /* [n_periodic] jump of their region           */
+  int64_t n_diffuse;
+  const int64_t* diffuse_sides;   /* [n_diffuse] diffuse (thermalising) walls     */
+  int64_t n_mixed;
+  const int64_t* mixed_sides;     /* [n_mixed] isothermal walls                   */
+  const double* mixed_value;      /* [n_mixed] their temperature                  */
+  int32_t contact_kind;           /* OBTE_CONTACT_*                               */
+  int64_t n_contact;
+  const int64_t* contact_sides;   /* [n_contact] (ignored for NANOWIRE)           */
+  double contact_alpha;           /* jump (periodic) or value (mixed)             */
+  double normalization;           /* EffectiveThermalConductivity.normalization   */
+  int32_t is_nanowire;            /* BoundaryConditions.is_nanowire               */
+  const double* heat_source;      /* [n_elems] or NULL (HeatSource data)          */
+} obte_problem;
+
+/* Ordinate data (openbte/objects.py:500-509). All host arrays. */
+typedef struct {
+  int32_t n_mfp;
+  int32_t n_dir;
+  int32_t dim_dir;                /* columns of vmfp                              */
+  int32_t dim_sigma;              /* columns of sigma                             */
+  const double* mfps;             /* [n_mfp] nm                                   */
+  const double* vmfp;             /* [n_dir, dim_dir] unit directions             */
+  const double* sigma;            /* [n_mfp, n_dir, dim_sigma]                    */
+  const double* t_coeff;          /* [n_mfp, n_dir]                               */
+  double heat_source_coeff;
+} obte_material;
+
+typedef struct {
+  int32_t precision;              /* OBTE_FP64 | OBTE_FP32_REFINE | OBTE_FP32     */
+  double rtol;                    /* residual tolerance ‖F(u)-u‖/‖u‖             */
+  int32_t max_sweeps;             /* cap on transport sweeps                      */
+  int32_t restart;                /* GMRES restart length                         */
+  int32_t refine_steps;           /* FP64 residual corrections (FP32_REFINE)      */
+  double inner_rtol;              /* inner FP32 tolerance (FP32_REFINE)           */
+} obte_solve_opts;
+
+typedef struct {
+  double kappa_eff;               /* sum of K                                    */
+  int32_t n_sweeps;               /* transport sweeps issued                      */
+  int32_t n_sweeps_fp64;          /* of which in FP64                             */
+  double residual;                /* final ‖F(u)-u‖/‖u‖ (FP64)                   */
+  double offset;                  /* constant shift applied to match the reference's conserved offset */
+  int32_t converged;
+} obte_solve_info;
+
+/* ---- context ------------------------------------------------------------ */
+/* stream: a cudaStream_t (NULL = legacy default stream). */
+obte_status obte_context_create(int device, void* stream, obte_context* out);
+obte_status obte_context_destroy(obte_context ctx);
+obte_status obte_context_set_stream(obte_context ctx, void* stream);
+const char* obte_status_string(int status);
+/* Last error text recorded on this thread (CUDA error names, argument checks). */
+const char* obte_last_error(void);
+/* Number of kernel launches this library issued in the calling process (instrumentation). */
+int64_t obte_launch_count(void);
+
+/* ---- BTE_RTA (openbte/bte.py:19-271) ------------------------------------ */
+/*
+ * Build the sweep plan: per-direction upwind level order with periodic faces
+ * cut, shared-memory slot assignment for the live front, and the operator
+ * tables of openbte/bte.py:47-158, uploaded to the device.  With ctx == NULL
+ * the plan is host-only: its schedule can be queried but not solved.  Fails with
+ * OBTE_ERR_CYCLE when a direction's upwind graph (periodic faces removed)
+ * is not acyclic.
+ */
+obte_status obte_bte_plan_create(obte_context ctx, const obte_problem* prob,
+                                 const obte_material* mat, obte_plan* out);
+obte_status obte_bte_plan_destroy(obte_plan plan);
+/* Device bytes held by the plan (tables) and by one solve's scratch. */
+obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision, int32_t restart,
+                                    int64_t* plan_bytes, int64_t* solve_bytes);
+
+/*
+ * Source iteration to the fixed point (openbte/bte.py:193-256).
+ *   dT0    device [n_elems]  initial lattice temperature (Fourier guess or zeros)
+ *   dT     device [n_elems]  Temperature_BTE
+ *   J      device [n_elems, dim_sigma]  Flux_BTE / 1e9 (W/m/nm), as accumulated by the reference
+ *   K, S   device [n_mfp, n_dir]  per-ordinate kappa and suppression (aux)
+ */
+obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opts, const double* dT0,
+                           double* dT, double* J, double* K, double* S, obte_solve_info* info);
+
+/*
+ * One transport sweep of every ordinate — the per-ordinate solves
+ * A_mq T = B of openbte/bte.py:208-243 followed by the reduction of
+ * openbte/objects.py:86-101 — at a given state.
+ *   u_in   device [n_elems + n_diffuse + n_x]  (DeltaT, T_B, periodic inflow)
+ *   u_out  device, same layout: (DeltaT', T_B', periodic outflow)
+ *   with_source 0/1: include the perturbation (periodic jump, isothermal, nanowire, heat source)
+ */
+obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
+                           int32_t with_source);
+/* Sizes of the state vector pieces: n_elems, n_diffuse, n_x. */
+obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x);
+/*
+ * Sweep schedule of direction q, as built on the host (for bit-exact checks):
+ *   order  host [n_elems]      element processed at each position
+ *   level_ptr host [n_levels+1] (pass NULL to query n_levels via *n_levels)
+ */
+obte_status obte_bte_schedule(obte_plan plan, int32_t q, int64_t* order, int64_t* level_ptr,
+                              int64_t* n_levels, int64_t* n_slots);
+
+/* ---- Fourier (openbte/fourier.py:15-185) -------------------------------- */
+typedef struct {
+  int32_t dim;
+  int64_t n_elems;
+  int64_t n_sides;
+  int32_t elem_nv;
+  const int64_t* side_elem_map;   /* [n_sides, 2]                          */
+  const double* normal_areas;     /* [n_sides, dim]                        */
+  const double* dists;            /* [n_sides, dim]                        */
+  const double* elem_volumes;     /* [n_elems]                             */
+  const double* side_areas;       /* [n_sides]                             */
+  const double* interp_weights;   /* [n_sides]                             */
+  const double* gradient_weights; /* [n_elems, dim, elem_nv]               */
+  const int64_t* elem_side_map;   /* [n_elems, elem_nv]                    */
+  int64_t n_internal;
+  const int64_t* internal;
+  int64_t n_periodic;
+  const int64_t* periodic_sides;
+  const double* periodic_jump;
+  int64_t n_mixed;
+  const int64_t* mixed_sides;
+  const double* mixed_value;
+  const double* mixed_conductance;
+  int32_t contact_kind;           /* OBTE_CONTACT_NONE / PERIODIC / MIXED  */
+  int64_t n_contact;
+  const int64_t* contact_sides;
+  double contact_alpha;           /* jump (periodic) or value (mixed)       */
+  double contact_conductance;     /* mixed contact only                     */
+  double normalization;
+  const double* kappa;            /* [dim, dim] thermal conductivity        */
+  const double* heat_source;      /* [n_elems] or NULL (W/m^3, x1e-18)       */
+  int32_t pin_elem;               /* element pinned to 0 without mixed BCs (10) */
+} obte_fourier_problem;
+
+typedef struct {
+  int32_t max_iter;               /* fourier_max_iter (40)                 */
+  double rtol;                    /* fourier_rtol (1e-8)                   */
+  double cg_rtol;                 /* inner CG tolerance                    */
+  int32_t cg_max_iter;
+} obte_fourier_opts;
+
+typedef struct {
+  double kappa;                   /* diffusive kappa (the value the reference prints) */
+  int32_t n_iter;                 /* deferred-correction iterations        */
+  int32_t n_cg;                   /* total CG iterations                   */
+} obte_fourier_info;
+
+obte_status obte_fourier_plan_create(obte_context ctx, const obte_fourier_problem* prob,
+                                     obte_fourier_plan* out);
+obte_status obte_fourier_plan_destroy(obte_fourier_plan plan);
+/*   T device [n_elems] Temperature_Fourier;  J device [n_elems, dim] Flux_Fourier / 1e9 */
+obte_status obte_fourier_solve(obte_fourier_plan plan, const obte_fourier_opts* opts, double* T,
+                               double* J, obte_fourier_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OBTE_H */

@@ -1,0 +1,185 @@
+// C ABI: context, error reporting, BTE plan lifecycle and queries.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+#include <string>
+
+#include "internal.h"
+
+namespace obte {
+
+static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+obte_status cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  g_last_error = buf;
+  return e == cudaErrorMemoryAllocation ? OBTE_ERR_OOM : OBTE_ERR_CUDA;
+}
+
+void count_launch(int n) { g_launches += n; }
+
+obte_status DevBuf::alloc(size_t n) {
+  release();
+  if (n == 0) n = 16;
+  cudaError_t e = cudaMalloc(&p, n);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+  }
+  bytes = n;
+  return OBTE_OK;
+}
+
+template <typename T>
+obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
+  OBTE_TRY(b.alloc(std::max<size_t>(v.size(), 1) * sizeof(T)));
+  if (!v.empty()) {
+    OBTE_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+    OBTE_CUDA(cudaStreamSynchronize(stream));
+  }
+  return OBTE_OK;
+}
+template obte_status upload<int32_t>(DevBuf&, const std::vector<int32_t>&, cudaStream_t);
+template obte_status upload<int64_t>(DevBuf&, const std::vector<int64_t>&, cudaStream_t);
+template obte_status upload<double>(DevBuf&, const std::vector<double>&, cudaStream_t);
+template obte_status upload<float>(DevBuf&, const std::vector<float>&, cudaStream_t);
+
+}  // namespace obte
+
+using namespace obte;
+
+extern "C" const char* obte_status_string(int status) {
+  switch (status) {
+    case OBTE_OK: return "OK";
+    case OBTE_ERR_BAD_ARG: return "BAD_ARG";
+    case OBTE_ERR_OOM: return "OOM";
+    case OBTE_ERR_ADMISSION: return "ADMISSION_REJECTED";
+    case OBTE_ERR_NOT_CONVERGED: return "NOT_CONVERGED";
+    case OBTE_ERR_CUDA: return "CUDA_ERROR";
+    case OBTE_ERR_CYCLE: return "CYCLE";
+    case OBTE_ERR_UNSUPPORTED: return "UNSUPPORTED";
+    default: return "UNKNOWN";
+  }
+}
+
+extern "C" const char* obte_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int64_t obte_launch_count(void) { return g_launches.load(); }
+
+extern "C" obte_status obte_context_create(int device, void* stream, obte_context* out) {
+  if (!out) { set_error("null out"); return OBTE_ERR_BAD_ARG; }
+  int count = 0;
+  OBTE_CUDA(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) { set_error("bad device index"); return OBTE_ERR_BAD_ARG; }
+  OBTE_CUDA(cudaSetDevice(device));
+  auto* c = new obte_context_s();
+  c->device = device;
+  c->stream = static_cast<cudaStream_t>(stream);
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaGetDeviceProperties", __FILE__, __LINE__); }
+  c->num_sms = prop.multiProcessorCount;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
+  *out = c;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_context_destroy(obte_context ctx) {
+  delete ctx;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_context_set_stream(obte_context ctx, void* stream) {
+  if (!ctx) { set_error("null context"); return OBTE_ERR_BAD_ARG; }
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem* prob, const obte_material* mat,
+                                            obte_plan* out) {
+  if (!out) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  if (ctx) OBTE_CUDA(cudaSetDevice(ctx->device));
+  auto* p = new obte_plan_s();
+  p->ctx = ctx;
+  obte_status st = build_schedule(prob, mat, p->sched);
+  if (st != OBTE_OK) { delete p; return st; }
+  const Schedule& s = p->sched;
+  p->nx = s.x_base[s.n_dir] * s.n_mfp;
+  p->nu = s.n + s.nd + p->nx;
+  // conserved-offset weights over the full state
+  std::vector<double> ell(p->nu, 0.0);
+  double sum = 0;
+  for (int64_t e = 0; e < s.n; ++e) { ell[e] = s.ell_T[e]; sum += s.ell_T[e]; }
+  for (int64_t w = 0; w < s.nd; ++w) { ell[s.n + w] = s.ell_B[w]; sum += s.ell_B[w]; }
+  p->ell_sum = sum;
+  if (!ctx) { *out = p; return OBTE_OK; }   // host-only plan: schedule queries, no device tables
+  std::vector<int32_t> nlev = s.nlev;
+  auto fail = [&](obte_status code) { delete p; return code; };
+  cudaStream_t strm = ctx->stream;
+  if ((st = upload(p->ell, ell, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->x_cell, s.x_cell, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->diffuse_cell, s.diffuse_cell, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->kconst, s.kconst, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->kshift, s.kshift, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->sshift, s.sshift, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->lev_off_dev, s.lev_off, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->nlev_dev, nlev, strm)) != OBTE_OK) return fail(st);
+  if ((st = upload(p->x_base_dev, s.x_base, strm)) != OBTE_OK) return fail(st);
+  *out = p;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_plan_destroy(obte_plan plan) {
+  delete plan;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision, int32_t restart,
+                                               int64_t* plan_bytes, int64_t* solve_bytes) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  const Schedule& s = plan->sched;
+  // table bytes per precision, computed from the host schedule (tables may not be uploaded yet)
+  auto tab = [&](size_t rb) {
+    size_t b = 0;
+    b += (s.cell.size() + s.slot.size() + s.xk.size() + s.wout.size() + s.contact.size() + s.in_idx.size() +
+          s.lev_ptr.size() + s.wo_wall.size()) * 4;
+    b += (s.in_coef.size() + s.D.size() + s.P.size() + s.mfp.size() + s.tco.size() + s.sig.size() +
+          s.wo_gg.size() + s.kcoef.size() + s.scoef.size() + s.hs.size()) * rb;
+    return (int64_t)b;
+  };
+  int64_t pb = (int64_t)plan->nu * 8 + (int64_t)s.x_cell.size() * 4 + (int64_t)s.kconst.size() * 24;
+  if (precision == OBTE_FP64) pb += tab(8);
+  else if (precision == OBTE_FP32) pb += tab(4);
+  else pb += tab(8) + tab(4);
+  if (plan_bytes) *plan_bytes = pb;
+  if (solve_bytes) *solve_bytes = plan->ctx ? solve_scratch_bytes(plan, restart > 0 ? restart : 30) : 0;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  if (n_elems) *n_elems = plan->sched.n;
+  if (n_diffuse) *n_diffuse = plan->sched.nd;
+  if (n_x) *n_x = plan->nx;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_schedule(obte_plan plan, int32_t q, int64_t* order, int64_t* level_ptr,
+                                         int64_t* n_levels, int64_t* n_slots) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  const Schedule& s = plan->sched;
+  if (q < 0 || q >= s.n_dir) { set_error("direction out of range"); return OBTE_ERR_BAD_ARG; }
+  const int nl = s.nlev[q];
+  if (n_levels) *n_levels = nl;
+  if (n_slots) *n_slots = s.nslots[q];
+  if (order)
+    for (int64_t p = 0; p < s.n; ++p) order[p] = s.cell[(size_t)q * s.n + p];
+  if (level_ptr)
+    for (int L = 0; L <= nl; ++L) level_ptr[L] = s.lev_ptr[s.lev_off[q] + L];
+  return OBTE_OK;
+}

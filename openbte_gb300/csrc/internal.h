@@ -1,0 +1,155 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/obte.h"
+
+namespace obte {
+
+// ---- error handling ----------------------------------------------------------
+void set_error(const std::string& msg);
+obte_status cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define OBTE_CUDA(call)                                                         \
+  do {                                                                          \
+    cudaError_t _e = (call);                                                    \
+    if (_e != cudaSuccess) return ::obte::cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define OBTE_TRY(call)                                                          \
+  do {                                                                          \
+    obte_status _s = (call);                                                    \
+    if (_s != OBTE_OK) return _s;                                               \
+  } while (0)
+
+// Count of kernel launches issued by this library (instrumentation for the bench).
+void count_launch(int n = 1);
+
+// ---- device buffer ------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  obte_status alloc(size_t n);
+  template <typename T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+// Upload a host vector into a fresh device buffer (synchronous on `stream`).
+template <typename T>
+obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream);
+
+}  // namespace obte
+
+struct obte_context_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+};
+
+namespace obte {
+
+// Inflow item kinds packed in the top 2 bits of an int32 (index in the low 30 bits).
+enum : int32_t { ITEM_NONE = 0, ITEM_CELL = 1, ITEM_PERIODIC = 2, ITEM_WALL = 3 };
+constexpr int ITEM_SHIFT = 30;
+constexpr int32_t ITEM_MASK = (1 << ITEM_SHIFT) - 1;
+inline int32_t pack_item(int kind, int32_t idx) { return (int32_t)((uint32_t)kind << ITEM_SHIFT) | idx; }
+
+// Host-side sweep schedule: one direction per block of n_elems items (level order).
+struct Schedule {
+  int dim = 2;
+  int nf = 3;                      // inflow slots per element (= sides per element)
+  int64_t n = 0;                   // elements
+  int n_dir = 0, n_mfp = 0, m_pad = 0, n_chunks = 0, ds = 2;
+  int64_t nd = 0;                  // diffuse wall sides (T_B entries)
+  // per direction, per position (n_dir * n)
+  std::vector<int32_t> cell, slot, xk, wout, contact;
+  std::vector<int32_t> in_idx;     // n_dir * n * nf
+  std::vector<double> in_coef;     // n_dir * n * nf
+  std::vector<double> D, P;        // n_dir * n
+  // levels
+  std::vector<int32_t> lev_ptr;    // concatenated level pointers
+  std::vector<int64_t> lev_off;    // [n_dir] start of direction q in lev_ptr
+  std::vector<int32_t> nlev;       // [n_dir]
+  std::vector<int32_t> nslots;     // [n_dir]
+  int max_slots = 0;
+  // periodic interface
+  std::vector<int64_t> x_base;     // [n_dir+1] source-cell offsets
+  std::vector<int32_t> x_cell;     // [x_base[n_dir]] element of each source slot
+  // wall outputs: entries (q, wall) with their re-emission weights
+  std::vector<int32_t> wo_wall;    // [n_wo]
+  std::vector<double> wo_gg;       // [n_wo * m_pad]  (-GG, i.e. >= 0)
+  // contact
+  std::vector<double> kcoef;       // [n_ce * m_pad]
+  std::vector<double> scoef;       // [n_ce]
+  std::vector<double> kconst;      // [n_mfp * n_dir]  alpha-term of K
+  std::vector<double> kshift;      // [n_mfp * n_dir]  dK/d(offset)
+  std::vector<double> sshift;      // [n_mfp * n_dir]  dS/d(offset)
+  // per-ordinate tables (padded)
+  std::vector<double> mfp;         // [m_pad]
+  std::vector<double> tco;         // [n_dir * m_pad]
+  std::vector<double> sig;         // [n_dir * m_pad * ds]
+  std::vector<double> sig_sum;     // [ds] sum over all ordinates of sigma
+  std::vector<double> hs;          // [n] heat_source * coeff (empty if none)
+  // offset weights (energy-conservation left null vector)
+  std::vector<double> ell_T, ell_B;
+  std::vector<int32_t> diffuse_cell;  // [nd] element of each wall side
+};
+
+obte_status build_schedule(const obte_problem* prob, const obte_material* mat, Schedule& s);
+
+// Device copy of the schedule in precision Real.
+struct DevSchedule {
+  bool ready = false;
+  DevBuf cell, slot, xk, wout, contact, in_idx, in_coef, D, P, lev_ptr, mfp, tco, sig, wo_wall,
+      wo_gg, kcoef, scoef, hs;
+  size_t bytes() const;
+};
+
+}  // namespace obte
+
+namespace obte {
+// Solver scratch, kept with the plan and reused across solves with the same restart length.
+struct SolveWork {
+  int64_t nu = 0;
+  int restart = 0;
+  int nb = 1;
+  DevBuf u, Fu, r, V, w, tmp, partial, hdev, Jraw, Kraw, Sraw, delta;
+};
+}  // namespace obte
+
+struct obte_plan_s {
+  obte_context ctx = nullptr;
+  std::unique_ptr<obte::SolveWork> work;
+  obte::Schedule sched;
+  obte::DevSchedule d64, d32;       // FP64 and FP32 tables (built lazily)
+  obte::DevBuf x_cell, diffuse_cell, kconst, kshift, sshift;
+  obte::DevBuf ell;                 // [nu] conserved-offset weights (zero on the periodic part)
+  double ell_sum = 0;               // ell . 1
+  obte::DevBuf lev_off_dev, nlev_dev, x_base_dev;
+  int64_t nx = 0;                   // periodic-inflow unknowns (source cells x n_mfp)
+  int64_t nu = 0;                   // state length
+};
+
+namespace obte {
+// One sweep (sweep.cu). final: also accumulate J (into Jraw), K and S.
+obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
+                         bool final_pass, double* Jraw, double* K, double* S);
+obte_status ensure_tables(obte_plan plan, bool fp32);
+int64_t solve_scratch_bytes(obte_plan plan, int restart);
+}  // namespace obte

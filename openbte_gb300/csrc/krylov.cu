@@ -1,0 +1,426 @@
+// Source iteration driver: GMRES on the sweep fixed point.
+//
+// The reference iterates u <- F(u) with exact per-ordinate solves
+// (openbte/bte.py:196-256), u = (DeltaT, T_B).  Here the state also carries
+// the periodic inflow of every ordinate, so that one sweep evaluates F
+// exactly without a sparse factorisation.  F is affine, F(u) = K u + f, and
+// the fixed point solves (I - K) u = f, done with restarted GMRES (one sweep
+// per Krylov vector, classical Gram-Schmidt with one re-orthogonalisation).
+//
+// I - K is singular along the constant mode (a uniform shift of every
+// temperature is a fixed point of the homogeneous map).  The reference's
+// Jacobi iteration conserves ell.u with ell = (element volumes, wall weights
+// A_w sum_mq t_mq L_m |min(s_q.n_w, 0)|), the left null vector of I - K; the
+// converged state is therefore shifted by a constant so that ell.u equals its
+// value at the initial guess, reproducing the reference's temperature level.
+//
+// Precision modes: FP64 sweeps; FP32 sweeps; FP32 sweeps inside an iterative
+// refinement whose residual F(u) - u is evaluated with FP64 sweeps.  Vectors,
+// reductions and the Hessenberg system are FP64 in every mode.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace obte {
+
+namespace {
+
+constexpr int VT = 256;       // threads per vector block
+constexpr int DOT_TILE = 8;   // vectors per multidot pass
+
+int vec_blocks(const obte_plan plan, int64_t n) {
+  const int64_t want = (n + VT - 1) / VT;
+  const int64_t cap = (int64_t)plan->ctx->num_sms * 4;
+  return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+// partial[b * k + j] = sum over block b's range of V[j*ld + i] * w[i]
+__global__ void __launch_bounds__(VT) multidot_kernel(const double* __restrict__ V, int64_t ld, int k,
+                                                      const double* __restrict__ w, int64_t n,
+                                                      double* __restrict__ partial) {
+  __shared__ double red[VT / 32][DOT_TILE];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int jt = 0; jt < k; jt += DOT_TILE) {
+    double acc[DOT_TILE];
+#pragma unroll
+    for (int t = 0; t < DOT_TILE; ++t) acc[t] = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
+      const double wi = w[i];
+#pragma unroll
+      for (int t = 0; t < DOT_TILE; ++t)
+        if (jt + t < k) acc[t] += V[(int64_t)(jt + t) * ld + i] * wi;
+    }
+#pragma unroll
+    for (int t = 0; t < DOT_TILE; ++t) {
+      double v = acc[t];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][t] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < DOT_TILE && jt + (int)threadIdx.x < k) {
+      double v = 0;
+      for (int w2 = 0; w2 < VT / 32; ++w2) v += red[w2][threadIdx.x];
+      partial[(int64_t)blockIdx.x * k + jt + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// out[j] = sum_b partial[b * k + j], fixed order (deterministic)
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int nb, int k, double* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  double v = 0;
+  for (int b = 0; b < nb; ++b) v += partial[(int64_t)b * k + j];
+  out[j] = v;
+}
+
+// w -= sum_j h[j] V[j]
+__global__ void __launch_bounds__(VT) update_kernel(double* __restrict__ w, const double* __restrict__ V, int64_t ld,
+                                                    int k, const double* __restrict__ h, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
+    double acc = w[i];
+    for (int j = 0; j < k; ++j) acc -= h[j] * V[(int64_t)j * ld + i];
+    w[i] = acc;
+  }
+}
+
+// y = a*x + b*y
+__global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
+// z = a*x + b*y
+__global__ void lincomb_kernel(double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                               double* __restrict__ z, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = a * x[i] + b * y[i];
+}
+
+// u0 = (dT0, dT0[wall elements], dT0[periodic source elements] for every MFP)
+__global__ void init_state_kernel(const double* __restrict__ dT0, int64_t n, const int32_t* __restrict__ wall_cell,
+                                  int64_t nd, const int32_t* __restrict__ x_cell, int64_t nsrc, int n_mfp,
+                                  double* __restrict__ u) {
+  const int64_t total = n + nd + nsrc * n_mfp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    double v;
+    if (i < n) v = dT0[i];
+    else if (i < n + nd) v = dT0[wall_cell[i - n]];
+    else v = dT0[x_cell[(i - n - nd) / n_mfp]];
+    u[i] = v;
+  }
+}
+
+// outputs: dT = Fu_T + c; J = Jraw - dT_in * sig_sum; K = Kraw + kconst + c*kshift; S = Sraw + c*sshift
+__global__ void finalize_kernel(const double* __restrict__ Fu, const double* __restrict__ u, int64_t n, double c,
+                                const double* __restrict__ Jraw, int ds, double s0, double s1, double s2,
+                                const double* __restrict__ Kraw, const double* __restrict__ Sraw,
+                                const double* __restrict__ kconst, const double* __restrict__ kshift,
+                                const double* __restrict__ sshift, int64_t nks, double* __restrict__ dT,
+                                double* __restrict__ J, double* __restrict__ K, double* __restrict__ S) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    if (dT) dT[i] = Fu[i] + c;
+    if (J) {
+      const double ss[3] = {s0, s1, s2};
+      for (int d = 0; d < ds; ++d) J[i * ds + d] = Jraw[i * ds + d] - u[i] * ss[d];
+    }
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nks; i += stride) {
+    if (K) K[i] = Kraw[i] + kconst[i] + c * kshift[i];
+    if (S) S[i] = Sraw[i] + c * sshift[i];
+  }
+}
+
+using Work = SolveWork;
+
+struct Solver {
+  obte_plan plan;
+  Work& wk;
+  int sweeps = 0, sweeps64 = 0;
+  int max_sweeps;
+  cudaStream_t st;
+
+  Solver(obte_plan p, Work& w, int ms) : plan(p), wk(w), max_sweeps(ms), st(p->ctx->stream) {}
+
+  obte_status sweep(bool fp32, const double* in, double* out, bool src, bool fin = false) {
+    ++sweeps;
+    if (!fp32) ++sweeps64;
+    return launch_sweep(plan, fp32, in, out, src, fin, wk.Jraw.as<double>(), wk.Kraw.as<double>(),
+                        wk.Sraw.as<double>());
+  }
+  // h[0..k) = V[0..k)^T w, also copied to host
+  obte_status multidot(const double* V, int k, const double* w, std::vector<double>& h) {
+    const int64_t n = wk.nu;
+    multidot_kernel<<<wk.nb, VT, 0, st>>>(V, n, k, w, n, wk.partial.as<double>());
+    reduce_partials_kernel<<<(k + 63) / 64, 64, 0, st>>>(wk.partial.as<double>(), wk.nb, k, wk.hdev.as<double>());
+    count_launch(2);
+    OBTE_CUDA(cudaGetLastError());
+    h.resize(k);
+    OBTE_CUDA(cudaMemcpyAsync(h.data(), wk.hdev.p, k * sizeof(double), cudaMemcpyDeviceToHost, st));
+    OBTE_CUDA(cudaStreamSynchronize(st));
+    return OBTE_OK;
+  }
+  obte_status norm(const double* x, double& out) {
+    std::vector<double> h;
+    OBTE_TRY(multidot(x, 1, x, h));
+    out = std::sqrt(std::max(h[0], 0.0));
+    return OBTE_OK;
+  }
+  obte_status lincomb(double a, const double* x, double b, const double* y, double* z) {
+    lincomb_kernel<<<wk.nb, VT, 0, st>>>(a, x, b, y, z, wk.nu);
+    count_launch();
+    OBTE_CUDA(cudaGetLastError());
+    return OBTE_OK;
+  }
+  obte_status axpby(double a, const double* x, double b, double* y) {
+    axpby_kernel<<<wk.nb, VT, 0, st>>>(a, x, b, y, wk.nu);
+    count_launch();
+    OBTE_CUDA(cudaGetLastError());
+    return OBTE_OK;
+  }
+
+  // residual of the correction equation (I-K) x = rhs:   r = rhs - x + K x   (rhs == nullptr: r = F(x) - x)
+  obte_status residual(bool fp32, const double* rhs, const double* x, double* r) {
+    if (rhs) {
+      OBTE_TRY(sweep(fp32, x, wk.tmp.as<double>(), false));
+      OBTE_TRY(lincomb(1.0, rhs, -1.0, x, r));
+      OBTE_TRY(axpby(1.0, wk.tmp.as<double>(), 1.0, r));
+    } else {
+      OBTE_TRY(sweep(fp32, x, wk.tmp.as<double>(), true));
+      OBTE_TRY(lincomb(1.0, wk.tmp.as<double>(), -1.0, x, r));
+    }
+    return OBTE_OK;
+  }
+
+  // Restarted GMRES on (I - K) x = rhs, FP64 vectors, sweeps in the given precision.
+  // Stops when the residual norm estimate <= tol_abs or the sweep cap is hit.
+  obte_status gmres(bool fp32, const double* rhs, double* x, double tol_abs, double& res_out, bool& ok) {
+    const int64_t n = wk.nu;
+    const int m = wk.restart;
+    double* V = wk.V.as<double>();
+    double* w = wk.w.as<double>();
+    double* r = wk.r.as<double>();
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), h, h2;
+    ok = false;
+    OBTE_TRY(residual(fp32, rhs, x, r));
+    double beta;
+    OBTE_TRY(norm(r, beta));
+    res_out = beta;
+    while (true) {
+      if (beta <= tol_abs) { ok = true; return OBTE_OK; }
+      if (sweeps >= max_sweeps) return OBTE_OK;
+      OBTE_TRY(lincomb(1.0 / beta, r, 0.0, r, V));
+      std::fill(g.begin(), g.end(), 0.0);
+      g[0] = beta;
+      int j = 0;
+      double est = beta;
+      for (; j < m && sweeps < max_sweeps; ++j) {
+        double* vj = V + (int64_t)j * n;
+        OBTE_TRY(sweep(fp32, vj, wk.tmp.as<double>(), false));
+        OBTE_TRY(lincomb(1.0, vj, -1.0, wk.tmp.as<double>(), w));
+        // classical Gram-Schmidt, two passes
+        OBTE_TRY(multidot(V, j + 1, w, h));
+        OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, h.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+        update_kernel<<<wk.nb, VT, 0, st>>>(w, V, n, j + 1, wk.hdev.as<double>(), n);
+        count_launch();
+        OBTE_TRY(multidot(V, j + 1, w, h2));
+        OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, h2.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+        update_kernel<<<wk.nb, VT, 0, st>>>(w, V, n, j + 1, wk.hdev.as<double>(), n);
+        count_launch();
+        OBTE_CUDA(cudaGetLastError());
+        for (int i = 0; i <= j; ++i) h[i] += h2[i];
+        double hn;
+        OBTE_TRY(norm(w, hn));
+        // Hessenberg column j
+        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = h[i];
+        H[(size_t)(j + 1) * m + j] = hn;
+        for (int i = 0; i < j; ++i) {
+          const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
+          H[(size_t)i * m + j] = cs[i] * a + sn[i] * b;
+          H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+        }
+        const double a = H[(size_t)j * m + j], b = H[(size_t)(j + 1) * m + j];
+        const double rr = std::hypot(a, b);
+        cs[j] = rr > 0 ? a / rr : 1.0;
+        sn[j] = rr > 0 ? b / rr : 0.0;
+        H[(size_t)j * m + j] = rr;
+        H[(size_t)(j + 1) * m + j] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        est = std::fabs(g[j + 1]);
+        if (hn > 0) OBTE_TRY(lincomb(1.0 / hn, w, 0.0, w, V + (int64_t)(j + 1) * n));
+        if (est <= tol_abs || hn == 0) { ++j; break; }
+      }
+      // y = H^-1 g (upper triangular j x j), x += V y
+      std::vector<double> y(j, 0.0);
+      for (int i = j - 1; i >= 0; --i) {
+        double acc = g[i];
+        for (int k = i + 1; k < j; ++k) acc -= H[(size_t)i * m + k] * y[k];
+        y[i] = H[(size_t)i * m + i] != 0 ? acc / H[(size_t)i * m + i] : 0.0;
+      }
+      for (double& v : y) v = -v;   // update_kernel subtracts
+      if (j > 0) {
+        OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, st));
+        update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n);
+        count_launch();
+        OBTE_CUDA(cudaGetLastError());
+      }
+      // true residual for the restart
+      OBTE_TRY(residual(fp32, rhs, x, r));
+      OBTE_TRY(norm(r, beta));
+      res_out = beta;
+      if (beta <= tol_abs) { ok = true; return OBTE_OK; }
+      if (sweeps >= max_sweeps) return OBTE_OK;
+    }
+  }
+};
+
+}  // namespace
+
+static obte_status alloc_work(obte_plan plan, Work& wk, int restart) {
+  const Schedule& s = plan->sched;
+  wk.nu = plan->nu;
+  wk.restart = restart;
+  wk.nb = vec_blocks(plan, wk.nu);
+  const size_t vb = (size_t)wk.nu * sizeof(double);
+  OBTE_TRY(wk.u.alloc(vb));
+  OBTE_TRY(wk.Fu.alloc(vb));
+  OBTE_TRY(wk.r.alloc(vb));
+  OBTE_TRY(wk.w.alloc(vb));
+  OBTE_TRY(wk.tmp.alloc(vb));
+  OBTE_TRY(wk.delta.alloc(vb));
+  OBTE_TRY(wk.V.alloc(vb * (restart + 1)));
+  OBTE_TRY(wk.partial.alloc((size_t)wk.nb * (restart + 1) * sizeof(double)));
+  OBTE_TRY(wk.hdev.alloc((size_t)(restart + 1) * sizeof(double)));
+  OBTE_TRY(wk.Jraw.alloc((size_t)s.n * s.ds * sizeof(double)));
+  OBTE_TRY(wk.Kraw.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+  OBTE_TRY(wk.Sraw.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+  return OBTE_OK;
+}
+
+int64_t solve_scratch_bytes(obte_plan plan, int restart) {
+  const Schedule& s = plan->sched;
+  const int64_t vb = plan->nu * (int64_t)sizeof(double);
+  return vb * (6 + restart + 1) + (int64_t)s.n * s.ds * 8 + 2LL * s.n_mfp * s.n_dir * 8 +
+         (int64_t)plan->ctx->num_sms * 4 * (restart + 1) * 8;
+}
+
+}  // namespace obte
+
+using namespace obte;
+
+extern "C" obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
+                                      int32_t with_source) {
+  if (!plan || !u_in || !u_out) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  if (!plan->ctx) { set_error("host-only plan cannot sweep"); return OBTE_ERR_BAD_ARG; }
+  // scratch for the final-pass outputs is not needed for a plain sweep
+  OBTE_TRY(launch_sweep(plan, precision != OBTE_FP64, u_in, u_out, with_source != 0, false, nullptr, nullptr,
+                        nullptr));
+  OBTE_CUDA(cudaStreamSynchronize(plan->ctx->stream));
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opts, const double* dT0, double* dT,
+                                      double* J, double* K, double* S, obte_solve_info* info) {
+  if (!plan || !opts || !dT0) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  if (!plan->ctx) { set_error("host-only plan cannot solve"); return OBTE_ERR_BAD_ARG; }
+  const Schedule& s = plan->sched;
+  const int prec = opts->precision;
+  if (prec != OBTE_FP64 && prec != OBTE_FP32 && prec != OBTE_FP32_REFINE) {
+    set_error("bad precision"); return OBTE_ERR_BAD_ARG;
+  }
+  const int restart = opts->restart > 0 ? std::min(opts->restart, 200) : 30;
+  const int max_sweeps = opts->max_sweeps > 0 ? opts->max_sweeps : 1000;
+  const double rtol = opts->rtol > 0 ? opts->rtol : 1e-10;
+  cudaStream_t st = plan->ctx->stream;
+  if (!plan->work || plan->work->restart != restart || plan->work->nu != plan->nu) {
+    plan->work.reset(new Work());
+    obte_status ast = alloc_work(plan, *plan->work, restart);
+    if (ast != OBTE_OK) { plan->work.reset(); return ast; }
+  }
+  Work& wk = *plan->work;
+  Solver sv(plan, wk, max_sweeps);
+  double* u = wk.u.as<double>();
+  const int64_t nsrc = s.x_base[s.n_dir];
+  init_state_kernel<<<wk.nb, VT, 0, st>>>(dT0, s.n, plan->diffuse_cell.as<int32_t>(), s.nd,
+                                          plan->x_cell.as<int32_t>(), nsrc, s.n_mfp, u);
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  // conserved ell.u of the initial state (DeltaT and T_B parts)
+  std::vector<double> h;
+  OBTE_TRY(sv.multidot(u, 1, plan->ell.as<double>(), h));
+  const double ell0 = h[0];
+
+  double unorm;
+  OBTE_TRY(sv.norm(u, unorm));
+  double res = 0;
+  bool ok = false;
+  if (prec == OBTE_FP64 || prec == OBTE_FP32) {
+    OBTE_TRY(sv.gmres(prec == OBTE_FP32, nullptr, u, rtol * std::max(unorm, 1e-300), res, ok));
+  } else {
+    const int steps = std::max(1, opts->refine_steps);
+    const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : 1e-5;
+    double* r64 = wk.Fu.as<double>();
+    double* d = wk.delta.as<double>();
+    for (int k = 0; k < steps; ++k) {
+      // FP64 residual r = F(u) - u
+      OBTE_TRY(sv.sweep(false, u, wk.tmp.as<double>(), true));
+      OBTE_TRY(sv.lincomb(1.0, wk.tmp.as<double>(), -1.0, u, r64));
+      double rn;
+      OBTE_TRY(sv.norm(r64, rn));
+      OBTE_TRY(sv.norm(u, unorm));
+      res = rn;
+      if (rn <= rtol * unorm) { ok = true; break; }
+      OBTE_CUDA(cudaMemsetAsync(d, 0, wk.nu * sizeof(double), st));
+      bool iok;
+      double ires;
+      OBTE_TRY(sv.gmres(true, r64, d, std::max(inner * rn, rtol * unorm * 0.5), ires, iok));
+      OBTE_TRY(sv.axpby(1.0, d, 1.0, u));
+      if (sv.sweeps >= max_sweeps) break;
+    }
+  }
+  // final pass: outputs at the fixed point (FP64 unless the FP32 mode was asked for)
+  const bool fin32 = prec == OBTE_FP32;
+  double* Fu = wk.Fu.as<double>();
+  OBTE_TRY(sv.sweep(fin32, u, Fu, true, true));
+  OBTE_TRY(sv.lincomb(1.0, Fu, -1.0, u, wk.r.as<double>()));
+  double rn;
+  OBTE_TRY(sv.norm(wk.r.as<double>(), rn));
+  OBTE_TRY(sv.norm(u, unorm));
+  res = rn / std::max(unorm, 1e-300);
+  ok = res <= rtol * 10;
+  // offset: ell.(Fu + c) = ell0
+  OBTE_TRY(sv.multidot(Fu, 1, plan->ell.as<double>(), h));
+  const double ellF = h[0];
+  const double c = (ell0 - ellF) / plan->ell_sum;
+  const double s0 = s.ds > 0 ? s.sig_sum[0] : 0, s1 = s.ds > 1 ? s.sig_sum[1] : 0, s2 = s.ds > 2 ? s.sig_sum[2] : 0;
+  finalize_kernel<<<wk.nb, VT, 0, st>>>(Fu, u, s.n, c, wk.Jraw.as<double>(), s.ds, s0, s1, s2,
+                                        wk.Kraw.as<double>(), wk.Sraw.as<double>(), plan->kconst.as<double>(),
+                                        plan->kshift.as<double>(), plan->sshift.as<double>(),
+                                        (int64_t)s.n_mfp * s.n_dir, dT, J, K, S);
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  double kappa = 0;
+  if (K) {
+    std::vector<double> kh((size_t)s.n_mfp * s.n_dir);
+    OBTE_CUDA(cudaMemcpyAsync(kh.data(), K, kh.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    OBTE_CUDA(cudaStreamSynchronize(st));
+    for (double v : kh) kappa += v;
+  }
+  OBTE_CUDA(cudaStreamSynchronize(st));
+  if (info) {
+    info->kappa_eff = kappa;
+    info->n_sweeps = sv.sweeps;
+    info->n_sweeps_fp64 = sv.sweeps64;
+    info->residual = res;
+    info->offset = c;
+    info->converged = ok ? 1 : 0;
+  }
+  return ok ? OBTE_OK : OBTE_ERR_NOT_CONVERGED;
+}

@@ -1,0 +1,436 @@
+// Host construction of the per-direction sweep schedule.
+//
+// For every direction q this restates the operator preparation of the
+// reference (openbte/bte.py:47-158) on directed faces, then orders the
+// elements for an upwind sweep:
+//   * directed internal faces carry k = ±(n A)/V (bte.py:48-54); the
+//     coefficient g = s_q·k splits into outflow (D, bte.py:59-62) and inflow;
+//   * inflow across a kept periodic side is *cut*: its upstream value becomes
+//     an interface unknown (periodic source cell) instead of a graph edge;
+//   * the remaining inflow edges form a DAG (checked); elements are layered by
+//     longest path from the sources and ordered by (level, element id);
+//   * each element that feeds a later element gets a slot in a ring of
+//     shared-memory rows that is recycled once its last consumer's level is done.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+
+#include "internal.h"
+
+namespace obte {
+
+namespace {
+
+bool in_range(int64_t v, int64_t n) { return v >= 0 && v < n; }
+
+}  // namespace
+
+obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Schedule& s) {
+  if (!pb || !mt) { set_error("null problem/material"); return OBTE_ERR_BAD_ARG; }
+  const int dim = pb->dim;
+  if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3"); return OBTE_ERR_BAD_ARG; }
+  const int64_t n = pb->n_elems;
+  const int64_t ns = pb->n_sides;
+  if (n <= 0 || ns <= 0 || n >= (1LL << 30)) { set_error("bad element/side count"); return OBTE_ERR_BAD_ARG; }
+  if (pb->elem_nv < dim + 1 || pb->elem_nv > 7) { set_error("bad elem_nv"); return OBTE_ERR_BAD_ARG; }
+  if (!pb->side_elem_map || !pb->normal_areas || !pb->elem_volumes || !pb->internal) {
+    set_error("missing mesh arrays"); return OBTE_ERR_BAD_ARG;
+  }
+  const int n_mfp = mt->n_mfp, n_dir = mt->n_dir;
+  if (n_mfp <= 0 || n_dir <= 0 || mt->dim_dir < dim || mt->dim_sigma < dim || !mt->mfps || !mt->vmfp ||
+      !mt->sigma || !mt->t_coeff) {
+    set_error("bad material"); return OBTE_ERR_BAD_ARG;
+  }
+  if (pb->is_nanowire && mt->dim_dir < 3) { set_error("nanowire needs 3 direction components"); return OBTE_ERR_BAD_ARG; }
+  const int nf = pb->elem_nv;
+  const int64_t* sem = pb->side_elem_map;
+  const double* na = pb->normal_areas;
+  const double* vol = pb->elem_volumes;
+  for (int64_t k = 0; k < 2 * ns; ++k)
+    if (!in_range(sem[k], n)) { set_error("side_elem_map out of range"); return OBTE_ERR_BAD_ARG; }
+  for (int64_t e = 0; e < n; ++e)
+    if (!(vol[e] > 0)) { set_error("non-positive element volume"); return OBTE_ERR_BAD_ARG; }
+
+  s.dim = dim; s.nf = nf; s.n = n; s.n_dir = n_dir; s.n_mfp = n_mfp;
+  s.n_chunks = (n_mfp + 31) / 32; s.m_pad = s.n_chunks * 32; s.ds = mt->dim_sigma;
+  const int m_pad = s.m_pad, ds = s.ds, dd = mt->dim_dir;
+
+  // ---- directed internal faces (bte.py:48-54) ----
+  const int64_t ni = pb->n_internal;
+  std::vector<char> is_per(ns, 0);
+  for (int64_t k = 0; k < pb->n_periodic; ++k) {
+    if (!in_range(pb->periodic_sides[k], ns)) { set_error("periodic side out of range"); return OBTE_ERR_BAD_ARG; }
+    is_per[pb->periodic_sides[k]] = 1;
+  }
+  const int64_t nfd = 2 * ni;
+  std::vector<int32_t> f_row(nfd), f_nb(nfd);
+  std::vector<char> f_cut(nfd);
+  std::vector<double> f_k(nfd * dim);
+  for (int64_t t = 0; t < ni; ++t) {
+    const int64_t sd = pb->internal[t];
+    if (!in_range(sd, ns)) { set_error("internal side out of range"); return OBTE_ERR_BAD_ARG; }
+    const int64_t i = sem[2 * sd], j = sem[2 * sd + 1];
+    if (i == j) { set_error("internal side with a single element"); return OBTE_ERR_BAD_ARG; }
+    f_row[t] = (int32_t)i; f_nb[t] = (int32_t)j; f_cut[t] = is_per[sd];
+    f_row[ni + t] = (int32_t)j; f_nb[ni + t] = (int32_t)i; f_cut[ni + t] = is_per[sd];
+    for (int d = 0; d < dim; ++d) {
+      f_k[t * dim + d] = na[sd * dim + d] / vol[i];
+      f_k[(ni + t) * dim + d] = -na[sd * dim + d] / vol[j];
+    }
+  }
+  // ---- walls ----
+  const int64_t nd = pb->n_diffuse;
+  s.nd = nd;
+  std::vector<int32_t> w_cell(nd);
+  std::vector<double> w_db(nd * dim);
+  for (int64_t w = 0; w < nd; ++w) {
+    const int64_t sd = pb->diffuse_sides[w];
+    if (!in_range(sd, ns)) { set_error("diffuse side out of range"); return OBTE_ERR_BAD_ARG; }
+    const int64_t i = sem[2 * sd];
+    w_cell[w] = (int32_t)i;
+    for (int d = 0; d < dim; ++d) w_db[w * dim + d] = na[sd * dim + d] / vol[i];
+  }
+  s.diffuse_cell = w_cell;
+  // re-emission weights GG (bte.py:73-78): -GG[m,q,w] = Gbp / (-sum_mq Gbm)
+  std::vector<double> gbm_sum(nd, 0.0);
+  auto gb_of = [&](int m, int q, int64_t w) {
+    double v = 0;
+    for (int d = 0; d < dim; ++d) v += mt->sigma[((int64_t)m * n_dir + q) * ds + d] * w_db[w * dim + d];
+    return v;
+  };
+  for (int64_t w = 0; w < nd; ++w) {
+    double acc = 0;
+    for (int m = 0; m < n_mfp; ++m)
+      for (int q = 0; q < n_dir; ++q) acc += std::min(gb_of(m, q, w), 0.0);
+    gbm_sum[w] = acc;
+  }
+  // ---- contact (bte.py:132-158) ----
+  std::vector<int32_t> c_e1, c_e2;
+  std::vector<double> c_na;  // [nc * dim]
+  std::vector<double> c_area;
+  const int ck = pb->contact_kind;
+  const double nrm = pb->normalization;
+  if (ck == OBTE_CONTACT_PERIODIC || ck == OBTE_CONTACT_MIXED) {
+    for (int64_t k = 0; k < pb->n_contact; ++k) {
+      const int64_t sd = pb->contact_sides[k];
+      if (!in_range(sd, ns)) { set_error("contact side out of range"); return OBTE_ERR_BAD_ARG; }
+      c_e1.push_back((int32_t)sem[2 * sd]);
+      c_e2.push_back(ck == OBTE_CONTACT_PERIODIC ? (int32_t)sem[2 * sd + 1] : -1);
+      double a2 = 0;
+      for (int d = 0; d < dim; ++d) { c_na.push_back(na[sd * dim + d]); a2 += na[sd * dim + d] * na[sd * dim + d]; }
+      c_area.push_back(std::sqrt(a2));
+    }
+  } else if (ck != OBTE_CONTACT_NONE && ck != OBTE_CONTACT_NANOWIRE) {
+    set_error("bad contact kind"); return OBTE_ERR_BAD_ARG;
+  }
+  if (ck == OBTE_CONTACT_NANOWIRE && ds < 3) { set_error("nanowire contact needs sigma_z"); return OBTE_ERR_BAD_ARG; }
+  const int64_t nc = (int64_t)c_e1.size();
+  // contact element -> list of (contact side, role) ; role 1 = e1, 2 = e2
+  std::unordered_map<int32_t, std::vector<std::pair<int64_t, int>>> contact_of;
+  for (int64_t k = 0; k < nc; ++k) {
+    contact_of[c_e1[k]].push_back({k, 1});
+    if (c_e2[k] >= 0) contact_of[c_e2[k]].push_back({k, 2});
+  }
+  auto sigma_n = [&](int m, int q, int64_t k) {
+    double v = 0;
+    for (int d = 0; d < dim; ++d) v += mt->sigma[((int64_t)m * n_dir + q) * ds + d] * c_na[k * dim + d];
+    return v;
+  };
+
+  // ---- per-ordinate tables ----
+  s.mfp.assign(m_pad, 0.0);
+  for (int m = 0; m < n_mfp; ++m) s.mfp[m] = mt->mfps[m];
+  s.tco.assign((size_t)n_dir * m_pad, 0.0);
+  s.sig.assign((size_t)n_dir * m_pad * ds, 0.0);
+  s.sig_sum.assign(ds, 0.0);
+  for (int q = 0; q < n_dir; ++q)
+    for (int m = 0; m < n_mfp; ++m) {
+      s.tco[(size_t)q * m_pad + m] = mt->t_coeff[(int64_t)m * n_dir + q];
+      for (int d = 0; d < ds; ++d) {
+        const double v = mt->sigma[((int64_t)m * n_dir + q) * ds + d];
+        s.sig[((size_t)q * m_pad + m) * ds + d] = v;
+        s.sig_sum[d] += v;
+      }
+    }
+  s.hs.clear();
+  if (pb->heat_source) {
+    s.hs.resize(n);
+    for (int64_t e = 0; e < n; ++e) s.hs[e] = pb->heat_source[e] * mt->heat_source_coeff;
+  }
+  s.kconst.assign((size_t)n_mfp * n_dir, 0.0);
+  s.kshift.assign((size_t)n_mfp * n_dir, 0.0);
+  s.sshift.assign((size_t)n_mfp * n_dir, 0.0);
+  // offset weights
+  s.ell_T.assign(vol, vol + n);
+  s.ell_B.assign(nd, 0.0);
+  for (int64_t w = 0; w < nd; ++w) {
+    const int64_t sd = pb->diffuse_sides[w];
+    double acc = 0;
+    for (int q = 0; q < n_dir; ++q) {
+      double sn = 0;
+      for (int d = 0; d < dim; ++d) sn += mt->vmfp[(int64_t)q * dd + d] * na[sd * dim + d];
+      if (sn < 0)
+        for (int m = 0; m < n_mfp; ++m) acc += mt->t_coeff[(int64_t)m * n_dir + q] * mt->mfps[m] * (-sn);
+    }
+    s.ell_B[w] = acc;
+  }
+
+  // ---- per-direction schedule ----
+  s.cell.assign((size_t)n_dir * n, 0);
+  s.slot.assign((size_t)n_dir * n, -1);
+  s.xk.assign((size_t)n_dir * n, -1);
+  s.wout.assign((size_t)n_dir * n, 0);
+  s.contact.assign((size_t)n_dir * n, -1);
+  s.in_idx.assign((size_t)n_dir * n * nf, 0);
+  s.in_coef.assign((size_t)n_dir * n * nf, 0.0);
+  s.D.assign((size_t)n_dir * n, 0.0);
+  s.P.assign((size_t)n_dir * n, 0.0);
+  s.lev_ptr.clear();
+  s.lev_off.assign(n_dir, 0);
+  s.nlev.assign(n_dir, 0);
+  s.nslots.assign(n_dir, 0);
+  s.x_base.assign(n_dir + 1, 0);
+  s.x_cell.clear();
+  s.wo_wall.clear();
+  s.wo_gg.clear();
+  s.kcoef.clear();
+  s.scoef.clear();
+  s.max_slots = 0;
+
+  std::vector<double> D(n), P(n);
+  std::vector<double> g(nfd);
+  std::vector<int32_t> indeg(n), level(n), order(n), pos_of(n), last_use(n), slot_of(n);
+  std::vector<int64_t> out_ptr(n + 1), in_ptr(n + 1);
+  std::vector<int32_t> out_adj, in_face;
+  std::vector<std::vector<int32_t>> wall_in(n);       // inflow walls per element
+  std::vector<int32_t> wall_any;                      // walls with any re-emission, per element lists
+  std::vector<std::vector<int32_t>> wall_out(n);
+
+  for (int q = 0; q < n_dir; ++q) {
+    const double* sq = mt->vmfp + (int64_t)q * dd;
+    std::fill(D.begin(), D.end(), 0.0);
+    std::fill(P.begin(), P.end(), 0.0);
+    // internal faces: outflow into D (bte.py:58-62), same accumulation order as the reference
+    for (int64_t f = 0; f < nfd; ++f) {
+      double v = 0;
+      for (int d = 0; d < dim; ++d) v += sq[d] * f_k[f * dim + d];
+      g[f] = v;
+      if (v > 0) D[f_row[f]] += v;
+    }
+    // diffuse walls (bte.py:80-84)
+    for (int64_t w = 0; w < nd; ++w) {
+      double v = 0;
+      for (int d = 0; d < dim; ++d) v += sq[d] * w_db[w * dim + d];
+      if (v > 0) D[w_cell[w]] += v;
+    }
+    // mixed walls (bte.py:90-96)
+    for (int64_t k = 0; k < pb->n_mixed; ++k) {
+      const int64_t sd = pb->mixed_sides[k];
+      if (!in_range(sd, ns)) { set_error("mixed side out of range"); return OBTE_ERR_BAD_ARG; }
+      const int64_t i = sem[2 * sd];
+      double v = 0;
+      for (int d = 0; d < dim; ++d) v += sq[d] * na[sd * dim + d] / vol[i];
+      if (v < 0) P[i] += -v * pb->mixed_value[k];
+      if (v > 0) D[i] += v;
+    }
+    // periodic jump (bte.py:99-110)
+    for (int64_t k = 0; k < pb->n_periodic; ++k) {
+      const int64_t sd = pb->periodic_sides[k];
+      const int64_t i = sem[2 * sd], j = sem[2 * sd + 1];
+      const double jump = pb->periodic_jump[k];
+      double v1 = 0, v2 = 0;
+      for (int d = 0; d < dim; ++d) {
+        v1 += sq[d] * na[sd * dim + d] / vol[i];
+        v2 += sq[d] * (-na[sd * dim + d]) / vol[j];
+      }
+      P[i] += -std::min(v1, 0.0) * jump;
+      P[j] += std::min(v2, 0.0) * jump;
+    }
+    if (pb->is_nanowire) {
+      for (int64_t e = 0; e < n; ++e) P[e] += -sq[2];
+    }
+
+    // DAG of uncut inflow edges nb -> row
+    std::fill(indeg.begin(), indeg.end(), 0);
+    std::fill(out_ptr.begin(), out_ptr.end(), 0);
+    std::fill(in_ptr.begin(), in_ptr.end(), 0);
+    for (int64_t f = 0; f < nfd; ++f)
+      if (g[f] < 0) {
+        in_ptr[f_row[f] + 1]++;
+        if (!f_cut[f]) { indeg[f_row[f]]++; out_ptr[f_nb[f] + 1]++; }
+      }
+    for (int64_t e = 0; e < n; ++e) { out_ptr[e + 1] += out_ptr[e]; in_ptr[e + 1] += in_ptr[e]; }
+    out_adj.assign(out_ptr[n], 0);
+    in_face.assign(in_ptr[n], 0);
+    {
+      std::vector<int64_t> oc(out_ptr.begin(), out_ptr.end() - 1), ic(in_ptr.begin(), in_ptr.end() - 1);
+      for (int64_t f = 0; f < nfd; ++f)
+        if (g[f] < 0) {
+          in_face[ic[f_row[f]]++] = (int32_t)f;
+          if (!f_cut[f]) out_adj[oc[f_nb[f]]++] = f_row[f];
+        }
+    }
+    // Kahn topological order + longest-path levels
+    std::vector<int32_t> queue;
+    queue.reserve(n);
+    for (int64_t e = 0; e < n; ++e) { level[e] = 0; if (indeg[e] == 0) queue.push_back((int32_t)e); }
+    for (size_t h = 0; h < queue.size(); ++h) {
+      const int32_t c = queue[h];
+      for (int64_t k = out_ptr[c]; k < out_ptr[c + 1]; ++k) {
+        const int32_t d = out_adj[k];
+        level[d] = std::max(level[d], level[c] + 1);
+        if (--indeg[d] == 0) queue.push_back(d);
+      }
+    }
+    if ((int64_t)queue.size() != n) {
+      set_error("upwind graph of direction " + std::to_string(q) + " has a cycle not broken by periodic cuts");
+      return OBTE_ERR_CYCLE;
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return level[a] < level[b]; });
+    int32_t nl = 0;
+    for (int64_t e = 0; e < n; ++e) nl = std::max(nl, level[e] + 1);
+    s.lev_off[q] = (int64_t)s.lev_ptr.size();
+    s.nlev[q] = nl;
+    {
+      std::vector<int32_t> cnt(nl + 1, 0);
+      for (int64_t e = 0; e < n; ++e) cnt[level[e] + 1]++;
+      for (int L = 0; L < nl; ++L) cnt[L + 1] += cnt[L];
+      s.lev_ptr.insert(s.lev_ptr.end(), cnt.begin(), cnt.end());
+    }
+    for (int64_t p = 0; p < n; ++p) pos_of[order[p]] = (int32_t)p;
+
+    // slots: element alive from its level to the last level of its consumers
+    for (int64_t e = 0; e < n; ++e) {
+      int32_t lu = -1;
+      for (int64_t k = out_ptr[e]; k < out_ptr[e + 1]; ++k) lu = std::max(lu, level[out_adj[k]]);
+      last_use[e] = lu;
+      slot_of[e] = -1;
+    }
+    {
+      std::vector<std::vector<int32_t>> release(nl + 1);
+      std::vector<int32_t> free_slots;
+      int32_t next = 0;
+      int64_t p = 0;
+      for (int L = 0; L < nl; ++L) {
+        for (int32_t sl : release[L]) free_slots.push_back(sl);
+        for (; p < n && level[order[p]] == L; ++p) {
+          const int32_t e = order[p];
+          if (last_use[e] < 0) continue;
+          int32_t sl;
+          if (!free_slots.empty()) { sl = free_slots.back(); free_slots.pop_back(); }
+          else sl = next++;
+          slot_of[e] = sl;
+          release[last_use[e] + 1].push_back(sl);
+        }
+      }
+      s.nslots[q] = next;
+      s.max_slots = std::max(s.max_slots, (int)next);
+    }
+
+    // periodic source cells of direction q (sorted unique upstream elements of cut inflow)
+    std::vector<int32_t> src;
+    for (int64_t f = 0; f < nfd; ++f)
+      if (g[f] < 0 && f_cut[f]) src.push_back(f_nb[f]);
+    std::sort(src.begin(), src.end());
+    src.erase(std::unique(src.begin(), src.end()), src.end());
+    s.x_base[q + 1] = s.x_base[q] + (int64_t)src.size();
+    std::unordered_map<int32_t, int32_t> src_idx;
+    for (size_t k = 0; k < src.size(); ++k) { src_idx[src[k]] = (int32_t)k; s.x_cell.push_back(src[k]); }
+
+    // inflow walls / wall outputs per element
+    for (int64_t e = 0; e < n; ++e) { wall_in[e].clear(); wall_out[e].clear(); }
+    for (int64_t w = 0; w < nd; ++w) {
+      double v = 0;
+      for (int d = 0; d < dim; ++d) v += sq[d] * w_db[w * dim + d];
+      if (v < 0) wall_in[w_cell[w]].push_back((int32_t)w);
+      bool any = false;
+      for (int m = 0; m < n_mfp && !any; ++m) any = gb_of(m, q, w) > 0;
+      if (any) wall_out[w_cell[w]].push_back((int32_t)w);
+    }
+
+    // items in level order
+    const size_t base = (size_t)q * n;
+    for (int64_t p = 0; p < n; ++p) {
+      const int32_t e = order[p];
+      const size_t it = base + p;
+      s.cell[it] = e;
+      s.slot[it] = slot_of[e];
+      s.D[it] = D[e];
+      s.P[it] = P[e];
+      int k = 0;
+      for (int64_t t = in_ptr[e]; t < in_ptr[e + 1]; ++t) {
+        const int32_t f = in_face[t];
+        if (k >= nf) { set_error("more inflow faces than element sides"); return OBTE_ERR_BAD_ARG; }
+        if (f_cut[f]) s.in_idx[it * nf + k] = pack_item(ITEM_PERIODIC, src_idx[f_nb[f]]);
+        else s.in_idx[it * nf + k] = pack_item(ITEM_CELL, slot_of[f_nb[f]]);
+        s.in_coef[it * nf + k] = g[f];
+        ++k;
+      }
+      for (int32_t w : wall_in[e]) {
+        if (k >= nf) { set_error("more inflow faces than element sides"); return OBTE_ERR_BAD_ARG; }
+        double v = 0;
+        for (int d = 0; d < dim; ++d) v += sq[d] * w_db[(int64_t)w * dim + d];
+        s.in_idx[it * nf + k] = pack_item(ITEM_WALL, w);
+        s.in_coef[it * nf + k] = v;
+        ++k;
+      }
+      auto si = src_idx.find(e);
+      if (si != src_idx.end()) s.xk[it] = si->second;
+      if (!wall_out[e].empty()) {
+        const int32_t begin = (int32_t)s.wo_wall.size();
+        if (wall_out[e].size() > 7) { set_error("too many wall sides on one element"); return OBTE_ERR_BAD_ARG; }
+        for (int32_t w : wall_out[e]) {
+          s.wo_wall.push_back(w);
+          for (int m = 0; m < m_pad; ++m) {
+            double v = 0;
+            if (m < n_mfp && gbm_sum[w] != 0) v = std::max(gb_of(m, q, w), 0.0) / (-gbm_sum[w]);
+            s.wo_gg.push_back(v);
+          }
+        }
+        s.wout[it] = (begin << 3) | (int32_t)wall_out[e].size();
+      }
+      // contact coefficients
+      if (ck == OBTE_CONTACT_NANOWIRE || contact_of.count(e)) {
+        const int32_t ce = (int32_t)s.scoef.size();
+        double sc = 0;
+        for (int m = 0; m < m_pad; ++m) {
+          double kc = 0;
+          if (m < n_mfp) {
+            if (ck == OBTE_CONTACT_NANOWIRE) {
+              kc = mt->sigma[((int64_t)m * n_dir + q) * ds + 2] * vol[e];
+            } else {
+              for (auto& pr : contact_of[e]) {
+                const double sn = sigma_n(m, q, pr.first);
+                kc += pr.second == 1 ? std::max(sn, 0.0) : std::min(sn, 0.0);
+              }
+            }
+          }
+          s.kcoef.push_back(kc * nrm);
+        }
+        if (ck != OBTE_CONTACT_NANOWIRE)
+          for (auto& pr : contact_of[e])
+            if (pr.second == 1) sc += c_area[pr.first];
+        s.scoef.push_back(sc * nrm);
+        s.contact[it] = ce;
+        for (int m = 0; m < n_mfp; ++m) {
+          s.kshift[(size_t)m * n_dir + q] += s.kcoef[(size_t)ce * m_pad + m];
+          s.sshift[(size_t)m * n_dir + q] += sc * nrm;
+        }
+      }
+    }
+    // alpha term of K (bte.py:243)
+    if (ck == OBTE_CONTACT_PERIODIC || ck == OBTE_CONTACT_MIXED)
+      for (int m = 0; m < n_mfp; ++m) {
+        double acc = 0;
+        for (int64_t k = 0; k < nc; ++k) acc += std::min(sigma_n(m, q, k), 0.0);
+        s.kconst[(size_t)m * n_dir + q] = pb->contact_alpha * acc * nrm;
+      }
+  }
+  return OBTE_OK;
+}
+
+}  // namespace obte

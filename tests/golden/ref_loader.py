@@ -1,0 +1,164 @@
+"""Import the unmodified OpenBTE reference solver in a container without its GUI/IO deps.
+
+Test infrastructure only: used to generate the golden fixtures in this
+directory and by CPU tests that are skipped when the reference checkout is
+absent. It never runs on the product path.
+
+The reference (romanodev/OpenBTE 3.0.16) imports shapely, sqlitedict,
+pickle5, plotly, jax, icosphere, nptyping, matplotlib and cachetools at module
+level, none of which the transport path uses. This loader:
+
+1. registers stub modules for them (a working ``cachetools`` LRU/``cached``);
+2. sets ``scipy.interpolate.interp2d`` (removed in scipy>=1.14; imported at
+   openbte/objects.py:10);
+3. registers a bare ``openbte`` package pointing at the reference sources, which
+   skips ``pkg_resources.require`` in openbte/__init__.py:24;
+4. pads 2-vectors in ``np.cross`` (numpy>=2 rejects them; openbte/mesh.py:186);
+5. re-executes ``Mesh.gradient`` without its dead dense ``(n, n, k)`` allocation
+   (openbte/objects.py:328), which is otherwise 80 GiB at 60k cells;
+6. sets ``sys.dont_write_bytecode`` so nothing is written into the reference tree;
+7. replaces ``utils.run`` (openbte/utils.py:186-219) by an in-process runner with
+   the same ``SharedMemory`` semantics (one worker), or leaves the forking
+   runner in place with ``n_process`` workers.
+"""
+from __future__ import annotations
+
+import importlib
+import inspect
+import os
+import sys
+import textwrap
+import types
+
+import numpy as np
+
+REF_ROOT = os.environ.get("OBTE_REFERENCE", "/root/reference")
+
+
+def available() -> bool:
+    return os.path.isfile(os.path.join(REF_ROOT, "openbte", "bte.py"))
+
+
+def _stub(name, **attrs):
+    m = types.ModuleType(name)
+    for k, v in attrs.items():
+        setattr(m, k, v)
+    sys.modules[name] = m
+    return m
+
+
+class _Anything:
+    def __init__(self, *a, **k):
+        pass
+
+    def __call__(self, *a, **k):
+        return _Anything()
+
+    def __getattr__(self, item):
+        return _Anything()
+
+    def __getitem__(self, item):
+        return _Anything()
+
+
+def _install_stubs():
+    sys.dont_write_bytecode = True
+    for name in ["shapely", "shapely.geometry", "shapely.ops", "shapely.affinity"]:
+        _stub(name, Polygon=_Anything, Point=_Anything, MultiPolygon=_Anything,
+              unary_union=_Anything(), translate=_Anything())
+    _stub("sqlitedict", SqliteDict=_Anything)
+    import pickle
+    sys.modules["pickle5"] = pickle
+    _stub("plotly")
+    _stub("plotly.graph_objs")
+    jax = _stub("jax", numpy=_Anything(), jit=lambda f=None, **k: f, custom_vjp=_Anything,
+                value_and_grad=_Anything())
+    _stub("jax.numpy")
+    jax.numpy = sys.modules["jax.numpy"]
+    _stub("icosphere", icosphere=_Anything())
+    _stub("nptyping", NDArray=_Anything(), Shape=_Anything(), Float=float, Int=int)
+    _stub("matplotlib")
+    _stub("matplotlib.pylab")
+
+    class LRUCache(dict):
+        def __init__(self, maxsize=128, **k):
+            super().__init__()
+            self.maxsize = int(maxsize)
+
+    def cached(cache):
+        def deco(f):
+            def wrapper(*args):
+                if args in cache:
+                    return cache[args]
+                v = f(*args)
+                if len(cache) >= cache.maxsize:
+                    cache.pop(next(iter(cache)))
+                cache[args] = v
+                return v
+            return wrapper
+        return deco
+
+    _stub("cachetools", LRUCache=LRUCache, cached=cached)
+    import scipy.interpolate
+    if not hasattr(scipy.interpolate, "interp2d"):
+        scipy.interpolate.interp2d = None
+
+    _cross = np.cross
+    if not getattr(np.cross, "_obte_padded", False):
+        def cross(a, b, *args, **kw):
+            a = np.asarray(a)
+            b = np.asarray(b)
+            if a.shape[-1] == 2:
+                a = np.concatenate([a, np.zeros(a.shape[:-1] + (1,))], axis=-1)
+            if b.shape[-1] == 2:
+                b = np.concatenate([b, np.zeros(b.shape[:-1] + (1,))], axis=-1)
+            return _cross(a, b, *args, **kw)
+        cross._obte_padded = True
+        np.cross = cross
+
+
+_LOADED = {}
+
+
+def load(in_process: bool = True):
+    """Return the reference modules as a namespace: mesh, bte, fourier, objects, material, utils."""
+    if "ns" in _LOADED:
+        return _LOADED["ns"]
+    if not available():
+        raise RuntimeError(f"reference checkout not found at {REF_ROOT}")
+    _install_stubs()
+    pkg = types.ModuleType("openbte")
+    pkg.__path__ = [os.path.join(REF_ROOT, "openbte")]
+    sys.modules["openbte"] = pkg
+    pkg.Geometry = _Anything
+    utils = importlib.import_module("openbte.utils")
+    objects = importlib.import_module("openbte.objects")
+    pkg.utils = utils
+    pkg.objects = objects
+
+    # Mesh.gradient without the dead dense allocation
+    src = textwrap.dedent(inspect.getsource(objects.Mesh.gradient))
+    src = "\n".join(l for l in src.splitlines() if "A = np.zeros((self.n_elems,self.n_elems" not in l)
+    g = {"np": np, "BoundaryConditions": objects.BoundaryConditions}
+    exec(compile(src, "<Mesh.gradient>", "exec"), g)
+    objects.Mesh.gradient = g["gradient"]
+
+    mesh = importlib.import_module("openbte.mesh")
+    material = importlib.import_module("openbte.material")
+    bte = importlib.import_module("openbte.bte")
+    fourier = importlib.import_module("openbte.fourier")
+
+    if in_process:
+        def run(target, n_tasks, shared_variables={}):
+            sh = objects.SharedMemory(1)
+            for name, value in shared_variables.items():
+                sh[name] = value
+            inds = [np.arange(n) for n in n_tasks]
+            target(sh, inds)
+            return sh
+        utils.run = run
+
+    ns = types.SimpleNamespace(mesh=mesh, bte=bte, fourier=fourier, objects=objects,
+                               material=material, utils=utils)
+    _LOADED["ns"] = ns
+    return ns

@@ -1,0 +1,87 @@
+"""GPU parity: the CUDA sweep and solver against the CPU oracle and the reference's golden vectors."""
+import numpy as np
+import pytest
+
+import bte_oracle
+import sweep_order
+from openbte_gb300 import objects as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _state_from_exact(geo, mat, bcs, dT, TB):
+    """Per-ordinate exact solves (the reference's splu) and the interface values they imply."""
+    ops = bte_oracle.setup_operators(geo, mat, bcs)
+    solver = bte_oracle.OrdinateSolver(geo, np.asarray(mat.mfps, dtype=np.float64), ops)
+    row, nb, k, cut = sweep_order.directed_faces(geo)
+    n = geo.n_elems
+    idf = ops["i_diffuse"]
+    out_T = np.zeros(n)
+    out_B = np.zeros(len(idf))
+    xs = []
+    for q in range(ops["n_angles"]):
+        g = k @ np.asarray(mat.vmfp[q])[: geo.dim]
+        src = np.unique(nb[(g < 0) & cut])
+        Tq = []
+        for m, mfp in enumerate(mat.mfps):
+            B = dT + mfp * ops["perturbation"][q]
+            np.add.at(B, idf, mfp * (-TB * ops["Gbm2"][q]))
+            T = solver.solve(q, m, B)
+            out_T += mat.t_coeff[m, q] * T
+            out_B -= T[idf] * ops["GG"][m, q]
+            Tq.append(T[src])
+        xs.append(np.array(Tq).T.reshape(-1))       # [src, m] -> (k * n_mfp + m)
+    return out_T, out_B, np.concatenate(xs)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("fp32", 2e-5)])
+def test_sweep_equals_exact_ordinate_solves(case, precision, tol):
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.runtime import HostProblem, get_plan
+    import ctypes as C
+    geo, mat, bcs, ek, d = case("a600")
+    rng = np.random.default_rng(0)
+    n = geo.n_elems
+    dT = 0.3 * rng.standard_normal(n)
+    TB = 0.3 * rng.standard_normal(len(geo.side_physical_regions["Boundary"]))
+    refT, refB, x = _state_from_exact(geo, mat, bcs, dT, TB)
+    plan = get_plan(HostProblem(geo, mat, bcs, ek))
+    assert plan.nx == len(x)
+    u = torch.tensor(np.concatenate([dT, TB, x]), dtype=torch.float64, device="cuda")
+    out = torch.zeros_like(u)
+    _lib.check(plan.lib.obte_bte_sweep(plan.handle, _lib.PRECISION[precision], C.c_void_p(u.data_ptr()),
+                                       C.c_void_p(out.data_ptr()), 1), "sweep")
+    o = out.cpu().numpy()
+    scale = max(np.abs(refT).max(), 1.0)
+    np.testing.assert_allclose(o[:n], refT, rtol=0, atol=tol * scale)
+    np.testing.assert_allclose(o[n:n + len(TB)], refB, rtol=0, atol=tol * scale)
+    np.testing.assert_allclose(o[n + len(TB):], x, rtol=0, atol=tol * scale)
+
+
+@pytest.mark.parametrize("name", ["a600", "gray600", "circ1k", "c0_2k"])
+def test_bte_fp64_matches_reference(case, name):
+    from openbte_gb300 import BTE_RTA
+    geo, mat, bcs, ek, d = case(name)
+    f = O.SolverResults(variables={"Temperature_Fourier": {"data": d["fourier_T"]}})
+    r = BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-11, precision="fp64")
+    # FP64 mode: 1e-6 relative on kappa and the temperature field
+    assert abs(r.kappa_eff - d["bte_kappa"]) / abs(d["bte_kappa"]) < 1e-6, (r.kappa_eff, d["bte_kappa"])
+    T = r.variables["Temperature_BTE"]["data"]
+    np.testing.assert_allclose(T, d["bte_T"], rtol=0, atol=1e-6 * np.abs(d["bte_T"]).max())
+    J = r.variables["Flux_BTE"]["data"]
+    np.testing.assert_allclose(J, d["bte_J"], rtol=0, atol=1e-6 * np.abs(d["bte_J"]).max())
+    np.testing.assert_allclose(r.aux["suppression"], d["bte_S"], rtol=0, atol=1e-6 * np.abs(d["bte_S"]).max())
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32_refine", 1e-6), ("fp32", 1e-4)])
+def test_bte_reduced_precision(case, precision, tol):
+    from openbte_gb300 import BTE_RTA
+    geo, mat, bcs, ek, d = case("c0_2k")
+    f = O.SolverResults(variables={"Temperature_Fourier": {"data": d["fourier_T"]}})
+    r = BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-9 if precision != "fp32" else 1e-6,
+                precision=precision)
+    err = abs(r.kappa_eff - d["bte_kappa"]) / abs(d["bte_kappa"])
+    assert err < tol, (precision, err, r.aux)
+    T = r.variables["Temperature_BTE"]["data"]
+    np.testing.assert_allclose(T, d["bte_T"], rtol=0, atol=10 * tol * np.abs(d["bte_T"]).max())
