@@ -192,6 +192,8 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-7)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-sweeps", type=int, default=0,
+                    help="only build the plan and run this many FP32 and FP64 sweeps (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -219,6 +221,16 @@ def main():
     plan = get_plan(hp, local)
     plan_s = time.time() - t0
     n_mfp, n_dir = np.asarray(mat.t_coeff).shape
+    if args.profile_sweeps:
+        u = torch.zeros(plan.nu, dtype=torch.float64, device=dev)
+        uo = torch.zeros_like(u)
+        for prec in ("fp32", "fp64"):
+            for _ in range(args.profile_sweeps):
+                _lib.check(lib.obte_bte_sweep(plan.handle, _lib.PRECISION[prec], C.c_void_p(u.data_ptr()),
+                                              C.c_void_p(uo.data_ptr()), 1), "sweep")
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_sweeps": args.profile_sweeps, "workload": args.workload}))
+        return
     dT0 = torch.zeros(geo.n_elems, dtype=torch.float64, device=dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)

@@ -35,7 +35,8 @@ typedef enum {
   OBTE_ERR_NOT_CONVERGED = 4,     /* iteration cap reached before tolerance    */
   OBTE_ERR_CUDA = 5,              /* a CUDA runtime call failed                */
   OBTE_ERR_CYCLE = 6,             /* upwind graph has a cycle besides periodic */
-  OBTE_ERR_UNSUPPORTED = 7        /* input outside what the kernels implement  */
+  OBTE_ERR_UNSUPPORTED = 7,       /* input outside what the kernels implement  */
+  OBTE_ERR_DEVICE_TIMEOUT = 8     /* a bounded device-side wait gave up        */
 } obte_status;
 
 typedef struct obte_context_s* obte_context;

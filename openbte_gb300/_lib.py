@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libobte_gb300.so")
 
 OBTE_OK = 0
 STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "ADMISSION_REJECTED", 4: "NOT_CONVERGED",
-                5: "CUDA_ERROR", 6: "CYCLE", 7: "UNSUPPORTED"}
+                5: "CUDA_ERROR", 6: "CYCLE", 7: "UNSUPPORTED", 8: "DEVICE_TIMEOUT"}
 OBTE_ERR_NOT_CONVERGED = 4
 OBTE_ERR_ADMISSION = 3
 

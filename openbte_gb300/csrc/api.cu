@@ -63,6 +63,7 @@ extern "C" const char* obte_status_string(int status) {
     case OBTE_ERR_CUDA: return "CUDA_ERROR";
     case OBTE_ERR_CYCLE: return "CYCLE";
     case OBTE_ERR_UNSUPPORTED: return "UNSUPPORTED";
+    case OBTE_ERR_DEVICE_TIMEOUT: return "DEVICE_TIMEOUT";
     default: return "UNKNOWN";
   }
 }
@@ -118,7 +119,6 @@ extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem
   for (int64_t w = 0; w < s.nd; ++w) { ell[s.n + w] = s.ell_B[w]; sum += s.ell_B[w]; }
   p->ell_sum = sum;
   if (!ctx) { *out = p; return OBTE_OK; }   // host-only plan: schedule queries, no device tables
-  std::vector<int32_t> nlev = s.nlev;
   auto fail = [&](obte_status code) { delete p; return code; };
   cudaStream_t strm = ctx->stream;
   if ((st = upload(p->ell, ell, strm)) != OBTE_OK) return fail(st);
@@ -127,8 +127,6 @@ extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem
   if ((st = upload(p->kconst, s.kconst, strm)) != OBTE_OK) return fail(st);
   if ((st = upload(p->kshift, s.kshift, strm)) != OBTE_OK) return fail(st);
   if ((st = upload(p->sshift, s.sshift, strm)) != OBTE_OK) return fail(st);
-  if ((st = upload(p->lev_off_dev, s.lev_off, strm)) != OBTE_OK) return fail(st);
-  if ((st = upload(p->nlev_dev, nlev, strm)) != OBTE_OK) return fail(st);
   if ((st = upload(p->x_base_dev, s.x_base, strm)) != OBTE_OK) return fail(st);
   *out = p;
   return OBTE_OK;

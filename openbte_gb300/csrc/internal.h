@@ -114,10 +114,12 @@ struct Schedule {
 obte_status build_schedule(const obte_problem* prob, const obte_material* mat, Schedule& s);
 
 // Device copy of the schedule in precision Real.
+//   rec      packed per-item records (level order, all directions)
+//   klev_*   kernel level pointers: levels split into units of at most `cap` items
 struct DevSchedule {
   bool ready = false;
-  DevBuf cell, slot, xk, wout, contact, in_idx, in_coef, D, P, lev_ptr, mfp, tco, sig, wo_wall,
-      wo_gg, kcoef, scoef, hs;
+  int cap = 0;
+  DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs;
   size_t bytes() const;
 };
 
@@ -141,7 +143,8 @@ struct obte_plan_s {
   obte::DevBuf x_cell, diffuse_cell, kconst, kshift, sshift;
   obte::DevBuf ell;                 // [nu] conserved-offset weights (zero on the periodic part)
   double ell_sum = 0;               // ell . 1
-  obte::DevBuf lev_off_dev, nlev_dev, x_base_dev;
+  obte::DevBuf x_base_dev;
+  obte::DevBuf err;                 // device error word (bounded waits that gave up)
   int64_t nx = 0;                   // periodic-inflow unknowns (source cells x n_mfp)
   int64_t nu = 0;                   // state length
 };
@@ -151,5 +154,6 @@ namespace obte {
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
                          bool final_pass, double* Jraw, double* K, double* S);
 obte_status ensure_tables(obte_plan plan, bool fp32);
+obte_status check_device_error(obte_plan plan);
 int64_t solve_scratch_bytes(obte_plan plan, int restart);
 }  // namespace obte

@@ -199,8 +199,10 @@ struct Solver {
   }
 
   // Restarted GMRES on (I - K) x = rhs, FP64 vectors, sweeps in the given precision.
-  // Stops when the residual norm estimate <= tol_abs or the sweep cap is hit.
-  obte_status gmres(bool fp32, const double* rhs, double* x, double tol_abs, double& res_out, bool& ok) {
+  // Stops when the residual norm <= max(tol_abs, tol_rel * scale) with scale = max(‖x‖, ‖r‖)
+  // taken at each (re)start, or when the sweep cap is hit.
+  obte_status gmres(bool fp32, const double* rhs, double* x, double tol_rel, double tol_abs, double& res_out,
+                    bool& ok) {
     const int64_t n = wk.nu;
     const int m = wk.restart;
     double* V = wk.V.as<double>();
@@ -213,7 +215,10 @@ struct Solver {
     OBTE_TRY(norm(r, beta));
     res_out = beta;
     while (true) {
-      if (beta <= tol_abs) { ok = true; return OBTE_OK; }
+      double xn;
+      OBTE_TRY(norm(x, xn));
+      const double tol = std::max(tol_abs, tol_rel * std::max(xn, beta));
+      if (beta <= tol) { ok = true; return OBTE_OK; }
       if (sweeps >= max_sweeps) return OBTE_OK;
       OBTE_TRY(lincomb(1.0 / beta, r, 0.0, r, V));
       std::fill(g.begin(), g.end(), 0.0);
@@ -255,7 +260,7 @@ struct Solver {
         g[j] = cs[j] * g[j];
         est = std::fabs(g[j + 1]);
         if (hn > 0) OBTE_TRY(lincomb(1.0 / hn, w, 0.0, w, V + (int64_t)(j + 1) * n));
-        if (est <= tol_abs || hn == 0) { ++j; break; }
+        if (est <= tol || hn == 0) { ++j; break; }
       }
       // y = H^-1 g (upper triangular j x j), x += V y
       std::vector<double> y(j, 0.0);
@@ -275,7 +280,7 @@ struct Solver {
       OBTE_TRY(residual(fp32, rhs, x, r));
       OBTE_TRY(norm(r, beta));
       res_out = beta;
-      if (beta <= tol_abs) { ok = true; return OBTE_OK; }
+      if (beta <= tol) { ok = true; return OBTE_OK; }
       if (sweeps >= max_sweeps) return OBTE_OK;
     }
   }
@@ -323,7 +328,7 @@ extern "C" obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const d
   OBTE_TRY(launch_sweep(plan, precision != OBTE_FP64, u_in, u_out, with_source != 0, false, nullptr, nullptr,
                         nullptr));
   OBTE_CUDA(cudaStreamSynchronize(plan->ctx->stream));
-  return OBTE_OK;
+  return check_device_error(plan);
 }
 
 extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opts, const double* dT0, double* dT,
@@ -362,7 +367,7 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   double res = 0;
   bool ok = false;
   if (prec == OBTE_FP64 || prec == OBTE_FP32) {
-    OBTE_TRY(sv.gmres(prec == OBTE_FP32, nullptr, u, rtol * std::max(unorm, 1e-300), res, ok));
+    OBTE_TRY(sv.gmres(prec == OBTE_FP32, nullptr, u, rtol, 0.0, res, ok));
   } else {
     const int steps = std::max(1, opts->refine_steps);
     const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : 1e-5;
@@ -380,7 +385,7 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
       OBTE_CUDA(cudaMemsetAsync(d, 0, wk.nu * sizeof(double), st));
       bool iok;
       double ires;
-      OBTE_TRY(sv.gmres(true, r64, d, std::max(inner * rn, rtol * unorm * 0.5), ires, iok));
+      OBTE_TRY(sv.gmres(true, r64, d, 0.0, std::max(inner * rn, rtol * unorm * 0.5), ires, iok));
       OBTE_TRY(sv.axpby(1.0, d, 1.0, u));
       if (sv.sweeps >= max_sweeps) break;
     }
@@ -414,6 +419,7 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
     for (double v : kh) kappa += v;
   }
   OBTE_CUDA(cudaStreamSynchronize(st));
+  OBTE_TRY(check_device_error(plan));
   if (info) {
     info->kappa_eff = kappa;
     info->n_sweeps = sv.sweeps;
