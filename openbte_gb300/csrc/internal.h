@@ -116,10 +116,13 @@ obte_status build_schedule(const obte_problem* prob, const obte_material* mat, S
 // Device copy of the schedule in precision Real.
 //   rec      packed per-item records (level order, all directions)
 //   klev_*   kernel level pointers: levels split into units of at most `cap` items
+//   vals     per-sweep (DeltaT + h, perturbation - wall inflow) pairs, level order
+//   si/sr    side table of special elements (periodic inflow, wall/periodic/contact outputs)
 struct DevSchedule {
   bool ready = false;
-  int cap = 0;
-  DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs;
+  int mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0;
+  size_t smem = 0;
+  DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap, Pq, si, sr;
   size_t bytes() const;
 };
 

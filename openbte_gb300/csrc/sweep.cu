@@ -1,34 +1,27 @@
 // Batched upwind transport sweep for sm_103a.
 //
-// One CTA = one direction q x one chunk of 32 mean free paths (lane = MFP).
-// The CTA walks the direction's elements level by level (longest-path layers
-// of the upwind DAG, periodic inflow cut); inside a level every warp takes a
-// contiguous run of elements, all 32 lanes solving an element for their own MFP:
+// One CTA = one direction q x one chunk of `mc` mean free paths.  The CTA walks
+// the direction's elements level by level (longest-path layers of the upwind
+// DAG with periodic inflow cut, split into units of at most 128 elements);
+// within a unit every thread owns one element and loops over the chunk's MFPs:
 //
-//   T_mq[c] = (DeltaT[c] + h[c] + L_m P_q[c] - L_m sum_in g_f T_up) / (1 + L_m D_q[c])
+//   T_mq[c] = (b[c] + L_m (p[c] - sum_in g_f T_up,m)) / (1 + L_m D_q[c])
 //
-// which is the row of A_mq T = B of openbte/bte.py:183-218 for an element whose
-// upwind neighbours are already known.  T_up comes from
-//   - the shared-memory slot of an upstream element (ITEM_CELL),
-//   - the periodic-inflow part of the state vector (ITEM_PERIODIC),
-//   - the wall temperature T_B (ITEM_WALL, openbte/bte.py:200,214).
+// the row of A_mq T = B of openbte/bte.py:183-218 for an element whose upwind
+// neighbours are known; b = DeltaT + heat source, p = perturbation minus the
+// wall inflow g_w T_B (openbte/bte.py:200,211-214).  T_up comes from a ring of
+// shared-memory rows (one row per live upstream element, one column per MFP);
+// a dedicated zero row absorbs absent faces.  Inflow across a cut periodic
+// face reads the periodic-inflow part of the state vector instead.
 //
-// Data movement per level:
-//   - the level's packed item records (geometry, coefficients, slots) arrive in
-//     shared memory by a TMA bulk copy (cp.async.bulk + mbarrier) issued one
-//     level ahead, so the record stream overlaps the previous level's compute;
-//   - DeltaT[c] for a warp's items is gathered by its lanes in one instruction
-//     and handed out by shuffles;
-//   - T stays in a shared-memory ring of slots (recycled after the last
-//     consumer's level); it never goes to HBM.
-// Reductions of openbte/bte.py:222-243 are fused:
-//   DeltaT'[c] += sum_m t_mq T        (warp shuffle, then one FP64 atomic)
-//   T_B'[w]    += sum_m (-GG) T       (walls)
-//   x'         = T at periodic source elements (interface unknowns)
-//   final pass: J += sum_m sigma_mq T, K_mq / S_mq in registers per lane.
+// Data movement per unit: the packed element records and the per-sweep values
+// (b, p) arrive in shared memory by TMA bulk copies (cp.async.bulk + mbarrier)
+// issued one unit ahead.  T never goes to HBM.  Reductions of
+// openbte/bte.py:222-243 are register accumulations over the MFP loop followed
+// by one FP64 atomic per element (DeltaT', T_B', J) or per MFP (K, S).
 // Every mbarrier wait is bounded; on timeout the CTA raises the device error
-// word, stops using the records, waits (bounded) for its own copy in flight
-// and leaves at the next block-wide barrier.
+// word, stops using the buffers, waits (bounded) for its copy in flight and
+// leaves at the next block-wide barrier.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,41 +31,93 @@
 
 namespace obte {
 
-// ---- packed item records ---------------------------------------------------------
-// FP32: 16 words (64 B); FP64: 24 words (96 B). Both multiples of 16 B (TMA).
-//   w0 cell  w1 slot  w2 xk  w3 wout  w4 contact  w5..w8 in_idx[4]
-//   FP32: w9..w12 in_coef[4]  w13 D  w14 P  w15 pad
-//   FP64: w9 pad, w10..w17 in_coef[4], w18..w19 D, w20..w21 P, w22..w23 pad
-template <typename Real> struct RecLayout;
-template <> struct RecLayout<float> { static constexpr int W = 16; };
-template <> struct RecLayout<double> { static constexpr int W = 24; };
+static constexpr int kUnit = 128;      // elements per level unit = threads per CTA
+
+// ---- packed element records -------------------------------------------------------
+// FP32: 12 words (48 B) : cell slot special s0 s1 s2 s3 | c0 c1 c2 c3 D
+// FP64: 20 words (80 B) : cell slot special s0 s1 s2 s3 pad | c0 c1 c2 c3 D (8 B each) | pad
+template <typename Real> struct Rec;
+template <> struct Rec<float> { static constexpr int W = 12, COEF = 7, D = 11; };
+template <> struct Rec<double> { static constexpr int W = 20, COEF = 8, D = 16; };
+
+// special-item table: int part and real part per entry
+//   si: xk wout contact nper p0 p1 nwall w0 w1 w2   (10 ints)
+//   sr: pc0 pc1 wc0 wc1 wc2                           (5 reals)
+static constexpr int SI = 10, SR = 5;
+
+struct Packed {
+  std::vector<int32_t> rec, cellmap, si;
+  std::vector<double> P, sr;
+};
 
 template <typename Real>
-static void pack_records(const Schedule& s, std::vector<int32_t>& out) {
-  constexpr int W = RecLayout<Real>::W;
+static obte_status pack(const Schedule& s, int zero_slot, Packed& pk) {
+  constexpr int W = Rec<Real>::W;
   const size_t total = (size_t)s.n_dir * s.n;
-  out.assign(total * W, 0);
+  pk.rec.assign(total * W, 0);
+  pk.cellmap.assign(total, 0);
+  pk.P.assign(total, 0.0);
+  pk.si.clear();
+  pk.sr.clear();
   for (size_t it = 0; it < total; ++it) {
-    int32_t* r = out.data() + it * W;
-    r[0] = s.cell[it]; r[1] = s.slot[it]; r[2] = s.xk[it]; r[3] = s.wout[it]; r[4] = s.contact[it];
-    for (int f = 0; f < 4; ++f) r[5 + f] = f < s.nf ? s.in_idx[it * s.nf + f] : 0;
+    int32_t* r = pk.rec.data() + it * W;
+    r[0] = s.cell[it];
+    r[1] = s.slot[it];
+    r[2] = -1;
+    pk.cellmap[it] = s.cell[it];
+    pk.P[it] = s.P[it];
+    int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0, 0, 0};
+    double sr[SR] = {0, 0, 0, 0, 0};
+    bool special = s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0;
+    double coef[4] = {0, 0, 0, 0};
+    int32_t slot_in[4] = {zero_slot, zero_slot, zero_slot, zero_slot};
+    int k = 0;
+    for (int f = 0; f < s.nf; ++f) {
+      const int32_t code = s.in_idx[it * s.nf + f];
+      const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
+      const int32_t idx = code & ITEM_MASK;
+      const double g = s.in_coef[it * s.nf + f];
+      if (kind == ITEM_CELL) {
+        slot_in[k] = idx;
+        coef[k] = g;
+        ++k;
+      } else if (kind == ITEM_PERIODIC) {
+        if (si[3] >= 2) { set_error("more than two periodic inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
+        si[4 + si[3]] = idx;
+        sr[si[3]] = g;
+        si[3]++;
+        special = true;
+      } else if (kind == ITEM_WALL) {
+        if (si[6] >= 3) { set_error("more than three wall inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
+        si[7 + si[6]] = idx;
+        sr[2 + si[6]] = g;
+        si[6]++;
+        special = true;
+      }
+    }
+    for (int f = 0; f < 4; ++f) r[3 + f] = slot_in[f];
+    if (special) {
+      r[2] = (int32_t)(pk.si.size() / SI);
+      pk.si.insert(pk.si.end(), si, si + SI);
+      pk.sr.insert(pk.sr.end(), sr, sr + SR);
+    }
     if (sizeof(Real) == 4) {
       for (int f = 0; f < 4; ++f) {
-        float v = f < s.nf ? (float)s.in_coef[it * s.nf + f] : 0.f;
-        std::memcpy(&r[9 + f], &v, 4);
+        float v = (float)coef[f];
+        std::memcpy(&r[Rec<float>::COEF + f], &v, 4);
       }
-      float d = (float)s.D[it], p = (float)s.P[it];
-      std::memcpy(&r[13], &d, 4);
-      std::memcpy(&r[14], &p, 4);
+      float d = (float)s.D[it];
+      std::memcpy(&r[Rec<float>::D], &d, 4);
     } else {
-      for (int f = 0; f < 4; ++f) {
-        double v = f < s.nf ? s.in_coef[it * s.nf + f] : 0.0;
-        std::memcpy(&r[10 + 2 * f], &v, 8);
-      }
-      std::memcpy(&r[18], &s.D[it], 8);
-      std::memcpy(&r[20], &s.P[it], 8);
+      for (int f = 0; f < 4; ++f) std::memcpy(&r[Rec<double>::COEF + 2 * f], &coef[f], 8);
+      std::memcpy(&r[Rec<double>::D], &s.D[it], 8);
     }
   }
+  if (pk.si.empty()) {
+    pk.si.assign(SI, 0);
+    pk.sr.assign(SR, 0.0);
+  }
+  return OBTE_OK;
 }
 
 // ---- PTX helpers (TMA bulk copy + mbarrier) -----------------------------------------
@@ -109,46 +154,68 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false if the phase did not complete within the iteration cap.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
   for (int i = 0; i < (1 << 22); ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
 
+// ---- per-sweep values: b = DeltaT + h, p = P - sum_walls g_w T_B ------------------
+template <typename Real>
+__global__ void sweep_values_kernel(const int32_t* __restrict__ cellmap, const double* __restrict__ Pq,
+                                    const int32_t* __restrict__ rec, int W, const int32_t* __restrict__ si,
+                                    const Real* __restrict__ sr, const double* __restrict__ u_in, int64_t n,
+                                    const double* __restrict__ hs, int with_src, int64_t total, Real* __restrict__ vals) {
+  const double* TB = u_in + n;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < total; it += (int64_t)gridDim.x * blockDim.x) {
+    const int c = cellmap[it];
+    double b = u_in[c];
+    double pp = 0;
+    if (with_src) {
+      if (hs) b += hs[c];
+      pp = Pq[it];
+    }
+    const int sp = rec[it * W + 2];
+    if (sp >= 0) {
+      const int32_t* s = si + (int64_t)sp * SI;
+      const Real* r = sr + (int64_t)sp * SR;
+      for (int k = 0; k < s[6]; ++k) pp -= (double)r[2 + k] * TB[s[7 + k]];
+    }
+    vals[2 * it] = (Real)b;
+    vals[2 * it + 1] = (Real)pp;
+  }
+}
+
 template <typename Real>
 struct SweepParams {
   int64_t n;
   int64_t nd;
-  int n_mfp, m_pad, n_chunks, n_dir, ds, cap;
-  const int32_t* __restrict__ rec;       // packed records
-  const int32_t* __restrict__ lev_ptr;   // kernel level units
+  int n_mfp, n_dir, ds;
+  int mc, mcp, n_chunks;   // MFPs per chunk, padded to 4, chunks per direction
+  int zero_slot;           // ring rows: zero_slot + 1
+  const int32_t* __restrict__ rec;
+  const Real* __restrict__ vals;
+  const int32_t* __restrict__ lev_ptr;
   const int64_t* __restrict__ lev_off;
   const int32_t* __restrict__ nlev;
   const int64_t* __restrict__ x_base;
+  const int32_t* __restrict__ si;
+  const Real* __restrict__ sr;
   const int32_t* __restrict__ wo_wall;
-  const Real* __restrict__ mfp;
-  const Real* __restrict__ tco;
-  const Real* __restrict__ sig;
-  const Real* __restrict__ wo_gg;
-  const Real* __restrict__ kcoef;
-  const Real* __restrict__ scoef;
-  const Real* __restrict__ hs;
+  const Real* __restrict__ mfp;    // [n_mfp]
+  const Real* __restrict__ tco;    // [n_dir * m_pad]
+  const Real* __restrict__ sig;    // [n_dir * m_pad * ds]
+  const Real* __restrict__ wo_gg;  // [n_wo * m_pad]
+  const Real* __restrict__ kcoef;  // [n_ce * m_pad]
+  const Real* __restrict__ scoef;  // [n_ce]
+  int m_pad;
   const double* __restrict__ u_in;
   double* __restrict__ u_out;
   double* __restrict__ Jraw;
   double* __restrict__ K;
   double* __restrict__ S;
   int* __restrict__ err;
-  int with_src;
 };
-
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 template <typename Real>
 __device__ __forceinline__ Real rec_real(const int32_t* r, int word);
@@ -161,52 +228,89 @@ __device__ __forceinline__ double rec_real<double>(const int32_t* r, int word) {
   return __hiloint2double(r[word + 1], r[word]);
 }
 
-template <typename Real, int NF, bool FINAL>
-__global__ void __launch_bounds__(256) bte_sweep_kernel(const SweepParams<Real> p) {
-  constexpr int W = RecLayout<Real>::W;
-  constexpr bool F32 = sizeof(Real) == 4;
-  constexpr int OFF_COEF = F32 ? 9 : 10;
-  constexpr int STEP = F32 ? 1 : 2;
-  constexpr int OFF_D = F32 ? 13 : 18;
-  constexpr int OFF_P = F32 ? 14 : 20;
+// 1/x: FP32 hardware reciprocal; FP64 refines an FP32 seed with two Newton-Raphson steps
+// (r <- r (2 - x r)), each squaring the relative error (2^-22 -> 2^-44 -> below 2^-53).
+__device__ __forceinline__ float recip(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double recip(double x) {
+  double r = (double)__fdividef(1.0f, (float)x);
+  r = r * (2.0 - x * r);
+  r = r * (2.0 - x * r);
+  return r;
+}
 
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);            // 2 mbarriers
-  int* s_abort = reinterpret_cast<int*>(smem_raw + 16);             // [2], by level parity
-  int32_t* recbuf0 = reinterpret_cast<int32_t*>(smem_raw + 128);
-  int32_t* recbuf1 = recbuf0 + (size_t)p.cap * W;
-  Real* buf = reinterpret_cast<Real*>(recbuf1 + (size_t)p.cap * W);  // T ring [slots][32]
+// Shared memory layout (bytes):
+//   [0,16) mbarriers  [16,24) abort flags  [128, ...) rec0 rec1 vals0 vals1 | lam t | sig | K S | ring
+template <typename Real>
+struct SmemLayout {
+  size_t rec0, rec1, val0, val1, lam, tco, sig, kacc, sacc, ring, total;
+  __host__ __device__ SmemLayout(int mcp, int ds, int rows) {
+    constexpr int W = Rec<Real>::W;
+    size_t o = 128;
+    rec0 = o; o += (size_t)kUnit * W * 4;
+    rec1 = o; o += (size_t)kUnit * W * 4;
+    val0 = o; o += (size_t)(kUnit + 2) * 2 * sizeof(Real);
+    val1 = o; o += (size_t)(kUnit + 2) * 2 * sizeof(Real);
+    o = (o + 15) & ~(size_t)15;
+    lam = o; o += (size_t)mcp * sizeof(Real);
+    tco = o; o += (size_t)mcp * sizeof(Real);
+    sig = o; o += (size_t)mcp * 3 * sizeof(Real);
+    kacc = o; o += (size_t)mcp * sizeof(Real);
+    sacc = o; o += (size_t)mcp * sizeof(Real);
+    o = (o + 15) & ~(size_t)15;
+    ring = o; o += (size_t)mcp * rows * sizeof(Real);
+    total = o;
+  }
+};
+
+template <typename Real, int NF, bool FINAL>
+__global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real> p) {
+  constexpr int W = Rec<Real>::W;
+  constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int rows = p.zero_slot + 1;
+  const SmemLayout<Real> L(p.mcp, p.ds, rows);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  int* s_abort = reinterpret_cast<int*>(smem + 16);
+  int32_t* const recb0 = reinterpret_cast<int32_t*>(smem + L.rec0);
+  int32_t* const recb1 = reinterpret_cast<int32_t*>(smem + L.rec1);
+  unsigned char* const valb0 = smem + L.val0;
+  unsigned char* const valb1 = smem + L.val1;
+  Real* s_lam = reinterpret_cast<Real*>(smem + L.lam);
+  Real* s_t = reinterpret_cast<Real*>(smem + L.tco);
+  Real* s_sig = reinterpret_cast<Real*>(smem + L.sig);
+  Real* s_k = reinterpret_cast<Real*>(smem + L.kacc);
+  Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
+  Real* ring = reinterpret_cast<Real*>(smem + L.ring);   // [mcp][rows]
 
   const int q = blockIdx.x / p.n_chunks;
   const int chunk = blockIdx.x - q * p.n_chunks;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
-  const int m = chunk * 32 + lane;
-  const bool active = m < p.n_mfp;
-
-  const Real lam = p.mfp[m];
-  const Real tq = p.tco[(int64_t)q * p.m_pad + m];
-  Real sg0 = 0, sg1 = 0, sg2 = 0;
-  if (FINAL) {
-    const Real* sp = p.sig + ((int64_t)q * p.m_pad + m) * p.ds;
-    sg0 = sp[0];
-    if (p.ds > 1) sg1 = sp[1];
-    if (p.ds > 2) sg2 = sp[2];
-  }
-  const double* __restrict__ dT = p.u_in;
-  const double* __restrict__ TB = p.u_in + p.n;
+  const int m0 = chunk * p.mc;
+  const int mc = min(p.mc, p.n_mfp - m0);
+  const int tid = threadIdx.x;
+  const int32_t* __restrict__ lev = p.lev_ptr + p.lev_off[q];
+  const int nlev = p.nlev[q];
+  const int32_t* __restrict__ rec_q = p.rec + (int64_t)q * p.n * W;
+  // values: absolute byte offsets from the (256-B aligned) array base keep every TMA window 16-B aligned
+  const unsigned char* __restrict__ val_base = reinterpret_cast<const unsigned char*>(p.vals);
+  const int64_t val_q0 = (int64_t)q * p.n * VB;
+  const int64_t xq = p.x_base[q];
   const double* __restrict__ X = p.u_in + p.n + p.nd;
   double* __restrict__ dT_out = p.u_out;
   double* __restrict__ TB_out = p.u_out + p.n;
   double* __restrict__ X_out = p.u_out + p.n + p.nd;
-  const int64_t xq = p.x_base[q];
-  const int32_t* __restrict__ lev = p.lev_ptr + p.lev_off[q];
-  const int nlev = p.nlev[q];
-  const int32_t* __restrict__ rec_q = p.rec + (int64_t)q * p.n * W;
-  const bool src = p.with_src != 0;
 
-  if (threadIdx.x == 0) {
+  // per-chunk ordinate data; padded MFPs get L = t = 0 (they compute a harmless T = b)
+  for (int j = tid; j < p.mcp; j += blockDim.x) {
+    const bool ok = j < mc;
+    s_lam[j] = ok ? p.mfp[m0 + j] : Real(0);
+    s_t[j] = ok ? p.tco[(int64_t)q * p.m_pad + m0 + j] : Real(0);
+    for (int d = 0; d < 3; ++d)
+      s_sig[j * 3 + d] = (ok && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m0 + j) * p.ds + d] : Real(0);
+    s_k[j] = 0;
+    s_s[j] = 0;
+  }
+  for (int i = tid; i < p.mcp * rows; i += blockDim.x) ring[i] = Real(0);
+  if (tid == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     s_abort[0] = 0;
@@ -214,126 +318,119 @@ __global__ void __launch_bounds__(256) bte_sweep_kernel(const SweepParams<Real> 
     fence_mbar_init();
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned bytes = (unsigned)(lev[1] - lev[0]) * W * 4u;
-    mbar_expect_tx(&bars[0], bytes);
-    tma_load_1d(recbuf0, rec_q + (int64_t)lev[0] * W, bytes, &bars[0]);
-  }
 
-  Real kacc = 0, sacc = 0;
-  bool issued_next = false;
-  for (int L = 0; L < nlev; ++L) {
-    const int b = lev[L];
-    const int e = lev[L + 1];
-    const int cur = L & 1;
-    issued_next = false;
-    if (threadIdx.x == 0 && L + 1 < nlev) {
-      // buffer cur^1 was last read during level L-1, finished at the barrier below
-      fence_proxy_async();
-      const unsigned bytes = (unsigned)(lev[L + 2] - lev[L + 1]) * W * 4u;
-      mbar_expect_tx(&bars[cur ^ 1], bytes);
-      tma_load_1d(cur ? recbuf0 : recbuf1, rec_q + (int64_t)lev[L + 1] * W, bytes, &bars[cur ^ 1]);
-      issued_next = true;
-    }
-    const bool ready = mbar_wait_bounded(&bars[cur], (unsigned)(L >> 1) & 1u);
+  // TMA of unit u into buffer u&1: records [a, e) and values [a, e) (values 16-B aligned window)
+  auto issue = [&](int u) {
+    const int a = lev[u], e = lev[u + 1];
+    const unsigned rbytes = (unsigned)(e - a) * W * 4u;
+    const int64_t vb0 = (val_q0 + (int64_t)a * VB) & ~(int64_t)15;
+    const int64_t vb1 = (val_q0 + (int64_t)e * VB + 15) & ~(int64_t)15;
+    const unsigned vbytes = (unsigned)(vb1 - vb0);
+    uint64_t* bar = &bars[u & 1];
+    fence_proxy_async();
+    mbar_expect_tx(bar, rbytes + vbytes);
+    tma_load_1d((u & 1) ? recb1 : recb0, rec_q + (int64_t)a * W, rbytes, bar);
+    tma_load_1d((u & 1) ? valb1 : valb0, val_base + vb0, vbytes, bar);
+  };
+  if (tid == 0) issue(0);
+
+  for (int u = 0; u < nlev; ++u) {
+    const int cur = u & 1;
+    const int a = lev[u], e = lev[u + 1];
+    const bool next = u + 1 < nlev;
+    if (tid == 0 && next) issue(u + 1);
+    const bool ready = mbar_wait_bounded(&bars[cur], (unsigned)(u >> 1) & 1u);
     if (!ready) {
       s_abort[cur] = 1;
-      if (lane == 0) atomicOr(p.err, 1);
-    } else {
-      const int32_t* recs = cur ? recbuf1 : recbuf0;
-      const int width = e - b;
-      const int ipw = (width + nw - 1) / nw;
-      const int i0 = warp * ipw;
-      const int cnt = max(0, min(ipw, width - i0));
-      // gather DeltaT (+ heat source) of this warp's items, one lane per item
-      Real my_dT = 0;
-      if (lane < cnt) {
-        const int c = recs[(i0 + lane) * W];
-        my_dT = (Real)dT[c];
-        if (src && p.hs) my_dT += p.hs[c];
+      atomicOr(p.err, 1);
+    } else if (tid < e - a) {
+      const int32_t* r = (cur ? recb1 : recb0) + tid * W;
+      const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
+      const Real* v = reinterpret_cast<const Real*>(cur ? valb1 : valb0) + 2 * (voff + tid);
+      const Real b = v[0], pw = v[1];
+      const int c = r[0], so = r[1], sp = r[2];
+      const int s0 = r[3], s1 = r[4], s2 = r[5], s3 = r[6];
+      const Real c0 = rec_real<Real>(r, Rec<Real>::COEF);
+      const Real c1 = rec_real<Real>(r, Rec<Real>::COEF + (W == 12 ? 1 : 2));
+      const Real c2 = rec_real<Real>(r, Rec<Real>::COEF + (W == 12 ? 2 : 4));
+      const Real c3 = rec_real<Real>(r, Rec<Real>::COEF + (W == 12 ? 3 : 6));
+      const Real D = rec_real<Real>(r, Rec<Real>::D);
+      // special element: periodic inflow / outputs
+      int xk = -1, wo = 0, ce = -1, np = 0, p0 = 0, p1 = 0;
+      Real pc0 = 0, pc1 = 0;
+      if (sp >= 0) {
+        const int32_t* si = p.si + (int64_t)sp * SI;
+        const Real* sr = p.sr + (int64_t)sp * SR;
+        xk = si[0]; wo = si[1]; ce = si[2]; np = si[3]; p0 = si[4]; p1 = si[5];
+        pc0 = sr[0]; pc1 = sr[1];
       }
-      for (int k = 0; k < cnt; ++k) {
-        const int32_t* r = recs + (i0 + k) * W;
-        const int c = r[0];
-        const int sl = r[1];
-        const int xk = r[2];
-        const int wo = r[3];
-        const int ce = r[4];
-        Real acc = __shfl_sync(0xffffffffu, my_dT, k);
-        if (src) acc += lam * rec_real<Real>(r, OFF_P);
+      // accumulate in the sweep precision (FP64 conversions are slow on this part); one FP64 atomic each
+      Real dacc = 0, j0 = 0, j1 = 0, j2 = 0, w0 = 0, w1 = 0, w2 = 0;
+      const int wb = wo >> 3, wn = wo & 7;
+      for (int mb = 0; mb < p.mcp; mb += 4) {
+        Real v0[4], v1[4], v2[4], v3[4];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          const int32_t code = r[5 + f];
-          const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
-          if (kind == ITEM_NONE) continue;
-          const int idx = code & ITEM_MASK;
-          Real v;
-          if (kind == ITEM_CELL) {
-            v = buf[idx * 32 + lane];
-          } else if (kind == ITEM_PERIODIC) {
-            v = active ? (Real)X[(xq + idx) * p.n_mfp + m] : Real(0);
-          } else {
-            v = (Real)TB[idx];
-          }
-          acc -= lam * rec_real<Real>(r, OFF_COEF + STEP * f) * v;
+        for (int j = 0; j < 4; ++j) {
+          const Real* row = ring + (size_t)(mb + j) * rows;
+          v0[j] = row[s0];
+          v1[j] = row[s1];
+          v2[j] = row[s2];
+          v3[j] = NF > 3 ? row[s3] : Real(0);
         }
-        const Real T = acc / (Real(1) + lam * rec_real<Real>(r, OFF_D));
-        if (sl >= 0) buf[sl * 32 + lane] = T;
-
-        const Real rs = warp_sum(tq * T);
-        if (lane == 0) atomicAdd(&dT_out[c], (double)rs);
-        if (xk >= 0 && active) X_out[(xq + xk) * p.n_mfp + m] = (double)T;
-        if (wo) {
-          const int wb = wo >> 3, wn = wo & 7;
-          for (int j = 0; j < wn; ++j) {
-            const Real rw = warp_sum(p.wo_gg[(int64_t)(wb + j) * p.m_pad + m] * T);
-            if (lane == 0) atomicAdd(&TB_out[p.wo_wall[wb + j]], (double)rw);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int mm = mb + j;
+          const Real lam = s_lam[mm];
+          Real s = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
+          if (NF > 3) s += c3 * v3[j];
+          if (np) {
+            if (mm < mc) {
+              s += pc0 * (Real)X[(xq + p0) * p.n_mfp + m0 + mm];
+              if (np > 1) s += pc1 * (Real)X[(xq + p1) * p.n_mfp + m0 + mm];
+            }
           }
-        }
-        if (FINAL) {
-          const Real r0 = warp_sum(sg0 * T);
-          if (lane == 0) atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)r0);
-          if (p.ds > 1) {
-            const Real r1 = warp_sum(sg1 * T);
-            if (lane == 0) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)r1);
+          const Real T = (b + lam * (pw - s)) * recip(Real(1) + lam * D);
+          if (so >= 0) ring[(size_t)mm * rows + so] = T;
+          dacc += s_t[mm] * T;
+          if (FINAL) {
+            j0 += s_sig[mm * 3] * T;
+            j1 += s_sig[mm * 3 + 1] * T;
+            j2 += s_sig[mm * 3 + 2] * T;
           }
-          if (p.ds > 2) {
-            const Real r2 = warp_sum(sg2 * T);
-            if (lane == 0) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)r2);
-          }
-          if (ce >= 0) {
-            kacc += p.kcoef[(int64_t)ce * p.m_pad + m] * T;
-            sacc += p.scoef[ce] * T;
+          if (sp >= 0 && mm < mc) {
+            if (xk >= 0) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)T;
+            if (wn > 0) w0 += p.wo_gg[(int64_t)wb * p.m_pad + m0 + mm] * T;
+            if (wn > 1) w1 += p.wo_gg[(int64_t)(wb + 1) * p.m_pad + m0 + mm] * T;
+            if (wn > 2) w2 += p.wo_gg[(int64_t)(wb + 2) * p.m_pad + m0 + mm] * T;
+            if (FINAL && ce >= 0) {
+              atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * T);
+              atomicAdd(&s_s[mm], p.scoef[ce] * T);
+            }
           }
         }
+      }
+      atomicAdd(&dT_out[c], (double)dacc);
+      if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wb]], (double)w0);
+      if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wb + 1]], (double)w1);
+      if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wb + 2]], (double)w2);
+      if (FINAL) {
+        atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
+        if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
+        if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
       }
     }
     __syncthreads();
-    // a flag raised during level L lives in word L&1; level L+1 writes the other word,
-    // so a warp still reading this one cannot see a later level's timeout
+    // a flag raised during unit u lives in word u&1; unit u+1 writes the other word
     if (s_abort[cur]) {
-      // leave together; first let the copy this CTA still has in flight land (bounded)
-      if (threadIdx.x == 0 && issued_next) mbar_wait_bounded(&bars[cur ^ 1], (unsigned)((L + 1) >> 1) & 1u);
+      if (tid == 0 && next) mbar_wait_bounded(&bars[cur ^ 1], (unsigned)((u + 1) >> 1) & 1u);
       __syncthreads();
       return;
     }
   }
   if (FINAL) {
-    // reduce the per-warp K/S partials (the T ring is free after the last barrier)
-    Real* red = buf;
-    red[warp * 32 + lane] = kacc;
-    red[(nw + warp) * 32 + lane] = sacc;
-    __syncthreads();
-    if (warp == 0) {
-      Real ks = 0, ss = 0;
-      for (int w = 0; w < nw; ++w) {
-        ks += red[w * 32 + lane];
-        ss += red[(nw + w) * 32 + lane];
-      }
-      if (active) {
-        p.K[(int64_t)m * p.n_dir + q] = (double)ks;
-        p.S[(int64_t)m * p.n_dir + q] = (double)ss;
-      }
+    for (int j = tid; j < mc; j += blockDim.x) {
+      p.K[(int64_t)(m0 + j) * p.n_dir + q] = (double)s_k[j];
+      p.S[(int64_t)(m0 + j) * p.n_dir + q] = (double)s_s[j];
     }
   }
 }
@@ -341,7 +438,8 @@ __global__ void __launch_bounds__(256) bte_sweep_kernel(const SweepParams<Real> 
 // ---- table upload ---------------------------------------------------------------
 
 size_t DevSchedule::bytes() const {
-  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &mfp, &tco, &sig, &wo_wall, &wo_gg, &kcoef, &scoef, &hs};
+  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &mfp, &tco, &sig, &wo_wall, &wo_gg, &kcoef, &scoef, &hs,
+                         &vals, &cellmap, &Pq, &si, &sr};
   size_t b = 0;
   for (auto* x : all) b += x->bytes;
   return b;
@@ -354,34 +452,45 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
   return upload(b, h, st);
 }
 
-static constexpr int kThreads = 256;
-
-// Shared memory of one CTA for a given level cap.
+// Choose MFPs per CTA: minimise waves x (per-level overhead + MFPs per CTA) under the
+// shared-memory budget; two CTAs per SM preferred.
 template <typename Real>
-static size_t sweep_smem(const Schedule& s, int cap) {
-  const int nw = kThreads / 32;
-  return 128 + 2 * (size_t)cap * RecLayout<Real>::W * 4 + (size_t)std::max(s.max_slots, 2 * nw) * 32 * sizeof(Real);
+static int choose_chunk(const Schedule& s, int num_sms, size_t optin, int& mcp_out) {
+  const int rows = s.max_slots + 1;
+  double best = 1e300;
+  int best_mc = 0;
+  for (int k = 1; k <= s.n_mfp; ++k) {
+    const int mc = (s.n_mfp + k - 1) / k;
+    if (k > 1 && (s.n_mfp + k - 2) / (k - 1) == mc) continue;
+    const int mcp = (mc + 3) & ~3;
+    const size_t sm = SmemLayout<Real>(mcp, s.ds, rows).total;
+    if (sm > optin) continue;
+    const int per_sm = std::max(1, std::min(4, (int)((228 * 1024) / (sm + 1024))));
+    const int64_t ctas = (int64_t)s.n_dir * k;
+    const int64_t waves = (ctas + (int64_t)num_sms * per_sm - 1) / ((int64_t)num_sms * per_sm);
+    const double cost = (double)waves * (24.0 + mcp) / std::min(per_sm, 2);
+    if (cost < best) { best = cost; best_mc = mc; mcp_out = mcp; }
+  }
+  return best_mc;
 }
 
 template <typename Real>
 static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   const Schedule& s = plan->sched;
   cudaStream_t st = plan->ctx->stream;
-  // level cap: largest of {128, 96, 64, 48, 32} that lets two CTAs share an SM, else the smallest that fits one
-  const size_t per_sm = 228 * 1024, reserve = 1024;
-  int cap = 0;
-  for (int c : {128, 96, 64, 48, 32})
-    if (sweep_smem<Real>(s, c) + reserve <= per_sm / 2) { cap = c; break; }
-  if (!cap)
-    for (int c : {128, 96, 64, 48, 32})
-      if (sweep_smem<Real>(s, c) <= plan->ctx->smem_optin) { cap = c; break; }
-  if (!cap) {
+  int mcp = 0;
+  const int mc = choose_chunk<Real>(s, plan->ctx->num_sms, plan->ctx->smem_optin, mcp);
+  if (!mc) {
     set_error("sweep front needs more shared memory than one CTA can have (" + std::to_string(s.max_slots) +
               " slots)");
     return OBTE_ERR_UNSUPPORTED;
   }
-  d.cap = cap;
-  // split levels into units of at most `cap` items (slots were assigned per level, so this stays valid)
+  d.mc = mc;
+  d.mcp = mcp;
+  d.n_chunks = (s.n_mfp + mc - 1) / mc;
+  d.zero_slot = s.max_slots;
+  d.smem = SmemLayout<Real>(mcp, s.ds, s.max_slots + 1).total;
+  // split levels into units of at most kUnit elements (slots were assigned per level, so this stays valid)
   std::vector<int32_t> kptr;
   std::vector<int64_t> koff(s.n_dir);
   std::vector<int32_t> kn(s.n_dir);
@@ -390,17 +499,20 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
     const int32_t* lp = s.lev_ptr.data() + s.lev_off[q];
     int units = 0;
     kptr.push_back(0);
-    for (int L = 0; L < s.nlev[q]; ++L) {
-      for (int32_t a = lp[L]; a < lp[L + 1]; a += cap) {
-        kptr.push_back(std::min(a + cap, lp[L + 1]));
+    for (int Lv = 0; Lv < s.nlev[q]; ++Lv)
+      for (int32_t a = lp[Lv]; a < lp[Lv + 1]; a += kUnit) {
+        kptr.push_back(std::min(a + kUnit, lp[Lv + 1]));
         ++units;
       }
-    }
     kn[q] = units;
   }
-  std::vector<int32_t> rec;
-  pack_records<Real>(s, rec);
-  OBTE_TRY(upload(d.rec, rec, st));
+  Packed pk;
+  OBTE_TRY(pack<Real>(s, d.zero_slot, pk));
+  OBTE_TRY(upload(d.rec, pk.rec, st));
+  OBTE_TRY(upload(d.cellmap, pk.cellmap, st));
+  OBTE_TRY(upload(d.Pq, pk.P, st));
+  OBTE_TRY(upload(d.si, pk.si, st));
+  OBTE_TRY(upload_real<Real>(d.sr, pk.sr, st));
   OBTE_TRY(upload(d.klev_ptr, kptr, st));
   OBTE_TRY(upload(d.klev_off, koff, st));
   OBTE_TRY(upload(d.knlev, kn, st));
@@ -413,7 +525,10 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   OBTE_TRY(upload_real<Real>(d.wo_gg, s.wo_gg, st));
   OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
   OBTE_TRY(upload_real<Real>(d.scoef, s.scoef, st));
-  if (!s.hs.empty()) OBTE_TRY(upload_real<Real>(d.hs, s.hs, st));
+  if (!s.hs.empty()) OBTE_TRY(upload(d.hs, s.hs, st));
+  // per-sweep values (b, p), padded by 32 B for the aligned TMA window
+  OBTE_TRY(d.vals.alloc((size_t)s.n_dir * s.n * 2 * sizeof(Real) + 32));
+  OBTE_CUDA(cudaMemsetAsync(d.vals.p, 0, d.vals.bytes, st));
   d.ready = true;
   return OBTE_OK;
 }
@@ -437,28 +552,45 @@ template <typename Real, int NF, bool FINAL>
 static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                bool with_src, double* Jraw, double* K, double* S) {
   const Schedule& s = plan->sched;
-  const size_t smem = sweep_smem<Real>(s, d.cap);
+  cudaStream_t st = plan->ctx->stream;
+  const int64_t total = (int64_t)s.n_dir * s.n;
+  const int vblocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)plan->ctx->num_sms * 8);
+  sweep_values_kernel<Real><<<vblocks, 256, 0, st>>>(
+      d.cellmap.as<int32_t>(), d.Pq.as<double>(), d.rec.as<int32_t>(), Rec<Real>::W, d.si.as<int32_t>(),
+      d.sr.as<Real>(), u_in, s.n, s.hs.empty() ? nullptr : d.hs.as<double>(), with_src ? 1 : 0, total,
+      d.vals.as<Real>());
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
   auto kern = bte_sweep_kernel<Real, NF, FINAL>;
-  OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
   SweepParams<Real> p;
-  p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.m_pad = s.m_pad; p.n_chunks = s.n_chunks; p.n_dir = s.n_dir;
-  p.ds = s.ds; p.cap = d.cap;
-  p.rec = d.rec.as<int32_t>();
-  p.lev_ptr = d.klev_ptr.as<int32_t>();
-  p.lev_off = d.klev_off.as<int64_t>();
-  p.nlev = d.knlev.as<int32_t>();
+  p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds;
+  p.mc = d.mc; p.mcp = d.mcp; p.n_chunks = d.n_chunks; p.zero_slot = d.zero_slot;
+  p.rec = d.rec.as<int32_t>(); p.vals = d.vals.as<Real>();
+  p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
   p.x_base = plan->x_base_dev.as<int64_t>();
+  p.si = d.si.as<int32_t>(); p.sr = d.sr.as<Real>();
   p.wo_wall = d.wo_wall.as<int32_t>();
   p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_gg = d.wo_gg.as<Real>();
-  p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
-  p.hs = s.hs.empty() ? nullptr : d.hs.as<Real>();
-  p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S = S; p.with_src = with_src ? 1 : 0;
+  p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>(); p.m_pad = s.m_pad;
+  p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S = S;
   p.err = plan->err.as<int>();
-  const int grid = s.n_dir * s.n_chunks;
-  kern<<<grid, kThreads, smem, plan->ctx->stream>>>(p);
+  const int grid = s.n_dir * d.n_chunks;
+  kern<<<grid, kUnit, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
   return OBTE_OK;
+}
+
+template <typename Real>
+static obte_status launch_nf(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
+                             bool with_src, bool final_pass, double* Jraw, double* K, double* S) {
+  if (plan->sched.nf == 3) {
+    if (final_pass) return launch_impl<Real, 3, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+    return launch_impl<Real, 3, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  }
+  if (final_pass) return launch_impl<Real, 4, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  return launch_impl<Real, 4, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
 }
 
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
@@ -470,19 +602,8 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
   if (s.nf > 4) { set_error("elements with more than 4 sides are not supported"); return OBTE_ERR_UNSUPPORTED; }
   OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
   if (final_pass) OBTE_CUDA(cudaMemsetAsync(Jraw, 0, (size_t)s.n * s.ds * sizeof(double), st));
-#define OBTE_DISPATCH(R, DS)                                                                        \
-  do {                                                                                              \
-    if (s.nf == 3) {                                                                                \
-      if (final_pass) return launch_impl<R, 3, true>(plan, DS, u_in, u_out, with_src, Jraw, K, S);  \
-      return launch_impl<R, 3, false>(plan, DS, u_in, u_out, with_src, Jraw, K, S);                 \
-    } else {                                                                                        \
-      if (final_pass) return launch_impl<R, 4, true>(plan, DS, u_in, u_out, with_src, Jraw, K, S);  \
-      return launch_impl<R, 4, false>(plan, DS, u_in, u_out, with_src, Jraw, K, S);                 \
-    }                                                                                               \
-  } while (0)
-  if (fp32) OBTE_DISPATCH(float, plan->d32);
-  else OBTE_DISPATCH(double, plan->d64);
-#undef OBTE_DISPATCH
+  if (fp32) return launch_nf<float>(plan, plan->d32, u_in, u_out, with_src, final_pass, Jraw, K, S);
+  return launch_nf<double>(plan, plan->d64, u_in, u_out, with_src, final_pass, Jraw, K, S);
 }
 
 // Device error word: nonzero after a bounded wait gave up (cleared on read).
