@@ -224,12 +224,19 @@ def main():
     if args.profile_sweeps:
         u = torch.zeros(plan.nu, dtype=torch.float64, device=dev)
         uo = torch.zeros_like(u)
+        ms = {}
         for prec in ("fp32", "fp64"):
-            for _ in range(args.profile_sweeps):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            for i in range(args.profile_sweeps):
+                if i == args.profile_sweeps // 2:
+                    ev[0].record()
                 _lib.check(lib.obte_bte_sweep(plan.handle, _lib.PRECISION[prec], C.c_void_p(u.data_ptr()),
                                               C.c_void_p(uo.data_ptr()), 1), "sweep")
-        torch.cuda.synchronize()
-        print(json.dumps({"profile_sweeps": args.profile_sweeps, "workload": args.workload}))
+            ev[1].record()
+            ev[1].synchronize()
+            ms[prec] = ev[0].elapsed_time(ev[1]) / max(1, args.profile_sweeps - args.profile_sweeps // 2)
+        print(json.dumps({"profile_sweeps": args.profile_sweeps, "workload": args.workload,
+                          "ms_per_sweep": ms, "mcp_env": os.environ.get("OBTE_SWEEP_MCP")}))
         return
     dT0 = torch.zeros(geo.n_elems, dtype=torch.float64, device=dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)

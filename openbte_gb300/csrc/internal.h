@@ -88,6 +88,7 @@ struct Schedule {
   std::vector<int32_t> nlev;       // [n_dir]
   std::vector<int32_t> nslots;     // [n_dir]
   int max_slots = 0;
+  int max_src = 0;                 // largest number of periodic source elements of one direction
   // periodic interface
   std::vector<int64_t> x_base;     // [n_dir+1] source-cell offsets
   std::vector<int32_t> x_cell;     // [x_base[n_dir]] element of each source slot
@@ -120,7 +121,7 @@ obte_status build_schedule(const obte_problem* prob, const obte_material* mat, S
 //   si/sr    side table of special elements (periodic inflow, wall/periodic/contact outputs)
 struct DevSchedule {
   bool ready = false;
-  int mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0;
+  int mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;
   size_t smem = 0;
   DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap, Pq, si, sr;
   size_t bytes() const;

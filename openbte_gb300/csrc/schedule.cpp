@@ -199,6 +199,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.kcoef.clear();
   s.scoef.clear();
   s.max_slots = 0;
+  s.max_src = 0;
 
   std::vector<double> D(n), P(n);
   std::vector<double> g(nfd);
@@ -303,10 +304,37 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     }
     for (int64_t p = 0; p < n; ++p) pos_of[order[p]] = (int32_t)p;
 
-    // slots: element alive from its level to the last level of its consumers
+    // periodic source cells of direction q (sorted unique upstream elements of cut inflow)
+    std::vector<int32_t> src;
+    for (int64_t f = 0; f < nfd; ++f)
+      if (g[f] < 0 && f_cut[f]) src.push_back(f_nb[f]);
+    std::sort(src.begin(), src.end());
+    src.erase(std::unique(src.begin(), src.end()), src.end());
+    s.x_base[q + 1] = s.x_base[q] + (int64_t)src.size();
+    s.max_src = std::max(s.max_src, (int)src.size());
+    std::unordered_map<int32_t, int32_t> src_idx;
+    for (size_t k = 0; k < src.size(); ++k) { src_idx[src[k]] = (int32_t)k; s.x_cell.push_back(src[k]); }
+
+    // inflow walls / wall outputs per element
+    for (int64_t e = 0; e < n; ++e) { wall_in[e].clear(); wall_out[e].clear(); }
+    for (int64_t w = 0; w < nd; ++w) {
+      double v = 0;
+      for (int d = 0; d < dim; ++d) v += sq[d] * w_db[w * dim + d];
+      if (v < 0) wall_in[w_cell[w]].push_back((int32_t)w);
+      bool any = false;
+      for (int m = 0; m < n_mfp && !any; ++m) any = gb_of(m, q, w) > 0;
+      if (any) wall_out[w_cell[w]].push_back((int32_t)w);
+    }
+
+    // slots: an element is alive from its level to the last level of its consumers; elements
+    // with per-MFP outputs (periodic source, wall re-emission, contact) hold a slot for their
+    // own level so their outputs can be read back after the MFP loop
     for (int64_t e = 0; e < n; ++e) {
       int32_t lu = -1;
       for (int64_t k = out_ptr[e]; k < out_ptr[e + 1]; ++k) lu = std::max(lu, level[out_adj[k]]);
+      const bool special = src_idx.count((int32_t)e) || !wall_out[e].empty() || ck == OBTE_CONTACT_NANOWIRE ||
+                           contact_of.count((int32_t)e);
+      if (special) lu = std::max(lu, level[e]);
       last_use[e] = lu;
       slot_of[e] = -1;
     }
@@ -329,27 +357,6 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       }
       s.nslots[q] = next;
       s.max_slots = std::max(s.max_slots, (int)next);
-    }
-
-    // periodic source cells of direction q (sorted unique upstream elements of cut inflow)
-    std::vector<int32_t> src;
-    for (int64_t f = 0; f < nfd; ++f)
-      if (g[f] < 0 && f_cut[f]) src.push_back(f_nb[f]);
-    std::sort(src.begin(), src.end());
-    src.erase(std::unique(src.begin(), src.end()), src.end());
-    s.x_base[q + 1] = s.x_base[q] + (int64_t)src.size();
-    std::unordered_map<int32_t, int32_t> src_idx;
-    for (size_t k = 0; k < src.size(); ++k) { src_idx[src[k]] = (int32_t)k; s.x_cell.push_back(src[k]); }
-
-    // inflow walls / wall outputs per element
-    for (int64_t e = 0; e < n; ++e) { wall_in[e].clear(); wall_out[e].clear(); }
-    for (int64_t w = 0; w < nd; ++w) {
-      double v = 0;
-      for (int d = 0; d < dim; ++d) v += sq[d] * w_db[w * dim + d];
-      if (v < 0) wall_in[w_cell[w]].push_back((int32_t)w);
-      bool any = false;
-      for (int m = 0; m < n_mfp && !any; ++m) any = gb_of(m, q, w) > 0;
-      if (any) wall_out[w_cell[w]].push_back((int32_t)w);
     }
 
     // items in level order

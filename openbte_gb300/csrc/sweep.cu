@@ -1,6 +1,6 @@
 // Batched upwind transport sweep for sm_103a.
 //
-// One CTA = one direction q x one chunk of `mc` mean free paths.  The CTA walks
+// One CTA = one direction q x one chunk of MCP mean free paths.  The CTA walks
 // the direction's elements level by level (longest-path layers of the upwind
 // DAG with periodic inflow cut, split into units of at most 128 elements);
 // within a unit every thread owns one element and loops over the chunk's MFPs:
@@ -9,10 +9,15 @@
 //
 // the row of A_mq T = B of openbte/bte.py:183-218 for an element whose upwind
 // neighbours are known; b = DeltaT + heat source, p = perturbation minus the
-// wall inflow g_w T_B (openbte/bte.py:200,211-214).  T_up comes from a ring of
-// shared-memory rows (one row per live upstream element, one column per MFP);
-// a dedicated zero row absorbs absent faces.  Inflow across a cut periodic
-// face reads the periodic-inflow part of the state vector instead.
+// wall inflow g_w T_B (openbte/bte.py:200,211-214).
+//
+// T_up lives in a ring of shared-memory rows, one per live upstream element
+// and one column per MFP (row-major by MFP).  Extra rows: a zero row for absent
+// faces, a trash row for elements nobody reads, and one row per periodic
+// source element of the direction, filled from the state vector at CTA start,
+// so inflow across a cut periodic face is an ordinary row read.  The MFP loop
+// is therefore branch-free; elements with per-MFP outputs (periodic source,
+// wall re-emission, contact) read their T back from their row afterwards.
 //
 // Data movement per unit: the packed element records and the per-sweep values
 // (b, p) arrive in shared memory by TMA bulk copies (cp.async.bulk + mbarrier)
@@ -25,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "internal.h"
@@ -37,22 +43,25 @@ static constexpr int kUnit = 128;      // elements per level unit = threads per 
 // FP32: 12 words (48 B) : cell slot special s0 s1 s2 s3 | c0 c1 c2 c3 D
 // FP64: 20 words (80 B) : cell slot special s0 s1 s2 s3 pad | c0 c1 c2 c3 D (8 B each) | pad
 template <typename Real> struct Rec;
-template <> struct Rec<float> { static constexpr int W = 12, COEF = 7, D = 11; };
-template <> struct Rec<double> { static constexpr int W = 20, COEF = 8, D = 16; };
+template <> struct Rec<float> { static constexpr int W = 12, COEF = 7, CSTEP = 1, D = 11; };
+template <> struct Rec<double> { static constexpr int W = 20, COEF = 8, CSTEP = 2, D = 16; };
 
-// special-item table: int part and real part per entry
-//   si: xk wout contact nper p0 p1 nwall w0 w1 w2   (10 ints)
-//   sr: pc0 pc1 wc0 wc1 wc2                           (5 reals)
-static constexpr int SI = 10, SR = 5;
+// special-element table
+//   si: xk wout contact nwall w0 w1 w2 pad     (8 ints)
+//   sr: wc0 wc1 wc2 pad                          (4 reals)
+static constexpr int SI = 8, SR = 4;
 
 struct Packed {
   std::vector<int32_t> rec, cellmap, si;
   std::vector<double> P, sr;
 };
 
+// Ring rows: [0, S) slots, S zero row, S+1 trash row, S+2+k periodic source k.
 template <typename Real>
-static obte_status pack(const Schedule& s, int zero_slot, Packed& pk) {
+static obte_status pack(const Schedule& s, Packed& pk) {
   constexpr int W = Rec<Real>::W;
+  const int S = s.max_slots;
+  const int zero_row = S, trash_row = S + 1, per_row = S + 2;
   const size_t total = (size_t)s.n_dir * s.n;
   pk.rec.assign(total * W, 0);
   pk.cellmap.assign(total, 0);
@@ -62,40 +71,39 @@ static obte_status pack(const Schedule& s, int zero_slot, Packed& pk) {
   for (size_t it = 0; it < total; ++it) {
     int32_t* r = pk.rec.data() + it * W;
     r[0] = s.cell[it];
-    r[1] = s.slot[it];
+    r[1] = s.slot[it] >= 0 ? s.slot[it] : trash_row;
     r[2] = -1;
     pk.cellmap[it] = s.cell[it];
     pk.P[it] = s.P[it];
-    int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0, 0, 0};
-    double sr[SR] = {0, 0, 0, 0, 0};
-    bool special = s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0;
+    int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0};
+    double sr[SR] = {0, 0, 0, 0};
+    const bool outputs = s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0;
+    if (outputs && s.slot[it] < 0) {
+      set_error("element with per-MFP outputs has no ring slot");
+      return OBTE_ERR_BAD_ARG;
+    }
+    bool special = outputs;
     double coef[4] = {0, 0, 0, 0};
-    int32_t slot_in[4] = {zero_slot, zero_slot, zero_slot, zero_slot};
+    int32_t row_in[4] = {zero_row, zero_row, zero_row, zero_row};
     int k = 0;
     for (int f = 0; f < s.nf; ++f) {
       const int32_t code = s.in_idx[it * s.nf + f];
       const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
       const int32_t idx = code & ITEM_MASK;
       const double g = s.in_coef[it * s.nf + f];
-      if (kind == ITEM_CELL) {
-        slot_in[k] = idx;
+      if (kind == ITEM_CELL || kind == ITEM_PERIODIC) {
+        row_in[k] = kind == ITEM_CELL ? idx : per_row + idx;
         coef[k] = g;
         ++k;
-      } else if (kind == ITEM_PERIODIC) {
-        if (si[3] >= 2) { set_error("more than two periodic inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
+      } else if (kind == ITEM_WALL) {
+        if (si[3] >= 3) { set_error("more than three wall inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
         si[4 + si[3]] = idx;
         sr[si[3]] = g;
         si[3]++;
         special = true;
-      } else if (kind == ITEM_WALL) {
-        if (si[6] >= 3) { set_error("more than three wall inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
-        si[7 + si[6]] = idx;
-        sr[2 + si[6]] = g;
-        si[6]++;
-        special = true;
       }
     }
-    for (int f = 0; f < 4; ++f) r[3 + f] = slot_in[f];
+    for (int f = 0; f < 4; ++f) r[3 + f] = row_in[f];
     if (special) {
       r[2] = (int32_t)(pk.si.size() / SI);
       pk.si.insert(pk.si.end(), si, si + SI);
@@ -179,7 +187,7 @@ __global__ void sweep_values_kernel(const int32_t* __restrict__ cellmap, const d
     if (sp >= 0) {
       const int32_t* s = si + (int64_t)sp * SI;
       const Real* r = sr + (int64_t)sp * SR;
-      for (int k = 0; k < s[6]; ++k) pp -= (double)r[2 + k] * TB[s[7 + k]];
+      for (int k = 0; k < s[3]; ++k) pp -= (double)r[k] * TB[s[4 + k]];
     }
     vals[2 * it] = (Real)b;
     vals[2 * it + 1] = (Real)pp;
@@ -190,9 +198,10 @@ template <typename Real>
 struct SweepParams {
   int64_t n;
   int64_t nd;
-  int n_mfp, n_dir, ds;
-  int mc, mcp, n_chunks;   // MFPs per chunk, padded to 4, chunks per direction
-  int zero_slot;           // ring rows: zero_slot + 1
+  int n_mfp, n_dir, ds, m_pad;
+  int n_chunks;            // chunks of MCP MFPs per direction
+  int rows;                // ring rows
+  int S;                   // slot rows before the zero/trash/periodic rows
   const int32_t* __restrict__ rec;
   const Real* __restrict__ vals;
   const int32_t* __restrict__ lev_ptr;
@@ -200,31 +209,29 @@ struct SweepParams {
   const int32_t* __restrict__ nlev;
   const int64_t* __restrict__ x_base;
   const int32_t* __restrict__ si;
-  const Real* __restrict__ sr;
   const int32_t* __restrict__ wo_wall;
-  const Real* __restrict__ mfp;    // [n_mfp]
+  const Real* __restrict__ mfp;    // [m_pad]
   const Real* __restrict__ tco;    // [n_dir * m_pad]
   const Real* __restrict__ sig;    // [n_dir * m_pad * ds]
   const Real* __restrict__ wo_gg;  // [n_wo * m_pad]
   const Real* __restrict__ kcoef;  // [n_ce * m_pad]
   const Real* __restrict__ scoef;  // [n_ce]
-  int m_pad;
   const double* __restrict__ u_in;
   double* __restrict__ u_out;
   double* __restrict__ Jraw;
   double* __restrict__ K;
-  double* __restrict__ S;
+  double* __restrict__ S_out;
   int* __restrict__ err;
 };
 
 template <typename Real>
-__device__ __forceinline__ Real rec_real(const int32_t* r, int word);
+__device__ __forceinline__ Real word_real(const int32_t* r, int word);
 template <>
-__device__ __forceinline__ float rec_real<float>(const int32_t* r, int word) {
+__device__ __forceinline__ float word_real<float>(const int32_t* r, int word) {
   return __int_as_float(r[word]);
 }
 template <>
-__device__ __forceinline__ double rec_real<double>(const int32_t* r, int word) {
+__device__ __forceinline__ double word_real<double>(const int32_t* r, int word) {
   return __hiloint2double(r[word + 1], r[word]);
 }
 
@@ -239,11 +246,11 @@ __device__ __forceinline__ double recip(double x) {
 }
 
 // Shared memory layout (bytes):
-//   [0,16) mbarriers  [16,24) abort flags  [128, ...) rec0 rec1 vals0 vals1 | lam t | sig | K S | ring
+//   [0,16) mbarriers  [16,24) abort flags  [128, ...) rec0 rec1 vals0 vals1 | sig | K S | ring
 template <typename Real>
 struct SmemLayout {
-  size_t rec0, rec1, val0, val1, lam, tco, sig, kacc, sacc, ring, total;
-  __host__ __device__ SmemLayout(int mcp, int ds, int rows) {
+  size_t rec0, rec1, val0, val1, sig, kacc, sacc, ring, total;
+  __host__ __device__ SmemLayout(int mcp, int rows) {
     constexpr int W = Rec<Real>::W;
     size_t o = 128;
     rec0 = o; o += (size_t)kUnit * W * 4;
@@ -251,8 +258,6 @@ struct SmemLayout {
     val0 = o; o += (size_t)(kUnit + 2) * 2 * sizeof(Real);
     val1 = o; o += (size_t)(kUnit + 2) * 2 * sizeof(Real);
     o = (o + 15) & ~(size_t)15;
-    lam = o; o += (size_t)mcp * sizeof(Real);
-    tco = o; o += (size_t)mcp * sizeof(Real);
     sig = o; o += (size_t)mcp * 3 * sizeof(Real);
     kacc = o; o += (size_t)mcp * sizeof(Real);
     sacc = o; o += (size_t)mcp * sizeof(Real);
@@ -262,30 +267,28 @@ struct SmemLayout {
   }
 };
 
-template <typename Real, int NF, bool FINAL>
+template <typename Real, int NF, int MCP, bool FINAL>
 __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real> p) {
   constexpr int W = Rec<Real>::W;
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
   extern __shared__ __align__(128) unsigned char smem[];
-  const int rows = p.zero_slot + 1;
-  const SmemLayout<Real> L(p.mcp, p.ds, rows);
+  const int rows = p.rows;
+  const SmemLayout<Real> L(MCP, rows);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   int* s_abort = reinterpret_cast<int*>(smem + 16);
   int32_t* const recb0 = reinterpret_cast<int32_t*>(smem + L.rec0);
   int32_t* const recb1 = reinterpret_cast<int32_t*>(smem + L.rec1);
   unsigned char* const valb0 = smem + L.val0;
   unsigned char* const valb1 = smem + L.val1;
-  Real* s_lam = reinterpret_cast<Real*>(smem + L.lam);
-  Real* s_t = reinterpret_cast<Real*>(smem + L.tco);
   Real* s_sig = reinterpret_cast<Real*>(smem + L.sig);
   Real* s_k = reinterpret_cast<Real*>(smem + L.kacc);
   Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
-  Real* ring = reinterpret_cast<Real*>(smem + L.ring);   // [mcp][rows]
+  Real* ring = reinterpret_cast<Real*>(smem + L.ring);   // [MCP][rows]
 
   const int q = blockIdx.x / p.n_chunks;
   const int chunk = blockIdx.x - q * p.n_chunks;
-  const int m0 = chunk * p.mc;
-  const int mc = min(p.mc, p.n_mfp - m0);
+  const int m0 = chunk * MCP;
+  const int mc = min(MCP, p.n_mfp - m0);
   const int tid = threadIdx.x;
   const int32_t* __restrict__ lev = p.lev_ptr + p.lev_off[q];
   const int nlev = p.nlev[q];
@@ -294,22 +297,36 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   const unsigned char* __restrict__ val_base = reinterpret_cast<const unsigned char*>(p.vals);
   const int64_t val_q0 = (int64_t)q * p.n * VB;
   const int64_t xq = p.x_base[q];
+  const int nsrc = (int)(p.x_base[q + 1] - xq);
   const double* __restrict__ X = p.u_in + p.n + p.nd;
   double* __restrict__ dT_out = p.u_out;
   double* __restrict__ TB_out = p.u_out + p.n;
   double* __restrict__ X_out = p.u_out + p.n + p.nd;
 
-  // per-chunk ordinate data; padded MFPs get L = t = 0 (they compute a harmless T = b)
-  for (int j = tid; j < p.mcp; j += blockDim.x) {
+  // per-chunk ordinate data in registers; padded MFPs get L = t = 0 (harmless T = b)
+  Real lam[MCP], tt[MCP];
+#pragma unroll
+  for (int j = 0; j < MCP; ++j) {
     const bool ok = j < mc;
-    s_lam[j] = ok ? p.mfp[m0 + j] : Real(0);
-    s_t[j] = ok ? p.tco[(int64_t)q * p.m_pad + m0 + j] : Real(0);
-    for (int d = 0; d < 3; ++d)
-      s_sig[j * 3 + d] = (ok && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m0 + j) * p.ds + d] : Real(0);
-    s_k[j] = 0;
-    s_s[j] = 0;
+    lam[j] = ok ? p.mfp[m0 + j] : Real(0);
+    tt[j] = ok ? p.tco[(int64_t)q * p.m_pad + m0 + j] : Real(0);
   }
-  for (int i = tid; i < p.mcp * rows; i += blockDim.x) ring[i] = Real(0);
+  if (FINAL) {
+    for (int j = tid; j < MCP; j += blockDim.x) {
+      for (int d = 0; d < 3; ++d)
+        s_sig[j * 3 + d] = (j < mc && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m0 + j) * p.ds + d] : Real(0);
+      s_k[j] = 0;
+      s_s[j] = 0;
+    }
+  }
+  // ring: zero the slot/zero/trash rows, fill the periodic-source rows from the state vector
+  for (int i = tid; i < MCP * rows; i += blockDim.x) {
+    const int mm = i / rows, row = i - mm * rows;
+    Real v = 0;
+    const int k = row - (p.S + 2);
+    if (k >= 0 && k < nsrc && mm < mc) v = (Real)X[(xq + k) * p.n_mfp + m0 + mm];
+    ring[i] = v;
+  }
   if (tid == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
@@ -319,7 +336,7 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   }
   __syncthreads();
 
-  // TMA of unit u into buffer u&1: records [a, e) and values [a, e) (values 16-B aligned window)
+  // TMA of unit u into buffer u&1: records [a, e) and values [a, e) (values in a 16-B aligned window)
   auto issue = [&](int u) {
     const int a = lev[u], e = lev[u + 1];
     const unsigned rbytes = (unsigned)(e - a) * W * 4u;
@@ -344,30 +361,27 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
       s_abort[cur] = 1;
       atomicOr(p.err, 1);
     } else if (tid < e - a) {
-      const int32_t* r = (cur ? recb1 : recb0) + tid * W;
+      // record: W/4 vector loads
+      int32_t r[W];
+      const int4* r4 = reinterpret_cast<const int4*>((cur ? recb1 : recb0) + tid * W);
+#pragma unroll
+      for (int i = 0; i < W / 4; ++i) {
+        const int4 x = r4[i];
+        r[4 * i] = x.x; r[4 * i + 1] = x.y; r[4 * i + 2] = x.z; r[4 * i + 3] = x.w;
+      }
       const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
       const Real* v = reinterpret_cast<const Real*>(cur ? valb1 : valb0) + 2 * (voff + tid);
       const Real b = v[0], pw = v[1];
       const int c = r[0], so = r[1], sp = r[2];
       const int s0 = r[3], s1 = r[4], s2 = r[5], s3 = r[6];
-      const Real c0 = rec_real<Real>(r, Rec<Real>::COEF);
-      const Real c1 = rec_real<Real>(r, Rec<Real>::COEF + (W == 12 ? 1 : 2));
-      const Real c2 = rec_real<Real>(r, Rec<Real>::COEF + (W == 12 ? 2 : 4));
-      const Real c3 = rec_real<Real>(r, Rec<Real>::COEF + (W == 12 ? 3 : 6));
-      const Real D = rec_real<Real>(r, Rec<Real>::D);
-      // special element: periodic inflow / outputs
-      int xk = -1, wo = 0, ce = -1, np = 0, p0 = 0, p1 = 0;
-      Real pc0 = 0, pc1 = 0;
-      if (sp >= 0) {
-        const int32_t* si = p.si + (int64_t)sp * SI;
-        const Real* sr = p.sr + (int64_t)sp * SR;
-        xk = si[0]; wo = si[1]; ce = si[2]; np = si[3]; p0 = si[4]; p1 = si[5];
-        pc0 = sr[0]; pc1 = sr[1];
-      }
-      // accumulate in the sweep precision (FP64 conversions are slow on this part); one FP64 atomic each
-      Real dacc = 0, j0 = 0, j1 = 0, j2 = 0, w0 = 0, w1 = 0, w2 = 0;
-      const int wb = wo >> 3, wn = wo & 7;
-      for (int mb = 0; mb < p.mcp; mb += 4) {
+      const Real c0 = word_real<Real>(r, Rec<Real>::COEF);
+      const Real c1 = word_real<Real>(r, Rec<Real>::COEF + Rec<Real>::CSTEP);
+      const Real c2 = word_real<Real>(r, Rec<Real>::COEF + 2 * Rec<Real>::CSTEP);
+      const Real c3 = word_real<Real>(r, Rec<Real>::COEF + 3 * Rec<Real>::CSTEP);
+      const Real D = word_real<Real>(r, Rec<Real>::D);
+      Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
+#pragma unroll
+      for (int mb = 0; mb < MCP; mb += 4) {
         Real v0[4], v1[4], v2[4], v3[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -375,48 +389,49 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
           v0[j] = row[s0];
           v1[j] = row[s1];
           v2[j] = row[s2];
-          v3[j] = NF > 3 ? row[s3] : Real(0);
+          if (NF > 3) v3[j] = row[s3];
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int mm = mb + j;
-          const Real lam = s_lam[mm];
           Real s = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
           if (NF > 3) s += c3 * v3[j];
-          if (np) {
-            if (mm < mc) {
-              s += pc0 * (Real)X[(xq + p0) * p.n_mfp + m0 + mm];
-              if (np > 1) s += pc1 * (Real)X[(xq + p1) * p.n_mfp + m0 + mm];
-            }
-          }
-          const Real T = (b + lam * (pw - s)) * recip(Real(1) + lam * D);
-          if (so >= 0) ring[(size_t)mm * rows + so] = T;
-          dacc += s_t[mm] * T;
+          const Real T = (b + lam[mm] * (pw - s)) * recip(Real(1) + lam[mm] * D);
+          ring[(size_t)mm * rows + so] = T;
+          dacc += tt[mm] * T;
           if (FINAL) {
             j0 += s_sig[mm * 3] * T;
             j1 += s_sig[mm * 3 + 1] * T;
             j2 += s_sig[mm * 3 + 2] * T;
           }
-          if (sp >= 0 && mm < mc) {
-            if (xk >= 0) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)T;
-            if (wn > 0) w0 += p.wo_gg[(int64_t)wb * p.m_pad + m0 + mm] * T;
-            if (wn > 1) w1 += p.wo_gg[(int64_t)(wb + 1) * p.m_pad + m0 + mm] * T;
-            if (wn > 2) w2 += p.wo_gg[(int64_t)(wb + 2) * p.m_pad + m0 + mm] * T;
-            if (FINAL && ce >= 0) {
-              atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * T);
-              atomicAdd(&s_s[mm], p.scoef[ce] * T);
-            }
-          }
         }
       }
       atomicAdd(&dT_out[c], (double)dacc);
-      if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wb]], (double)w0);
-      if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wb + 1]], (double)w1);
-      if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wb + 2]], (double)w2);
       if (FINAL) {
         atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
         if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
         if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
+      }
+      // per-MFP outputs of special elements, read back from their own row
+      if (sp >= 0) {
+        const int32_t* si = p.si + (int64_t)sp * SI;
+        const int xk = si[0], wo = si[1], ce = si[2];
+        const int wb = wo >> 3, wn = wo & 7;
+        Real w0 = 0, w1 = 0, w2 = 0;
+        for (int mm = 0; mm < mc; ++mm) {
+          const Real T = ring[(size_t)mm * rows + so];
+          if (xk >= 0) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)T;
+          if (wn > 0) w0 += p.wo_gg[(int64_t)wb * p.m_pad + m0 + mm] * T;
+          if (wn > 1) w1 += p.wo_gg[(int64_t)(wb + 1) * p.m_pad + m0 + mm] * T;
+          if (wn > 2) w2 += p.wo_gg[(int64_t)(wb + 2) * p.m_pad + m0 + mm] * T;
+          if (FINAL && ce >= 0) {
+            atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * T);
+            atomicAdd(&s_s[mm], p.scoef[ce] * T);
+          }
+        }
+        if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wb]], (double)w0);
+        if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wb + 1]], (double)w1);
+        if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wb + 2]], (double)w2);
       }
     }
     __syncthreads();
@@ -430,7 +445,7 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   if (FINAL) {
     for (int j = tid; j < mc; j += blockDim.x) {
       p.K[(int64_t)(m0 + j) * p.n_dir + q] = (double)s_k[j];
-      p.S[(int64_t)(m0 + j) * p.n_dir + q] = (double)s_s[j];
+      p.S_out[(int64_t)(m0 + j) * p.n_dir + q] = (double)s_s[j];
     }
   }
 }
@@ -452,44 +467,55 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
   return upload(b, h, st);
 }
 
-// Choose MFPs per CTA: minimise waves x (per-level overhead + MFPs per CTA) under the
-// shared-memory budget; two CTAs per SM preferred.
+// Chunk widths compiled for each precision.
+template <typename Real> struct Widths;
+template <> struct Widths<float> { static constexpr int N = 5; static constexpr int v[N] = {8, 12, 16, 24, 32}; };
+template <> struct Widths<double> { static constexpr int N = 4; static constexpr int v[N] = {4, 8, 12, 16}; };
+constexpr int Widths<float>::v[];
+constexpr int Widths<double>::v[];
+
+// Choose the chunk width: minimise waves x (per-unit overhead + chunk width) / resident CTAs,
+// under the shared-memory budget.  OBTE_SWEEP_MCP forces a width (tuning).
 template <typename Real>
-static int choose_chunk(const Schedule& s, int num_sms, size_t optin, int& mcp_out) {
-  const int rows = s.max_slots + 1;
+static int choose_mcp(const Schedule& s, int rows, int num_sms, size_t optin) {
+  const char* env = std::getenv("OBTE_SWEEP_MCP");
+  const int forced = env ? std::atoi(env) : 0;
   double best = 1e300;
-  int best_mc = 0;
-  for (int k = 1; k <= s.n_mfp; ++k) {
-    const int mc = (s.n_mfp + k - 1) / k;
-    if (k > 1 && (s.n_mfp + k - 2) / (k - 1) == mc) continue;
-    const int mcp = (mc + 3) & ~3;
-    const size_t sm = SmemLayout<Real>(mcp, s.ds, rows).total;
+  int best_w = 0;
+  for (int i = 0; i < Widths<Real>::N; ++i) {
+    const int w = Widths<Real>::v[i];
+    if (forced && w != forced) continue;
+    const size_t sm = SmemLayout<Real>(w, rows).total;
     if (sm > optin) continue;
-    const int per_sm = std::max(1, std::min(4, (int)((228 * 1024) / (sm + 1024))));
-    const int64_t ctas = (int64_t)s.n_dir * k;
-    const int64_t waves = (ctas + (int64_t)num_sms * per_sm - 1) / ((int64_t)num_sms * per_sm);
-    const double cost = (double)waves * (24.0 + mcp) / std::min(per_sm, 2);
-    if (cost < best) { best = cost; best_mc = mc; mcp_out = mcp; }
+    const int per_sm = std::max(1, std::min(8, (int)((228 * 1024) / (sm + 1024))));
+    const int chunks = (s.n_mfp + w - 1) / w;
+    const int64_t ctas = (int64_t)s.n_dir * chunks;
+    const int64_t slots = (int64_t)num_sms * per_sm;
+    const int64_t waves = (ctas + slots - 1) / slots;
+    // per-CTA time ~ units x (overhead + w); resident CTAs share the SM's issue slots
+    const double per_cta = 40.0 + w;
+    const double cost = (double)waves * per_cta * std::min<int64_t>(per_sm, ctas / num_sms + 1) / 4.0;
+    if (cost < best) { best = cost; best_w = w; }
   }
-  return best_mc;
+  return best_w;
 }
 
 template <typename Real>
 static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   const Schedule& s = plan->sched;
   cudaStream_t st = plan->ctx->stream;
-  int mcp = 0;
-  const int mc = choose_chunk<Real>(s, plan->ctx->num_sms, plan->ctx->smem_optin, mcp);
-  if (!mc) {
-    set_error("sweep front needs more shared memory than one CTA can have (" + std::to_string(s.max_slots) +
-              " slots)");
+  const int rows = s.max_slots + 2 + s.max_src;
+  const int mcp = choose_mcp<Real>(s, rows, plan->ctx->num_sms, plan->ctx->smem_optin);
+  if (!mcp) {
+    set_error("sweep front needs more shared memory than one CTA can have (" + std::to_string(rows) + " rows)");
     return OBTE_ERR_UNSUPPORTED;
   }
-  d.mc = mc;
+  d.mc = mcp;
   d.mcp = mcp;
-  d.n_chunks = (s.n_mfp + mc - 1) / mc;
+  d.n_chunks = (s.n_mfp + mcp - 1) / mcp;
   d.zero_slot = s.max_slots;
-  d.smem = SmemLayout<Real>(mcp, s.ds, s.max_slots + 1).total;
+  d.rows = rows;
+  d.smem = SmemLayout<Real>(mcp, rows).total;
   // split levels into units of at most kUnit elements (slots were assigned per level, so this stays valid)
   std::vector<int32_t> kptr;
   std::vector<int64_t> koff(s.n_dir);
@@ -507,7 +533,7 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
     kn[q] = units;
   }
   Packed pk;
-  OBTE_TRY(pack<Real>(s, d.zero_slot, pk));
+  OBTE_TRY(pack<Real>(s, pk));
   OBTE_TRY(upload(d.rec, pk.rec, st));
   OBTE_TRY(upload(d.cellmap, pk.cellmap, st));
   OBTE_TRY(upload(d.Pq, pk.P, st));
@@ -548,7 +574,7 @@ obte_status ensure_tables(obte_plan plan, bool fp32) {
 
 // ---- launch -----------------------------------------------------------------------
 
-template <typename Real, int NF, bool FINAL>
+template <typename Real, int NF, int MCP, bool FINAL>
 static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                bool with_src, double* Jraw, double* K, double* S) {
   const Schedule& s = plan->sched;
@@ -561,19 +587,19 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
       d.vals.as<Real>());
   count_launch();
   OBTE_CUDA(cudaGetLastError());
-  auto kern = bte_sweep_kernel<Real, NF, FINAL>;
+  auto kern = bte_sweep_kernel<Real, NF, MCP, FINAL>;
   OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
   SweepParams<Real> p;
-  p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds;
-  p.mc = d.mc; p.mcp = d.mcp; p.n_chunks = d.n_chunks; p.zero_slot = d.zero_slot;
+  p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
+  p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;
   p.rec = d.rec.as<int32_t>(); p.vals = d.vals.as<Real>();
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
   p.x_base = plan->x_base_dev.as<int64_t>();
-  p.si = d.si.as<int32_t>(); p.sr = d.sr.as<Real>();
+  p.si = d.si.as<int32_t>();
   p.wo_wall = d.wo_wall.as<int32_t>();
   p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_gg = d.wo_gg.as<Real>();
-  p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>(); p.m_pad = s.m_pad;
-  p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S = S;
+  p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
+  p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S_out = S;
   p.err = plan->err.as<int>();
   const int grid = s.n_dir * d.n_chunks;
   kern<<<grid, kUnit, d.smem, st>>>(p);
@@ -582,15 +608,15 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   return OBTE_OK;
 }
 
-template <typename Real>
-static obte_status launch_nf(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
-                             bool with_src, bool final_pass, double* Jraw, double* K, double* S) {
+template <typename Real, int MCP>
+static obte_status launch_w(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out, bool with_src,
+                            bool final_pass, double* Jraw, double* K, double* S) {
   if (plan->sched.nf == 3) {
-    if (final_pass) return launch_impl<Real, 3, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
-    return launch_impl<Real, 3, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+    if (final_pass) return launch_impl<Real, 3, MCP, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+    return launch_impl<Real, 3, MCP, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
   }
-  if (final_pass) return launch_impl<Real, 4, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
-  return launch_impl<Real, 4, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  if (final_pass) return launch_impl<Real, 4, MCP, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  return launch_impl<Real, 4, MCP, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
 }
 
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
@@ -602,8 +628,17 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
   if (s.nf > 4) { set_error("elements with more than 4 sides are not supported"); return OBTE_ERR_UNSUPPORTED; }
   OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
   if (final_pass) OBTE_CUDA(cudaMemsetAsync(Jraw, 0, (size_t)s.n * s.ds * sizeof(double), st));
-  if (fp32) return launch_nf<float>(plan, plan->d32, u_in, u_out, with_src, final_pass, Jraw, K, S);
-  return launch_nf<double>(plan, plan->d64, u_in, u_out, with_src, final_pass, Jraw, K, S);
+  const DevSchedule& d = fp32 ? plan->d32 : plan->d64;
+#define OBTE_W(R, M) \
+  case M: return launch_w<R, M>(plan, d, u_in, u_out, with_src, final_pass, Jraw, K, S)
+  if (fp32) {
+    switch (d.mcp) { OBTE_W(float, 8); OBTE_W(float, 12); OBTE_W(float, 16); OBTE_W(float, 24); OBTE_W(float, 32); }
+  } else {
+    switch (d.mcp) { OBTE_W(double, 4); OBTE_W(double, 8); OBTE_W(double, 12); OBTE_W(double, 16); }
+  }
+#undef OBTE_W
+  set_error("no compiled sweep kernel for this chunk width");
+  return OBTE_ERR_UNSUPPORTED;
 }
 
 // Device error word: nonzero after a bounded wait gave up (cleared on read).
