@@ -95,6 +95,8 @@ struct Schedule {
   // wall outputs: entries (q, wall) with their re-emission weights
   std::vector<int32_t> wo_wall;    // [n_wo]
   std::vector<double> wo_gg;       // [n_wo * m_pad]  (-GG, i.e. >= 0)
+  std::vector<int32_t> wo_off;     // [n_dir+1] first wall-output entry of each direction
+  int max_wo = 0;                  // most wall-output entries of one direction
   // contact
   std::vector<double> kcoef;       // [n_ce * m_pad]
   std::vector<double> scoef;       // [n_ce]
@@ -123,7 +125,8 @@ struct DevSchedule {
   bool ready = false;
   int mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;
   size_t smem = 0;
-  DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap, Pq, si, sr;
+  DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap, Pq, si, sr,
+      wo_off;
   size_t bytes() const;
 };
 

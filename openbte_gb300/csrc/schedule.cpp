@@ -196,6 +196,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.x_cell.clear();
   s.wo_wall.clear();
   s.wo_gg.clear();
+  s.wo_off.assign(n_dir + 1, 0);
+  s.max_wo = 0;
   s.kcoef.clear();
   s.scoef.clear();
   s.max_slots = 0;
@@ -359,6 +361,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       s.max_slots = std::max(s.max_slots, (int)next);
     }
 
+    s.wo_off[q] = (int32_t)s.wo_wall.size();
     // items in level order
     const size_t base = (size_t)q * n;
     for (int64_t p = 0; p < n; ++p) {
@@ -429,6 +432,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         }
       }
     }
+    s.wo_off[q + 1] = (int32_t)s.wo_wall.size();
+    s.max_wo = std::max(s.max_wo, s.wo_off[q + 1] - s.wo_off[q]);
     // alpha term of K (bte.py:243)
     if (ck == OBTE_CONTACT_PERIODIC || ck == OBTE_CONTACT_MIXED)
       for (int m = 0; m < n_mfp; ++m) {

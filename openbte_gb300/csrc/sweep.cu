@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 
@@ -40,11 +41,17 @@ namespace obte {
 static constexpr int kUnit = 128;      // elements per level unit = threads per CTA
 
 // ---- packed element records -------------------------------------------------------
-// FP32: 12 words (48 B) : cell slot special s0 s1 s2 s3 | c0 c1 c2 c3 D
-// FP64: 20 words (80 B) : cell slot special s0 s1 s2 s3 pad | c0 c1 c2 c3 D (8 B each) | pad
+// FP32: 16 words (64 B) : cell slot special s0 s1 s2 s3 | c0 c1 c2 c3 D | xk wout contact pad
+// FP64: 20 words (80 B) : cell slot special s0 s1 s2 s3 xk | c0 c1 c2 c3 D (8 B each) | wout contact
+// special >= 0 marks elements with wall inflow (folded into p by the values kernel) or per-MFP
+// outputs: xk (periodic source index), wout (wall re-emission entries), contact (kappa entry).
 template <typename Real> struct Rec;
-template <> struct Rec<float> { static constexpr int W = 12, COEF = 7, CSTEP = 1, D = 11; };
-template <> struct Rec<double> { static constexpr int W = 20, COEF = 8, CSTEP = 2, D = 16; };
+template <> struct Rec<float> {
+  static constexpr int W = 16, COEF = 7, CSTEP = 1, D = 11, XK = 12, WOUT = 13, CONTACT = 14;
+};
+template <> struct Rec<double> {
+  static constexpr int W = 20, COEF = 8, CSTEP = 2, D = 16, XK = 7, WOUT = 18, CONTACT = 19;
+};
 
 // special-element table
 //   si: xk wout contact nwall w0 w1 w2 pad     (8 ints)
@@ -73,6 +80,15 @@ static obte_status pack(const Schedule& s, Packed& pk) {
     r[0] = s.cell[it];
     r[1] = s.slot[it] >= 0 ? s.slot[it] : trash_row;
     r[2] = -1;
+    r[Rec<Real>::XK] = s.xk[it];
+    r[Rec<Real>::CONTACT] = s.contact[it];
+    // wall re-emission entries: begin relative to the direction's first entry (staged in shared memory)
+    if (s.wout[it]) {
+      const int32_t wb = s.wout[it] >> 3, wn = s.wout[it] & 7;
+      r[Rec<Real>::WOUT] = ((wb - s.wo_off[it / s.n]) << 3) | wn;
+    } else {
+      r[Rec<Real>::WOUT] = 0;
+    }
     pk.cellmap[it] = s.cell[it];
     pk.P[it] = s.P[it];
     int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0};
@@ -208,7 +224,8 @@ struct SweepParams {
   const int64_t* __restrict__ lev_off;
   const int32_t* __restrict__ nlev;
   const int64_t* __restrict__ x_base;
-  const int32_t* __restrict__ si;
+  const int32_t* __restrict__ wo_off;   // [n_dir+1] first wall-output entry of each direction
+  int max_wo;
   const int32_t* __restrict__ wo_wall;
   const Real* __restrict__ mfp;    // [m_pad]
   const Real* __restrict__ tco;    // [n_dir * m_pad]
@@ -246,21 +263,24 @@ __device__ __forceinline__ double recip(double x) {
 }
 
 // Shared memory layout (bytes):
-//   [0,16) mbarriers  [16,24) abort flags  [128, ...) rec0 rec1 vals0 vals1 | sig | K S | ring
+//   [0,64) mbarriers  [64,72) abort flags  [128, ...) NBUF x (records, values) | sig | K S | wall weights | ring
+static constexpr int NBUF = 4;   // TMA pipeline depth (units in flight)
+
 template <typename Real>
 struct SmemLayout {
-  size_t rec0, rec1, val0, val1, sig, kacc, sacc, ring, total;
-  __host__ __device__ SmemLayout(int mcp, int rows) {
+  size_t rec, val, rec_stride, val_stride, sig, kacc, sacc, gg, ring, total;
+  __host__ __device__ SmemLayout(int mcp, int rows, int max_wo) {
     constexpr int W = Rec<Real>::W;
     size_t o = 128;
-    rec0 = o; o += (size_t)kUnit * W * 4;
-    rec1 = o; o += (size_t)kUnit * W * 4;
-    val0 = o; o += (size_t)(kUnit + 2) * 2 * sizeof(Real);
-    val1 = o; o += (size_t)(kUnit + 2) * 2 * sizeof(Real);
-    o = (o + 15) & ~(size_t)15;
+    rec_stride = (size_t)kUnit * W * 4;
+    val_stride = (size_t)(kUnit + 2) * 2 * sizeof(Real);
+    val_stride = (val_stride + 15) & ~(size_t)15;
+    rec = o; o += NBUF * rec_stride;
+    val = o; o += NBUF * val_stride;
     sig = o; o += (size_t)mcp * 3 * sizeof(Real);
     kacc = o; o += (size_t)mcp * sizeof(Real);
     sacc = o; o += (size_t)mcp * sizeof(Real);
+    gg = o; o += (size_t)max_wo * mcp * sizeof(Real);
     o = (o + 15) & ~(size_t)15;
     ring = o; o += (size_t)mcp * rows * sizeof(Real);
     total = o;
@@ -273,17 +293,14 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
   extern __shared__ __align__(128) unsigned char smem[];
   const int rows = p.rows;
-  const SmemLayout<Real> L(MCP, rows);
+  const SmemLayout<Real> L(MCP, rows, p.max_wo);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
-  int* s_abort = reinterpret_cast<int*>(smem + 16);
-  int32_t* const recb0 = reinterpret_cast<int32_t*>(smem + L.rec0);
-  int32_t* const recb1 = reinterpret_cast<int32_t*>(smem + L.rec1);
-  unsigned char* const valb0 = smem + L.val0;
-  unsigned char* const valb1 = smem + L.val1;
+  int* s_abort = reinterpret_cast<int*>(smem + 64);
   Real* s_sig = reinterpret_cast<Real*>(smem + L.sig);
   Real* s_k = reinterpret_cast<Real*>(smem + L.kacc);
   Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
-  Real* ring = reinterpret_cast<Real*>(smem + L.ring);   // [MCP][rows]
+  Real* s_gg = reinterpret_cast<Real*>(smem + L.gg);      // [wall entry of q][MCP]
+  Real* ring = reinterpret_cast<Real*>(smem + L.ring);    // [MCP][rows]
 
   const int q = blockIdx.x / p.n_chunks;
   const int chunk = blockIdx.x - q * p.n_chunks;
@@ -298,6 +315,8 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   const int64_t val_q0 = (int64_t)q * p.n * VB;
   const int64_t xq = p.x_base[q];
   const int nsrc = (int)(p.x_base[q + 1] - xq);
+  const int wo0 = p.wo_off[q];
+  const int nwo = p.wo_off[q + 1] - wo0;
   const double* __restrict__ X = p.u_in + p.n + p.nd;
   double* __restrict__ dT_out = p.u_out;
   double* __restrict__ TB_out = p.u_out + p.n;
@@ -319,6 +338,10 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
       s_s[j] = 0;
     }
   }
+  for (int i = tid; i < nwo * MCP; i += blockDim.x) {
+    const int e = i / MCP, mm = i - e * MCP;
+    s_gg[i] = mm < mc ? p.wo_gg[(int64_t)(wo0 + e) * p.m_pad + m0 + mm] : Real(0);
+  }
   // ring: zero the slot/zero/trash rows, fill the periodic-source rows from the state vector
   for (int i = tid; i < MCP * rows; i += blockDim.x) {
     const int mm = i / rows, row = i - mm * rows;
@@ -328,57 +351,60 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
     ring[i] = v;
   }
   if (tid == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    for (int i = 0; i < NBUF; ++i) mbar_init(&bars[i], 1);
     s_abort[0] = 0;
     s_abort[1] = 0;
     fence_mbar_init();
   }
   __syncthreads();
 
-  // TMA of unit u into buffer u&1: records [a, e) and values [a, e) (values in a 16-B aligned window)
+  // TMA of unit u into buffer u % NBUF: records [a, e) and values [a, e) (16-B aligned window)
   auto issue = [&](int u) {
     const int a = lev[u], e = lev[u + 1];
+    const int bi = u % NBUF;
     const unsigned rbytes = (unsigned)(e - a) * W * 4u;
     const int64_t vb0 = (val_q0 + (int64_t)a * VB) & ~(int64_t)15;
     const int64_t vb1 = (val_q0 + (int64_t)e * VB + 15) & ~(int64_t)15;
     const unsigned vbytes = (unsigned)(vb1 - vb0);
-    uint64_t* bar = &bars[u & 1];
+    uint64_t* bar = &bars[bi];
     fence_proxy_async();
     mbar_expect_tx(bar, rbytes + vbytes);
-    tma_load_1d((u & 1) ? recb1 : recb0, rec_q + (int64_t)a * W, rbytes, bar);
-    tma_load_1d((u & 1) ? valb1 : valb0, val_base + vb0, vbytes, bar);
+    tma_load_1d(smem + L.rec + bi * L.rec_stride, rec_q + (int64_t)a * W, rbytes, bar);
+    tma_load_1d(smem + L.val + bi * L.val_stride, val_base + vb0, vbytes, bar);
   };
-  if (tid == 0) issue(0);
+  if (tid == 0)
+    for (int u = 0; u < NBUF - 1 && u < nlev; ++u) issue(u);
 
   for (int u = 0; u < nlev; ++u) {
+    const int bi = u % NBUF;
     const int cur = u & 1;
     const int a = lev[u], e = lev[u + 1];
-    const bool next = u + 1 < nlev;
-    if (tid == 0 && next) issue(u + 1);
-    const bool ready = mbar_wait_bounded(&bars[cur], (unsigned)(u >> 1) & 1u);
+    // buffer (u + NBUF - 1) % NBUF was last read during unit u - 1, finished at the barrier below
+    if (tid == 0 && u + NBUF - 1 < nlev) issue(u + NBUF - 1);
+    const bool ready = mbar_wait_bounded(&bars[bi], (unsigned)(u / NBUF) & 1u);
     if (!ready) {
       s_abort[cur] = 1;
       atomicOr(p.err, 1);
     } else if (tid < e - a) {
       // record: W/4 vector loads
       int32_t r[W];
-      const int4* r4 = reinterpret_cast<const int4*>((cur ? recb1 : recb0) + tid * W);
+      const int4* r4 = reinterpret_cast<const int4*>(smem + L.rec + bi * L.rec_stride) + tid * (W / 4);
 #pragma unroll
       for (int i = 0; i < W / 4; ++i) {
         const int4 x = r4[i];
         r[4 * i] = x.x; r[4 * i + 1] = x.y; r[4 * i + 2] = x.z; r[4 * i + 3] = x.w;
       }
       const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
-      const Real* v = reinterpret_cast<const Real*>(cur ? valb1 : valb0) + 2 * (voff + tid);
+      const Real* v = reinterpret_cast<const Real*>(smem + L.val + bi * L.val_stride) + 2 * (voff + tid);
       const Real b = v[0], pw = v[1];
-      const int c = r[0], so = r[1], sp = r[2];
+      const int c = r[0], so = r[1];
       const int s0 = r[3], s1 = r[4], s2 = r[5], s3 = r[6];
       const Real c0 = word_real<Real>(r, Rec<Real>::COEF);
       const Real c1 = word_real<Real>(r, Rec<Real>::COEF + Rec<Real>::CSTEP);
       const Real c2 = word_real<Real>(r, Rec<Real>::COEF + 2 * Rec<Real>::CSTEP);
       const Real c3 = word_real<Real>(r, Rec<Real>::COEF + 3 * Rec<Real>::CSTEP);
       const Real D = word_real<Real>(r, Rec<Real>::D);
+      const int xk = r[Rec<Real>::XK], wo = r[Rec<Real>::WOUT], ce = r[Rec<Real>::CONTACT];
       Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
 #pragma unroll
       for (int mb = 0; mb < MCP; mb += 4) {
@@ -412,32 +438,32 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
         if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
         if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
       }
-      // per-MFP outputs of special elements, read back from their own row
-      if (sp >= 0) {
-        const int32_t* si = p.si + (int64_t)sp * SI;
-        const int xk = si[0], wo = si[1], ce = si[2];
+      // per-MFP outputs of special elements, read back from their own row (shared memory only)
+      if (xk >= 0 || wo != 0 || (FINAL && ce >= 0)) {
         const int wb = wo >> 3, wn = wo & 7;
         Real w0 = 0, w1 = 0, w2 = 0;
         for (int mm = 0; mm < mc; ++mm) {
           const Real T = ring[(size_t)mm * rows + so];
           if (xk >= 0) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)T;
-          if (wn > 0) w0 += p.wo_gg[(int64_t)wb * p.m_pad + m0 + mm] * T;
-          if (wn > 1) w1 += p.wo_gg[(int64_t)(wb + 1) * p.m_pad + m0 + mm] * T;
-          if (wn > 2) w2 += p.wo_gg[(int64_t)(wb + 2) * p.m_pad + m0 + mm] * T;
+          if (wn > 0) w0 += s_gg[wb * MCP + mm] * T;
+          if (wn > 1) w1 += s_gg[(wb + 1) * MCP + mm] * T;
+          if (wn > 2) w2 += s_gg[(wb + 2) * MCP + mm] * T;
           if (FINAL && ce >= 0) {
             atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * T);
             atomicAdd(&s_s[mm], p.scoef[ce] * T);
           }
         }
-        if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wb]], (double)w0);
-        if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wb + 1]], (double)w1);
-        if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wb + 2]], (double)w2);
+        if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
+        if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 1]], (double)w1);
+        if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 2]], (double)w2);
       }
     }
     __syncthreads();
     // a flag raised during unit u lives in word u&1; unit u+1 writes the other word
     if (s_abort[cur]) {
-      if (tid == 0 && next) mbar_wait_bounded(&bars[cur ^ 1], (unsigned)((u + 1) >> 1) & 1u);
+      // let the copies this CTA still has in flight land before leaving (bounded)
+      if (tid == 0)
+        for (int w = u + 1; w < nlev && w < u + NBUF; ++w) mbar_wait_bounded(&bars[w % NBUF], (unsigned)(w / NBUF) & 1u);
       __syncthreads();
       return;
     }
@@ -454,7 +480,7 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
 
 size_t DevSchedule::bytes() const {
   const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &mfp, &tco, &sig, &wo_wall, &wo_gg, &kcoef, &scoef, &hs,
-                         &vals, &cellmap, &Pq, &si, &sr};
+                         &vals, &cellmap, &Pq, &si, &sr, &wo_off};
   size_t b = 0;
   for (auto* x : all) b += x->bytes;
   return b;
@@ -469,7 +495,7 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
 
 // Chunk widths compiled for each precision.
 template <typename Real> struct Widths;
-template <> struct Widths<float> { static constexpr int N = 5; static constexpr int v[N] = {8, 12, 16, 24, 32}; };
+template <> struct Widths<float> { static constexpr int N = 5; static constexpr int v[N] = {4, 8, 12, 16, 24}; };
 template <> struct Widths<double> { static constexpr int N = 4; static constexpr int v[N] = {4, 8, 12, 16}; };
 constexpr int Widths<float>::v[];
 constexpr int Widths<double>::v[];
@@ -485,7 +511,7 @@ static int choose_mcp(const Schedule& s, int rows, int num_sms, size_t optin) {
   for (int i = 0; i < Widths<Real>::N; ++i) {
     const int w = Widths<Real>::v[i];
     if (forced && w != forced) continue;
-    const size_t sm = SmemLayout<Real>(w, rows).total;
+    const size_t sm = SmemLayout<Real>(w, rows, s.max_wo).total;
     if (sm > optin) continue;
     const int per_sm = std::max(1, std::min(8, (int)((228 * 1024) / (sm + 1024))));
     const int chunks = (s.n_mfp + w - 1) / w;
@@ -493,8 +519,9 @@ static int choose_mcp(const Schedule& s, int rows, int num_sms, size_t optin) {
     const int64_t slots = (int64_t)num_sms * per_sm;
     const int64_t waves = (ctas + slots - 1) / slots;
     // per-CTA time ~ units x (overhead + w); resident CTAs share the SM's issue slots
-    const double per_cta = 40.0 + w;
-    const double cost = (double)waves * per_cta * std::min<int64_t>(per_sm, ctas / num_sms + 1) / 4.0;
+    // measured on a 60k-element mesh: per-unit overhead ~ 16 MFP-iterations; co-resident CTAs overlap
+    const double per_cta = 16.0 + w;
+    const double cost = (double)waves * per_cta / std::sqrt((double)std::min<int64_t>(per_sm, 4));
     if (cost < best) { best = cost; best_w = w; }
   }
   return best_w;
@@ -515,7 +542,7 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   d.n_chunks = (s.n_mfp + mcp - 1) / mcp;
   d.zero_slot = s.max_slots;
   d.rows = rows;
-  d.smem = SmemLayout<Real>(mcp, rows).total;
+  d.smem = SmemLayout<Real>(mcp, rows, s.max_wo).total;
   // split levels into units of at most kUnit elements (slots were assigned per level, so this stays valid)
   std::vector<int32_t> kptr;
   std::vector<int64_t> koff(s.n_dir);
@@ -545,6 +572,7 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   std::vector<int32_t> wo = s.wo_wall;
   if (wo.empty()) wo.push_back(0);
   OBTE_TRY(upload(d.wo_wall, wo, st));
+  OBTE_TRY(upload(d.wo_off, s.wo_off, st));
   OBTE_TRY(upload_real<Real>(d.mfp, s.mfp, st));
   OBTE_TRY(upload_real<Real>(d.tco, s.tco, st));
   OBTE_TRY(upload_real<Real>(d.sig, s.sig, st));
@@ -595,7 +623,8 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.rec = d.rec.as<int32_t>(); p.vals = d.vals.as<Real>();
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
   p.x_base = plan->x_base_dev.as<int64_t>();
-  p.si = d.si.as<int32_t>();
+  p.wo_off = d.wo_off.as<int32_t>();
+  p.max_wo = s.max_wo;
   p.wo_wall = d.wo_wall.as<int32_t>();
   p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_gg = d.wo_gg.as<Real>();
   p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
@@ -632,7 +661,7 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
 #define OBTE_W(R, M) \
   case M: return launch_w<R, M>(plan, d, u_in, u_out, with_src, final_pass, Jraw, K, S)
   if (fp32) {
-    switch (d.mcp) { OBTE_W(float, 8); OBTE_W(float, 12); OBTE_W(float, 16); OBTE_W(float, 24); OBTE_W(float, 32); }
+    switch (d.mcp) { OBTE_W(float, 4); OBTE_W(float, 8); OBTE_W(float, 12); OBTE_W(float, 16); OBTE_W(float, 24); }
   } else {
     switch (d.mcp) { OBTE_W(double, 4); OBTE_W(double, 8); OBTE_W(double, 12); OBTE_W(double, 16); }
   }
