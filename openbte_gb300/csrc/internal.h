@@ -126,7 +126,7 @@ struct DevSchedule {
   int mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;
   size_t smem = 0;
   DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap, Pq, si, sr,
-      wo_off;
+      wo_off, spec;
   size_t bytes() const;
 };
 

@@ -41,17 +41,15 @@ namespace obte {
 static constexpr int kUnit = 128;      // elements per level unit = threads per CTA
 
 // ---- packed element records -------------------------------------------------------
-// FP32: 16 words (64 B) : cell slot special s0 s1 s2 s3 | c0 c1 c2 c3 D | xk wout contact pad
-// FP64: 20 words (80 B) : cell slot special s0 s1 s2 s3 xk | c0 c1 c2 c3 D (8 B each) | wout contact
-// special >= 0 marks elements with wall inflow (folded into p by the values kernel) or per-MFP
-// outputs: xk (periodic source index), wout (wall re-emission entries), contact (kappa entry).
+// Integer words (both precisions), ring rows and indices in 16-bit halves:
+//   w0 cell | w1 so, s0 | w2 s1, s2 | w3 s3, xk+1 | w4 wout | w5 contact+1
+// then the reals c0 c1 c2 c3 D:  FP32 words 6..10 (+1 pad) = 12 words (48 B);
+//                                FP64 words 6..15          = 16 words (64 B).
+// so = output row, s* = inflow rows, xk = periodic source index, wout = wall re-emission
+// entries (begin << 3 | count, begin relative to the direction), contact = kappa entry.
 template <typename Real> struct Rec;
-template <> struct Rec<float> {
-  static constexpr int W = 16, COEF = 7, CSTEP = 1, D = 11, XK = 12, WOUT = 13, CONTACT = 14;
-};
-template <> struct Rec<double> {
-  static constexpr int W = 20, COEF = 8, CSTEP = 2, D = 16, XK = 7, WOUT = 18, CONTACT = 19;
-};
+template <> struct Rec<float> { static constexpr int W = 12, COEF = 6, CSTEP = 1, D = 10; };
+template <> struct Rec<double> { static constexpr int W = 16, COEF = 6, CSTEP = 2, D = 14; };
 
 // special-element table
 //   si: xk wout contact nwall w0 w1 w2 pad     (8 ints)
@@ -59,7 +57,7 @@ template <> struct Rec<double> {
 static constexpr int SI = 8, SR = 4;
 
 struct Packed {
-  std::vector<int32_t> rec, cellmap, si;
+  std::vector<int32_t> rec, cellmap, si, spec;
   std::vector<double> P, sr;
 };
 
@@ -69,26 +67,24 @@ static obte_status pack(const Schedule& s, Packed& pk) {
   constexpr int W = Rec<Real>::W;
   const int S = s.max_slots;
   const int zero_row = S, trash_row = S + 1, per_row = S + 2;
+  if (S + 2 + s.max_src >= 65535) {
+    set_error("sweep ring rows do not fit 16-bit indices");
+    return OBTE_ERR_UNSUPPORTED;
+  }
   const size_t total = (size_t)s.n_dir * s.n;
   pk.rec.assign(total * W, 0);
   pk.cellmap.assign(total, 0);
+  pk.spec.assign(total, -1);
   pk.P.assign(total, 0.0);
   pk.si.clear();
   pk.sr.clear();
   for (size_t it = 0; it < total; ++it) {
     int32_t* r = pk.rec.data() + it * W;
+    const int32_t so = s.slot[it] >= 0 ? s.slot[it] : trash_row;
     r[0] = s.cell[it];
-    r[1] = s.slot[it] >= 0 ? s.slot[it] : trash_row;
-    r[2] = -1;
-    r[Rec<Real>::XK] = s.xk[it];
-    r[Rec<Real>::CONTACT] = s.contact[it];
     // wall re-emission entries: begin relative to the direction's first entry (staged in shared memory)
-    if (s.wout[it]) {
-      const int32_t wb = s.wout[it] >> 3, wn = s.wout[it] & 7;
-      r[Rec<Real>::WOUT] = ((wb - s.wo_off[it / s.n]) << 3) | wn;
-    } else {
-      r[Rec<Real>::WOUT] = 0;
-    }
+    r[4] = s.wout[it] ? (((s.wout[it] >> 3) - s.wo_off[it / s.n]) << 3) | (s.wout[it] & 7) : 0;
+    r[5] = s.contact[it] + 1;
     pk.cellmap[it] = s.cell[it];
     pk.P[it] = s.P[it];
     int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0};
@@ -119,9 +115,11 @@ static obte_status pack(const Schedule& s, Packed& pk) {
         special = true;
       }
     }
-    for (int f = 0; f < 4; ++f) r[3 + f] = row_in[f];
+    r[1] = (so & 0xFFFF) | (row_in[0] << 16);
+    r[2] = (row_in[1] & 0xFFFF) | (row_in[2] << 16);
+    r[3] = (row_in[3] & 0xFFFF) | ((s.xk[it] + 1) << 16);
     if (special) {
-      r[2] = (int32_t)(pk.si.size() / SI);
+      pk.spec[it] = (int32_t)(pk.si.size() / SI);
       pk.si.insert(pk.si.end(), si, si + SI);
       pk.sr.insert(pk.sr.end(), sr, sr + SR);
     }
@@ -187,7 +185,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
 // ---- per-sweep values: b = DeltaT + h, p = P - sum_walls g_w T_B ------------------
 template <typename Real>
 __global__ void sweep_values_kernel(const int32_t* __restrict__ cellmap, const double* __restrict__ Pq,
-                                    const int32_t* __restrict__ rec, int W, const int32_t* __restrict__ si,
+                                    const int32_t* __restrict__ spec, const int32_t* __restrict__ si,
                                     const Real* __restrict__ sr, const double* __restrict__ u_in, int64_t n,
                                     const double* __restrict__ hs, int with_src, int64_t total, Real* __restrict__ vals) {
   const double* TB = u_in + n;
@@ -199,7 +197,7 @@ __global__ void sweep_values_kernel(const int32_t* __restrict__ cellmap, const d
       if (hs) b += hs[c];
       pp = Pq[it];
     }
-    const int sp = rec[it * W + 2];
+    const int sp = spec[it];
     if (sp >= 0) {
       const int32_t* s = si + (int64_t)sp * SI;
       const Real* r = sr + (int64_t)sp * SR;
@@ -264,7 +262,7 @@ __device__ __forceinline__ double recip(double x) {
 
 // Shared memory layout (bytes):
 //   [0,64) mbarriers  [64,72) abort flags  [128, ...) NBUF x (records, values) | sig | K S | wall weights | ring
-static constexpr int NBUF = 4;   // TMA pipeline depth (units in flight)
+static constexpr int NBUF = 3;   // TMA pipeline depth (units in flight)
 
 template <typename Real>
 struct SmemLayout {
@@ -397,14 +395,16 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
       const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
       const Real* v = reinterpret_cast<const Real*>(smem + L.val + bi * L.val_stride) + 2 * (voff + tid);
       const Real b = v[0], pw = v[1];
-      const int c = r[0], so = r[1];
-      const int s0 = r[3], s1 = r[4], s2 = r[5], s3 = r[6];
+      const int c = r[0];
+      const int so = r[1] & 0xFFFF, s0 = (int)((unsigned)r[1] >> 16);
+      const int s1 = r[2] & 0xFFFF, s2 = (int)((unsigned)r[2] >> 16);
+      const int s3 = r[3] & 0xFFFF, xk = (int)((unsigned)r[3] >> 16) - 1;
+      const int wo = r[4], ce = r[5] - 1;
       const Real c0 = word_real<Real>(r, Rec<Real>::COEF);
       const Real c1 = word_real<Real>(r, Rec<Real>::COEF + Rec<Real>::CSTEP);
       const Real c2 = word_real<Real>(r, Rec<Real>::COEF + 2 * Rec<Real>::CSTEP);
       const Real c3 = word_real<Real>(r, Rec<Real>::COEF + 3 * Rec<Real>::CSTEP);
       const Real D = word_real<Real>(r, Rec<Real>::D);
-      const int xk = r[Rec<Real>::XK], wo = r[Rec<Real>::WOUT], ce = r[Rec<Real>::CONTACT];
       Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
 #pragma unroll
       for (int mb = 0; mb < MCP; mb += 4) {
@@ -441,16 +441,32 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
       // per-MFP outputs of special elements, read back from their own row (shared memory only)
       if (xk >= 0 || wo != 0 || (FINAL && ce >= 0)) {
         const int wb = wo >> 3, wn = wo & 7;
+        // gg of absent entries (and padded MFPs) are zero: read the first entry's row instead
+        const Real* g0 = s_gg + wb * MCP;
+        const Real* g1 = s_gg + (wn > 1 ? wb + 1 : wb) * MCP;
+        const Real* g2 = s_gg + (wn > 2 ? wb + 2 : wb) * MCP;
+        Real Ts[MCP];
+#pragma unroll
+        for (int mm = 0; mm < MCP; ++mm) Ts[mm] = ring[(size_t)mm * rows + so];
         Real w0 = 0, w1 = 0, w2 = 0;
-        for (int mm = 0; mm < mc; ++mm) {
-          const Real T = ring[(size_t)mm * rows + so];
-          if (xk >= 0) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)T;
-          if (wn > 0) w0 += s_gg[wb * MCP + mm] * T;
-          if (wn > 1) w1 += s_gg[(wb + 1) * MCP + mm] * T;
-          if (wn > 2) w2 += s_gg[(wb + 2) * MCP + mm] * T;
-          if (FINAL && ce >= 0) {
-            atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * T);
-            atomicAdd(&s_s[mm], p.scoef[ce] * T);
+#pragma unroll
+        for (int mm = 0; mm < MCP; ++mm) {
+          w0 += g0[mm] * Ts[mm];
+          w1 += g1[mm] * Ts[mm];
+          w2 += g2[mm] * Ts[mm];
+        }
+        if (xk >= 0) {
+#pragma unroll
+          for (int mm = 0; mm < MCP; ++mm)
+            if (mm < mc) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)Ts[mm];
+        }
+        if (FINAL && ce >= 0) {
+#pragma unroll
+          for (int mm = 0; mm < MCP; ++mm) {
+            if (mm < mc) {
+              atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * Ts[mm]);
+              atomicAdd(&s_s[mm], p.scoef[ce] * Ts[mm]);
+            }
           }
         }
         if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
@@ -565,6 +581,7 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   OBTE_TRY(upload(d.cellmap, pk.cellmap, st));
   OBTE_TRY(upload(d.Pq, pk.P, st));
   OBTE_TRY(upload(d.si, pk.si, st));
+  OBTE_TRY(upload(d.spec, pk.spec, st));
   OBTE_TRY(upload_real<Real>(d.sr, pk.sr, st));
   OBTE_TRY(upload(d.klev_ptr, kptr, st));
   OBTE_TRY(upload(d.klev_off, koff, st));
@@ -610,7 +627,7 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   const int64_t total = (int64_t)s.n_dir * s.n;
   const int vblocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)plan->ctx->num_sms * 8);
   sweep_values_kernel<Real><<<vblocks, 256, 0, st>>>(
-      d.cellmap.as<int32_t>(), d.Pq.as<double>(), d.rec.as<int32_t>(), Rec<Real>::W, d.si.as<int32_t>(),
+      d.cellmap.as<int32_t>(), d.Pq.as<double>(), d.spec.as<int32_t>(), d.si.as<int32_t>(),
       d.sr.as<Real>(), u_in, s.n, s.hs.empty() ? nullptr : d.hs.as<double>(), with_src ? 1 : 0, total,
       d.vals.as<Real>());
   count_launch();
