@@ -212,6 +212,7 @@ def main():
 
     from openbte_gb300 import _lib
     from openbte_gb300.bte import BTE_RTA, solve_plan
+    from openbte_gb300.fourier import Fourier, get_fourier_plan
     from openbte_gb300.runtime import HostProblem, get_plan
     lib = _lib.load()
 
@@ -242,8 +243,12 @@ def main():
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    fplan = get_fourier_plan(geo, mat.thermal_conductivity, bcs, ek, [], local)
+
     def one(prec):
-        return solve_plan(plan, dT0, precision=prec, rtol=args.rtol, max_sweeps=2000, restart=40)
+        # one kappa_eff solve: device Fourier first guess, then the BTE source iteration
+        finfo, T0, _ = fplan.solve(device=local)
+        return solve_plan(plan, T0, precision=prec, rtol=args.rtol, max_sweeps=2000, restart=40)
 
     def barrier():
         if world > 1:
@@ -298,11 +303,25 @@ def main():
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        r = BTE_RTA(geo, mat, bcs, effective_thermal_conductivity=ek, bte_rtol=args.rtol, precision=args.precision,
+        f = Fourier(geo, mat.thermal_conductivity, bcs, effective_thermal_conductivity=ek, verbose=False)
+        r = BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=args.rtol,
+                    precision=args.precision,
                     restart=40, max_sweeps=2000)
         e2e_lat.append(time.perf_counter() - t1)
+    # host->device: the Fourier temperature handed to BTE_RTA; device->host: Fourier T and flux,
+    # BTE temperature, flux, per-ordinate kappa and suppression
     h2d = geo.n_elems * 8
-    d2h = geo.n_elems * 8 * (1 + np.asarray(mat.sigma).shape[2]) + 2 * n_mfp * n_dir * 8
+    d2h = (geo.n_elems * 8 * (1 + geo.dim) + geo.n_elems * 8 * (1 + np.asarray(mat.sigma).shape[2])
+           + 2 * n_mfp * n_dir * 8)
+    # Fourier alone (device resident)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    finfo, _, _ = fplan.solve(device=local)
+    e1.record(stream)
+    e1.synchronize()
+    fourier_ms = e0.elapsed_time(e1)
 
     # roofline of the dominant kernel: one sweep of every ordinate
     fp32 = args.precision != "fp64"
@@ -338,6 +357,8 @@ def main():
                    "rtol": args.rtol, "l2": "flushed between steps (2x L2 write)",
                    "parallelism": f"replicas{world}" if world > 1 else "single"},
         "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
+        "fourier": {"ms": fourier_ms, "outer_iterations": finfo.n_iter, "cg_iterations": finfo.n_cg,
+                    "kappa": finfo.kappa},
         "fp64": {"solves_per_s": 1.0 / float(np.median(lat64)), "ms": float(np.median(lat64) * 1e3),
                  "sweeps": i64.n_sweeps},
         "speedup_vs_fp64": float(np.median(lat64) / t_step),
