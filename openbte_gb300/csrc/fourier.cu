@@ -109,6 +109,90 @@ __global__ void cg_direction_kernel(int64_t n, double* __restrict__ sc, double* 
 
 __global__ void copy_scalar_kernel(double* __restrict__ sc, int dst, int src) { sc[dst] = sc[src]; }
 
+// Sum of per-block partials in a fixed order; every block computes the same value, so a
+// kernel can use a grid-wide reduction of the previous kernel without another launch.
+__device__ __forceinline__ double sum_partials(const double* __restrict__ part, int nb) {
+  __shared__ double red[FT / 32];
+  __shared__ double total;
+  double acc = 0;
+  for (int b = threadIdx.x; b < nb; b += FT) acc += part[b];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < FT / 32; ++w) t += red[w];
+    total = t;
+  }
+  __syncthreads();
+  return total;
+}
+
+// one CG step after the SpMV: alpha = rz / sum(pAp partials); x += a p; r -= a Ap; z = r dinv;
+// partials of r.z (next rz) and r.r.  rz is read from sc[cur].
+__global__ void cg_step_kernel(int64_t n, const double* __restrict__ part_pap, int nb, const double* __restrict__ sc,
+                               int cur, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
+                               const double* __restrict__ p, const double* __restrict__ Ap,
+                               const double* __restrict__ dinv, double* __restrict__ part_rz,
+                               double* __restrict__ part_rr) {
+  __shared__ double red[2][FT / 32];
+  const double pap = sum_partials(part_pap, nb);
+  const double a = pap != 0 ? sc[cur] / pap : 0.0;
+  double rz = 0, rr = 0;
+  for (int64_t i = (int64_t)blockIdx.x * FT + threadIdx.x; i < n; i += (int64_t)gridDim.x * FT) {
+    x[i] += a * p[i];
+    const double ri = r[i] - a * Ap[i];
+    r[i] = ri;
+    const double zi = ri * dinv[i];
+    z[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    rz += __shfl_xor_sync(0xffffffffu, rz, o);
+    rr += __shfl_xor_sync(0xffffffffu, rr, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = rz;
+    red[1][threadIdx.x >> 5] = rr;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0;
+    for (int w = 0; w < FT / 32; ++w) { t0 += red[0][w]; t1 += red[1][w]; }
+    part_rz[blockIdx.x] = t0;
+    part_rr[blockIdx.x] = t1;
+  }
+}
+
+// p = z + (rz_new / rz) p with rz_new = sum(rz partials); block 0 stores rz_new in sc[cur^1]
+// and r.r in sc[3] (read by the host between batches)
+__global__ void cg_dir_kernel(int64_t n, const double* __restrict__ part_rz, const double* __restrict__ part_rr,
+                              int nb, double* __restrict__ sc, int cur, double* __restrict__ p,
+                              const double* __restrict__ z) {
+  const double rzn = sum_partials(part_rz, nb);
+  const double rz = sc[cur];
+  const double b = rz != 0 ? rzn / rz : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * FT + threadIdx.x; i < n; i += (int64_t)gridDim.x * FT) p[i] = z[i] + b * p[i];
+  if (blockIdx.x == 0) {
+    const double rr = sum_partials(part_rr, nb);
+    if (threadIdx.x == 0) {
+      sc[cur ^ 1] = rzn;
+      sc[3] = rr;
+    }
+  }
+}
+
+// warm start consistent with the pin: T += (B + C)_N - T_N  (two launches: read, then shift)
+__global__ void pin_delta_kernel(const double* __restrict__ T, const double* __restrict__ B,
+                                 const double* __restrict__ C, int pin, double* __restrict__ out) {
+  *out = B[pin] + C[pin] - T[pin];
+}
+__global__ void shift_by_kernel(int64_t n, double* __restrict__ T, const double* __restrict__ d) {
+  const double v = *d;
+  for (int64_t i = (int64_t)blockIdx.x * FT + threadIdx.x; i < n; i += (int64_t)gridDim.x * FT) T[i] += v;
+}
+
 // r = rhs - Ap; z = r dinv; p = z; partials of r.z, r.r and rhs.rhs
 __global__ void cg_init_kernel(int64_t n, const double* __restrict__ rhs, const double* __restrict__ Ap,
                                const double* __restrict__ dinv, double* __restrict__ r, double* __restrict__ z,
@@ -512,18 +596,19 @@ static obte_status cg_solve(obte_fourier_plan P, double* T, double rtol, int max
     const double tol = rtol * std::max(std::sqrt(std::max(hs[5], 0.0)), 1e-300);
     iters = 0;
     if (std::sqrt(std::max(hs[3], 0.0)) <= tol) return OBTE_OK;
+    // three launches per iteration; rz alternates between sc[0] and sc[1]
     const int check = 8;
+    int cur = 0;
+    double* pp = P->part.as<double>();
+    double* prz = P->part2.as<double>();
+    double* prr = P->part3.as<double>();
     while (iters < max_iter) {
       for (int k = 0; k < check; ++k) {
-        spmv_kernel<<<nb, FT, 0, st>>>(n, rp, ci, val, p, Ap, P->part.as<double>());
-        reduce_kernel<<<1, FT, 0, st>>>(P->part.as<double>(), nb, sc + 1);   // pAp
-        cg_update_kernel<<<nb, FT, 0, st>>>(n, sc, T, r, z, p, Ap, P->dinv.as<double>(), P->part.as<double>(),
-                                            P->part2.as<double>());
-        reduce_kernel<<<1, FT, 0, st>>>(P->part.as<double>(), nb, sc + 2);   // rz_new
-        reduce_kernel<<<1, FT, 0, st>>>(P->part2.as<double>(), nb, sc + 3);  // rr
-        cg_direction_kernel<<<nb, FT, 0, st>>>(n, sc, p, z);
-        copy_scalar_kernel<<<1, 1, 0, st>>>(sc, 0, 2);
-        count_launch(7);
+        spmv_kernel<<<nb, FT, 0, st>>>(n, rp, ci, val, p, Ap, pp);
+        cg_step_kernel<<<nb, FT, 0, st>>>(n, pp, nb, sc, cur, T, r, z, p, Ap, P->dinv.as<double>(), prz, prr);
+        cg_dir_kernel<<<nb, FT, 0, st>>>(n, prz, prr, nb, sc, cur, p, z);
+        count_launch(3);
+        cur ^= 1;
         ++iters;
       }
       OBTE_CUDA(cudaGetLastError());
@@ -556,6 +641,13 @@ extern "C" obte_status obte_fourier_solve(obte_fourier_plan P, const obte_fourie
                                      P->rhs.as<double>());
     count_launch();
     int k = 0;
+    if (P->pin >= 0) {
+      // the previous T was re-centred; shift it back onto the pinned value so the warm start
+      // differs from the new solution only by the change of C (a uniform shift is in L's null space)
+      pin_delta_kernel<<<1, 1, 0, st>>>(T, P->B.as<double>(), C, P->pin, P->sc.as<double>() + 6);
+      shift_by_kernel<<<nb, FT, 0, st>>>(n, T, P->sc.as<double>() + 6);
+      count_launch(2);
+    }
     OBTE_TRY(cg_solve(P, T, cg_rtol, cg_max, k));                                // fourier.py:152
     ncg += k;
     if (P->pin >= 0) {
