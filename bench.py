@@ -51,6 +51,68 @@ def problem(workload):
     return geo, mat, bcs, ek
 
 
+def _stream_mesh(args):
+    """Mesh of one serving request (built in a worker process)."""
+    from openbte_gb300.geometry import porous_cell_2d
+    from openbte_gb300.mesh import mesh_from_cell
+    n_tri, phi, pore, seed = args
+    return mesh_from_cell(porous_cell_2d(n_tri, phi, pore, seed=seed))
+
+
+def serving_stream(n_req, seed=0):
+    """Seeded request mix: porosity U(0.05, 0.40), circle/square pore 50/50, log-uniform 2k-60k triangles,
+    48 or 96 directions, 30-100 MFPs (meshes built in a spawn pool before the stream starts)."""
+    import multiprocessing as mp
+    from openbte_gb300 import objects as O
+    from openbte_gb300.material import synthetic_isotropic_2d
+    from openbte_gb300.serving import Request
+    rng = np.random.default_rng(seed)
+    spec = []
+    for i in range(n_req):
+        phi = float(rng.uniform(0.05, 0.40))
+        pore = "circle" if rng.random() < 0.5 else "square"
+        n_tri = int(round(math.exp(rng.uniform(math.log(2000), math.log(60000)))))
+        n_dir = int(rng.choice([48, 96]))
+        n_mfp = int(rng.integers(30, 101))
+        spec.append((n_tri, phi, pore, 1000 + i, n_dir, n_mfp))
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        meshes = pool.map(_stream_mesh, [(a, b, c, d) for a, b, c, d, _, _ in spec])
+    bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
+    ek = O.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
+    reqs = []
+    for i, (geo, (n_tri, phi, pore, _, n_dir, n_mfp)) in enumerate(zip(meshes, spec)):
+        reqs.append(Request(geo, synthetic_isotropic_2d(n_mfp, n_dir), bcs, ek, rid=i,
+                            tag={"n_elems": geo.n_elems, "phi": phi, "pore": pore, "n_dir": n_dir, "n_mfp": n_mfp}))
+    return reqs
+
+
+def run_serving(n_req, rate, device, slots=4):
+    from openbte_gb300.serving import GPUBackend, Server, replay, summarize
+    reqs = serving_stream(n_req)
+    out = {"requests": n_req, "rate_per_s": rate,
+           "unknowns_per_sweep_mean": float(np.mean([r.tag["n_elems"] * r.tag["n_dir"] * r.tag["n_mfp"]
+                                                     for r in reqs]))}
+    for prec, nslots in (("fp32_refine", slots), ("fp64", 1)):
+        for r in reqs:
+            r.precision = prec
+            r.rtol = 1e-6 if prec == "fp32_refine" else 1e-8
+        srv = Server(backend=GPUBackend(device=device), slots=nslots, builders=4)
+        t0 = time.perf_counter()
+        res = replay(srv, reqs, rate=rate, seed=1)
+        wall = time.perf_counter() - t0
+        srv.close()
+        s = summarize(res, wall)
+        s["slots"] = nslots
+        s["max_concurrent"] = srv.max_concurrent
+        out[prec] = s
+        if prec == "fp32_refine":
+            k32 = {r.rid: r.kappa for r in res}
+        else:
+            errs = [abs(k32[r.rid] - r.kappa) / abs(r.kappa) for r in res if r.status == "ok"]
+            out["kappa_rel_err_fp32_refine_vs_fp64_max"] = float(max(errs)) if errs else None
+    return out
+
+
 def algorithmic_sweep_bytes(geo, mat, b_T):
     """Per-sweep algorithmic bytes: N_cells*N_ord*b_T + N_dir*(4*N_cells + 8*F_d)."""
     n = geo.n_elems
@@ -192,6 +254,9 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-7)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve", type=int, default=0,
+                    help="also replay a seeded serving stream of this many requests (Poisson arrivals)")
+    ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--profile-sweeps", type=int, default=0,
                     help="only build the plan and run this many FP32 and FP64 sweeps (for ncu captures)")
     args = ap.parse_args()
@@ -377,6 +442,8 @@ def main():
         "plan_build_s": plan_s,
         "wall_timed_s": t_total,
     }
+    if args.serve:
+        line["serving"] = run_serving(args.serve, args.serve_rate, local)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geo, mat, bcs, ek)
         line["cpu_baseline"].pop("seconds_per_solve", None)

@@ -102,6 +102,8 @@ typedef struct {
   int32_t restart;                /* GMRES restart length                         */
   int32_t refine_steps;           /* FP64 residual corrections (FP32_REFINE)      */
   double inner_rtol;              /* inner FP32 tolerance (FP32_REFINE)           */
+  int32_t warm_start;             /* 1: start from this plan's previous converged state (dT0 still
+                                     fixes the conserved temperature level); 0: start from dT0 */
 } obte_solve_opts;
 
 typedef struct {
@@ -136,6 +138,12 @@ int64_t obte_launch_count(void);
 obte_status obte_bte_plan_create(obte_context ctx, const obte_problem* prob,
                                  const obte_material* mat, obte_plan* out);
 obte_status obte_bte_plan_destroy(obte_plan plan);
+/*
+ * Issue this plan's later work on `stream` (a cudaStream_t; work already issued is finished
+ * first).  No counterpart in the reference: it lets a serving loop run plans concurrently on
+ * separate streams.  One plan must not be used by two threads at the same time.
+ */
+obte_status obte_bte_plan_set_stream(obte_plan plan, void* stream);
 /* Device bytes held by the plan (tables) and by one solve's scratch. */
 obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision, int32_t restart,
                                     int64_t* plan_bytes, int64_t* solve_bytes);

@@ -50,7 +50,8 @@ class MaterialC(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_sweeps", C.c_int32),
-                ("restart", C.c_int32), ("refine_steps", C.c_int32), ("inner_rtol", C.c_double)]
+                ("restart", C.c_int32), ("refine_steps", C.c_int32), ("inner_rtol", C.c_double),
+                ("warm_start", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -91,6 +92,7 @@ SIGNATURES = [
     ("obte_launch_count", C.c_int64, []),
     ("obte_bte_plan_create", C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(MaterialC), C.POINTER(C.c_void_p)]),
     ("obte_bte_plan_destroy", C.c_int, [C.c_void_p]),
+    ("obte_bte_plan_set_stream", C.c_int, [C.c_void_p, C.c_void_p]),
     ("obte_bte_plan_footprint", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, p_i64, p_i64]),
     ("obte_bte_solve", C.c_int, [C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.POINTER(SolveInfo)]),

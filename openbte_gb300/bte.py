@@ -28,26 +28,34 @@ def _tensor_ptr(t):
 
 
 def solve_plan(plan, dT0, precision="fp64", rtol=1e-10, max_sweeps=1000, restart=30, refine_steps=3,
-               inner_rtol=1e-5, want_outputs=True):
-    """Solve on a prepared plan. dT0: torch CUDA float64 tensor [n]. Returns (info, dT, J, K, S) tensors."""
+               inner_rtol=1e-5, warm_start=False):
+    """Solve on a prepared plan. dT0: torch CUDA float64 tensor [n]. Returns (info, dT, J, K, S) tensors.
+
+    Allocations and the solve run on the plan's stream; the plan lock keeps one solve per plan at a time.
+    """
+    import contextlib
     import torch
     dev = dT0.device
     n = plan.n
     hp = plan.hp
-    dT = torch.empty(n, dtype=torch.float64, device=dev)
-    J = torch.empty((n, hp.sigma.shape[2]), dtype=torch.float64, device=dev)
-    K = torch.empty((hp.n_mfp, hp.n_dir), dtype=torch.float64, device=dev)
-    S = torch.empty((hp.n_mfp, hp.n_dir), dtype=torch.float64, device=dev)
-    o = _lib.SolveOpts()
-    o.precision = _lib.PRECISION[precision]
-    o.rtol = float(rtol)
-    o.max_sweeps = int(max_sweeps)
-    o.restart = int(restart)
-    o.refine_steps = int(refine_steps)
-    o.inner_rtol = float(inner_rtol)
-    info = _lib.SolveInfo()
-    st = plan.lib.obte_bte_solve(plan.handle, C.byref(o), _tensor_ptr(dT0), _tensor_ptr(dT), _tensor_ptr(J),
-                                 _tensor_ptr(K), _tensor_ptr(S), C.byref(info))
+    on_stream = (torch.cuda.stream(torch.cuda.ExternalStream(plan.stream, device=dev)) if plan.stream
+                 else contextlib.nullcontext())
+    with plan.lock, on_stream:
+        dT = torch.empty(n, dtype=torch.float64, device=dev)
+        J = torch.empty((n, hp.sigma.shape[2]), dtype=torch.float64, device=dev)
+        K = torch.empty((hp.n_mfp, hp.n_dir), dtype=torch.float64, device=dev)
+        S = torch.empty((hp.n_mfp, hp.n_dir), dtype=torch.float64, device=dev)
+        o = _lib.SolveOpts()
+        o.precision = _lib.PRECISION[precision]
+        o.rtol = float(rtol)
+        o.max_sweeps = int(max_sweeps)
+        o.restart = int(restart)
+        o.refine_steps = int(refine_steps)
+        o.inner_rtol = float(inner_rtol)
+        o.warm_start = 1 if warm_start else 0
+        info = _lib.SolveInfo()
+        st = plan.lib.obte_bte_solve(plan.handle, C.byref(o), _tensor_ptr(dT0), _tensor_ptr(dT), _tensor_ptr(J),
+                                     _tensor_ptr(K), _tensor_ptr(S), C.byref(info))
     if st not in (_lib.OBTE_OK, _lib.OBTE_ERR_NOT_CONVERGED):
         _lib.check(st, "obte_bte_solve")
     return info, dT, J, K, S

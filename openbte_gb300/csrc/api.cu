@@ -121,6 +121,7 @@ extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem
   if (!ctx) { *out = p; return OBTE_OK; }   // host-only plan: schedule queries, no device tables
   auto fail = [&](obte_status code) { delete p; return code; };
   cudaStream_t strm = ctx->stream;
+  p->stream = strm;
   if ((st = upload(p->ell, ell, strm)) != OBTE_OK) return fail(st);
   if ((st = upload(p->x_cell, s.x_cell, strm)) != OBTE_OK) return fail(st);
   if ((st = upload(p->diffuse_cell, s.diffuse_cell, strm)) != OBTE_OK) return fail(st);
@@ -133,7 +134,16 @@ extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem
 }
 
 extern "C" obte_status obte_bte_plan_destroy(obte_plan plan) {
+  if (plan && plan->stream) cudaStreamSynchronize(plan->stream);
   delete plan;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_plan_set_stream(obte_plan plan, void* stream) {
+  if (!plan || !plan->ctx) { set_error("null or host-only plan"); return OBTE_ERR_BAD_ARG; }
+  // finish work issued on the previous stream before switching
+  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  plan->stream = static_cast<cudaStream_t>(stream);
   return OBTE_OK;
 }
 

@@ -144,6 +144,7 @@ struct SolveWork {
 
 struct obte_plan_s {
   obte_context ctx = nullptr;
+  cudaStream_t stream = nullptr;    // stream of every call on this plan (set at creation, changeable)
   std::unique_ptr<obte::SolveWork> work;
   obte::Schedule sched;
   obte::DevSchedule d64, d32;       // FP64 and FP32 tables (built lazily)
@@ -154,6 +155,7 @@ struct obte_plan_s {
   obte::DevBuf err;                 // device error word (bounded waits that gave up)
   int64_t nx = 0;                   // periodic-inflow unknowns (source cells x n_mfp)
   int64_t nu = 0;                   // state length
+  bool has_solution = false;        // work->u holds the last converged state
 };
 
 namespace obte {

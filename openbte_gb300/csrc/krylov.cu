@@ -146,7 +146,7 @@ struct Solver {
   int max_sweeps;
   cudaStream_t st;
 
-  Solver(obte_plan p, Work& w, int ms) : plan(p), wk(w), max_sweeps(ms), st(p->ctx->stream) {}
+  Solver(obte_plan p, Work& w, int ms) : plan(p), wk(w), max_sweeps(ms), st(p->stream) {}
 
   obte_status sweep(bool fp32, const double* in, double* out, bool src, bool fin = false) {
     ++sweeps;
@@ -334,7 +334,7 @@ extern "C" obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const d
   // scratch for the final-pass outputs is not needed for a plain sweep
   OBTE_TRY(launch_sweep(plan, precision != OBTE_FP64, u_in, u_out, with_source != 0, false, nullptr, nullptr,
                         nullptr));
-  OBTE_CUDA(cudaStreamSynchronize(plan->ctx->stream));
+  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
   return check_device_error(plan);
 }
 
@@ -350,23 +350,29 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   const int restart = opts->restart > 0 ? std::min(opts->restart, 200) : 30;
   const int max_sweeps = opts->max_sweeps > 0 ? opts->max_sweeps : 1000;
   const double rtol = opts->rtol > 0 ? opts->rtol : 1e-10;
-  cudaStream_t st = plan->ctx->stream;
+  cudaStream_t st = plan->stream;
   if (!plan->work || plan->work->restart != restart || plan->work->nu != plan->nu) {
     plan->work.reset(new Work());
+    plan->has_solution = false;
     obte_status ast = alloc_work(plan, *plan->work, restart);
     if (ast != OBTE_OK) { plan->work.reset(); return ast; }
   }
   Work& wk = *plan->work;
+  const bool warm = opts->warm_start && plan->has_solution;
+  plan->has_solution = false;
   Solver sv(plan, wk, max_sweeps);
   double* u = wk.u.as<double>();
   const int64_t nsrc = s.x_base[s.n_dir];
+  // the state implied by dT0 fixes the conserved temperature level; a warm start keeps the
+  // previous converged state as the iterate
+  double* u0 = warm ? wk.tmp.as<double>() : u;
   init_state_kernel<<<wk.nb, VT, 0, st>>>(dT0, s.n, plan->diffuse_cell.as<int32_t>(), s.nd,
-                                          plan->x_cell.as<int32_t>(), nsrc, s.n_mfp, u);
+                                          plan->x_cell.as<int32_t>(), nsrc, s.n_mfp, u0);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
   // conserved ell.u of the initial state (DeltaT and T_B parts)
   std::vector<double> h;
-  OBTE_TRY(sv.multidot(u, 1, plan->ell.as<double>(), h));
+  OBTE_TRY(sv.multidot(u0, 1, plan->ell.as<double>(), h));
   const double ell0 = h[0];
 
   double unorm;
@@ -426,6 +432,7 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   }
   OBTE_CUDA(cudaStreamSynchronize(st));
   OBTE_TRY(check_device_error(plan));
+  plan->has_solution = true;
   if (info) {
     info->kappa_eff = kappa;
     info->n_sweeps = sv.sweeps;

@@ -11,11 +11,16 @@
 //     longest path from the sources and ordered by (level, element id);
 //   * each element that feeds a later element gets a slot in a ring of
 //     shared-memory rows that is recycled once its last consumer's level is done.
+// Directions are independent: they are built by a pool of host threads into
+// per-direction buffers and merged in direction order, so the result does not
+// depend on the thread count.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <cstdlib>
+#include <thread>
 #include <unordered_map>
 
 #include "internal.h"
@@ -178,7 +183,12 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     s.ell_B[w] = acc;
   }
 
-  // ---- per-direction schedule ----
+
+  // mixed sides are validated up front (the per-direction workers do not report errors for them)
+  for (int64_t k = 0; k < pb->n_mixed; ++k)
+    if (!in_range(pb->mixed_sides[k], ns)) { set_error("mixed side out of range"); return OBTE_ERR_BAD_ARG; }
+
+  // ---- per-direction schedule: directions in parallel, merged in direction order ----
   s.cell.assign((size_t)n_dir * n, 0);
   s.slot.assign((size_t)n_dir * n, -1);
   s.xk.assign((size_t)n_dir * n, -1);
@@ -188,31 +198,23 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.in_coef.assign((size_t)n_dir * n * nf, 0.0);
   s.D.assign((size_t)n_dir * n, 0.0);
   s.P.assign((size_t)n_dir * n, 0.0);
-  s.lev_ptr.clear();
-  s.lev_off.assign(n_dir, 0);
   s.nlev.assign(n_dir, 0);
   s.nslots.assign(n_dir, 0);
-  s.x_base.assign(n_dir + 1, 0);
-  s.x_cell.clear();
-  s.wo_wall.clear();
-  s.wo_gg.clear();
-  s.wo_off.assign(n_dir + 1, 0);
-  s.max_wo = 0;
-  s.kcoef.clear();
-  s.scoef.clear();
-  s.max_slots = 0;
-  s.max_src = 0;
 
-  std::vector<double> D(n), P(n);
-  std::vector<double> g(nfd);
-  std::vector<int32_t> indeg(n), level(n), order(n), pos_of(n), last_use(n), slot_of(n);
-  std::vector<int64_t> out_ptr(n + 1), in_ptr(n + 1);
-  std::vector<int32_t> out_adj, in_face;
-  std::vector<std::vector<int32_t>> wall_in(n);       // inflow walls per element
-  std::vector<int32_t> wall_any;                      // walls with any re-emission, per element lists
-  std::vector<std::vector<int32_t>> wall_out(n);
+  struct DirOut {
+    std::vector<int32_t> lev, x_cell, wo_wall;
+    std::vector<double> wo_gg, kcoef, scoef;
+    int nslots = 0;
+    obte_status st = OBTE_OK;
+    std::string err;
+  };
+  std::vector<DirOut> outs(n_dir);
 
-  for (int q = 0; q < n_dir; ++q) {
+  auto build_dir = [&](int q, DirOut& o, std::vector<double>& D, std::vector<double>& P, std::vector<double>& g,
+                       std::vector<int32_t>& indeg, std::vector<int32_t>& level, std::vector<int32_t>& order,
+                       std::vector<int32_t>& last_use, std::vector<int32_t>& slot_of, std::vector<int64_t>& out_ptr,
+                       std::vector<int64_t>& in_ptr, std::vector<int32_t>& out_adj, std::vector<int32_t>& in_face,
+                       std::vector<std::vector<int32_t>>& wall_in, std::vector<std::vector<int32_t>>& wall_out) {
     const double* sq = mt->vmfp + (int64_t)q * dd;
     std::fill(D.begin(), D.end(), 0.0);
     std::fill(P.begin(), P.end(), 0.0);
@@ -232,7 +234,6 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     // mixed walls (bte.py:90-96)
     for (int64_t k = 0; k < pb->n_mixed; ++k) {
       const int64_t sd = pb->mixed_sides[k];
-      if (!in_range(sd, ns)) { set_error("mixed side out of range"); return OBTE_ERR_BAD_ARG; }
       const int64_t i = sem[2 * sd];
       double v = 0;
       for (int d = 0; d < dim; ++d) v += sq[d] * na[sd * dim + d] / vol[i];
@@ -252,9 +253,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       P[i] += -std::min(v1, 0.0) * jump;
       P[j] += std::min(v2, 0.0) * jump;
     }
-    if (pb->is_nanowire) {
+    if (pb->is_nanowire)
       for (int64_t e = 0; e < n; ++e) P[e] += -sq[2];
-    }
 
     // DAG of uncut inflow edges nb -> row
     std::fill(indeg.begin(), indeg.end(), 0);
@@ -289,33 +289,26 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       }
     }
     if ((int64_t)queue.size() != n) {
-      set_error("upwind graph of direction " + std::to_string(q) + " has a cycle not broken by periodic cuts");
-      return OBTE_ERR_CYCLE;
+      o.st = OBTE_ERR_CYCLE;
+      o.err = "upwind graph of direction " + std::to_string(q) + " has a cycle not broken by periodic cuts";
+      return;
     }
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return level[a] < level[b]; });
     int32_t nl = 0;
     for (int64_t e = 0; e < n; ++e) nl = std::max(nl, level[e] + 1);
-    s.lev_off[q] = (int64_t)s.lev_ptr.size();
-    s.nlev[q] = nl;
-    {
-      std::vector<int32_t> cnt(nl + 1, 0);
-      for (int64_t e = 0; e < n; ++e) cnt[level[e] + 1]++;
-      for (int L = 0; L < nl; ++L) cnt[L + 1] += cnt[L];
-      s.lev_ptr.insert(s.lev_ptr.end(), cnt.begin(), cnt.end());
-    }
-    for (int64_t p = 0; p < n; ++p) pos_of[order[p]] = (int32_t)p;
+    o.lev.assign(nl + 1, 0);
+    for (int64_t e = 0; e < n; ++e) o.lev[level[e] + 1]++;
+    for (int L = 0; L < nl; ++L) o.lev[L + 1] += o.lev[L];
 
     // periodic source cells of direction q (sorted unique upstream elements of cut inflow)
-    std::vector<int32_t> src;
+    std::vector<int32_t>& src = o.x_cell;
     for (int64_t f = 0; f < nfd; ++f)
       if (g[f] < 0 && f_cut[f]) src.push_back(f_nb[f]);
     std::sort(src.begin(), src.end());
     src.erase(std::unique(src.begin(), src.end()), src.end());
-    s.x_base[q + 1] = s.x_base[q] + (int64_t)src.size();
-    s.max_src = std::max(s.max_src, (int)src.size());
     std::unordered_map<int32_t, int32_t> src_idx;
-    for (size_t k = 0; k < src.size(); ++k) { src_idx[src[k]] = (int32_t)k; s.x_cell.push_back(src[k]); }
+    for (size_t k = 0; k < src.size(); ++k) src_idx[src[k]] = (int32_t)k;
 
     // inflow walls / wall outputs per element
     for (int64_t e = 0; e < n; ++e) { wall_in[e].clear(); wall_out[e].clear(); }
@@ -335,7 +328,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       int32_t lu = -1;
       for (int64_t k = out_ptr[e]; k < out_ptr[e + 1]; ++k) lu = std::max(lu, level[out_adj[k]]);
       const bool special = src_idx.count((int32_t)e) || !wall_out[e].empty() || ck == OBTE_CONTACT_NANOWIRE ||
-                           contact_of.count((int32_t)e);
+                           contact_of.find((int32_t)e) != contact_of.end();
       if (special) lu = std::max(lu, level[e]);
       last_use[e] = lu;
       slot_of[e] = -1;
@@ -357,12 +350,10 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
           release[last_use[e] + 1].push_back(sl);
         }
       }
-      s.nslots[q] = next;
-      s.max_slots = std::max(s.max_slots, (int)next);
+      o.nslots = next;
     }
 
-    s.wo_off[q] = (int32_t)s.wo_wall.size();
-    // items in level order
+    // items in level order (wout and contact indices local to the direction; rebased on merge)
     const size_t base = (size_t)q * n;
     for (int64_t p = 0; p < n; ++p) {
       const int32_t e = order[p];
@@ -374,14 +365,14 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       int k = 0;
       for (int64_t t = in_ptr[e]; t < in_ptr[e + 1]; ++t) {
         const int32_t f = in_face[t];
-        if (k >= nf) { set_error("more inflow faces than element sides"); return OBTE_ERR_BAD_ARG; }
+        if (k >= nf) { o.st = OBTE_ERR_BAD_ARG; o.err = "more inflow faces than element sides"; return; }
         if (f_cut[f]) s.in_idx[it * nf + k] = pack_item(ITEM_PERIODIC, src_idx[f_nb[f]]);
         else s.in_idx[it * nf + k] = pack_item(ITEM_CELL, slot_of[f_nb[f]]);
         s.in_coef[it * nf + k] = g[f];
         ++k;
       }
       for (int32_t w : wall_in[e]) {
-        if (k >= nf) { set_error("more inflow faces than element sides"); return OBTE_ERR_BAD_ARG; }
+        if (k >= nf) { o.st = OBTE_ERR_BAD_ARG; o.err = "more inflow faces than element sides"; return; }
         double v = 0;
         for (int d = 0; d < dim; ++d) v += sq[d] * w_db[(int64_t)w * dim + d];
         s.in_idx[it * nf + k] = pack_item(ITEM_WALL, w);
@@ -391,21 +382,22 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       auto si = src_idx.find(e);
       if (si != src_idx.end()) s.xk[it] = si->second;
       if (!wall_out[e].empty()) {
-        const int32_t begin = (int32_t)s.wo_wall.size();
-        if (wall_out[e].size() > 7) { set_error("too many wall sides on one element"); return OBTE_ERR_BAD_ARG; }
+        const int32_t begin = (int32_t)o.wo_wall.size();
+        if (wall_out[e].size() > 7) { o.st = OBTE_ERR_BAD_ARG; o.err = "too many wall sides on one element"; return; }
         for (int32_t w : wall_out[e]) {
-          s.wo_wall.push_back(w);
+          o.wo_wall.push_back(w);
           for (int m = 0; m < m_pad; ++m) {
             double v = 0;
             if (m < n_mfp && gbm_sum[w] != 0) v = std::max(gb_of(m, q, w), 0.0) / (-gbm_sum[w]);
-            s.wo_gg.push_back(v);
+            o.wo_gg.push_back(v);
           }
         }
         s.wout[it] = (begin << 3) | (int32_t)wall_out[e].size();
       }
       // contact coefficients
-      if (ck == OBTE_CONTACT_NANOWIRE || contact_of.count(e)) {
-        const int32_t ce = (int32_t)s.scoef.size();
+      auto co = contact_of.find(e);
+      if (ck == OBTE_CONTACT_NANOWIRE || co != contact_of.end()) {
+        const int32_t ce = (int32_t)o.scoef.size();
         double sc = 0;
         for (int m = 0; m < m_pad; ++m) {
           double kc = 0;
@@ -413,27 +405,25 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
             if (ck == OBTE_CONTACT_NANOWIRE) {
               kc = mt->sigma[((int64_t)m * n_dir + q) * ds + 2] * vol[e];
             } else {
-              for (auto& pr : contact_of[e]) {
+              for (auto& pr : co->second) {
                 const double sn = sigma_n(m, q, pr.first);
                 kc += pr.second == 1 ? std::max(sn, 0.0) : std::min(sn, 0.0);
               }
             }
           }
-          s.kcoef.push_back(kc * nrm);
+          o.kcoef.push_back(kc * nrm);
         }
         if (ck != OBTE_CONTACT_NANOWIRE)
-          for (auto& pr : contact_of[e])
+          for (auto& pr : co->second)
             if (pr.second == 1) sc += c_area[pr.first];
-        s.scoef.push_back(sc * nrm);
+        o.scoef.push_back(sc * nrm);
         s.contact[it] = ce;
         for (int m = 0; m < n_mfp; ++m) {
-          s.kshift[(size_t)m * n_dir + q] += s.kcoef[(size_t)ce * m_pad + m];
+          s.kshift[(size_t)m * n_dir + q] += o.kcoef[(size_t)ce * m_pad + m];
           s.sshift[(size_t)m * n_dir + q] += sc * nrm;
         }
       }
     }
-    s.wo_off[q + 1] = (int32_t)s.wo_wall.size();
-    s.max_wo = std::max(s.max_wo, s.wo_off[q + 1] - s.wo_off[q]);
     // alpha term of K (bte.py:243)
     if (ck == OBTE_CONTACT_PERIODIC || ck == OBTE_CONTACT_MIXED)
       for (int m = 0; m < n_mfp; ++m) {
@@ -441,6 +431,66 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         for (int64_t k = 0; k < nc; ++k) acc += std::min(sigma_n(m, q, k), 0.0);
         s.kconst[(size_t)m * n_dir + q] = pb->contact_alpha * acc * nrm;
       }
+  };
+
+  int nthreads = (int)std::thread::hardware_concurrency();
+  if (const char* env = std::getenv("OBTE_HOST_THREADS")) nthreads = std::atoi(env);
+  nthreads = std::max(1, std::min({nthreads, n_dir, 32}));
+  auto worker = [&](int tid) {
+    std::vector<double> D(n), P(n), g(nfd);
+    std::vector<int32_t> indeg(n), level(n), order(n), last_use(n), slot_of(n), out_adj, in_face;
+    std::vector<int64_t> out_ptr(n + 1), in_ptr(n + 1);
+    std::vector<std::vector<int32_t>> wall_in(n), wall_out(n);
+    for (int q = tid; q < n_dir; q += nthreads)
+      build_dir(q, outs[q], D, P, g, indeg, level, order, last_use, slot_of, out_ptr, in_ptr, out_adj, in_face,
+                wall_in, wall_out);
+  };
+  if (nthreads == 1) {
+    worker(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker, t);
+    for (auto& th : pool) th.join();
+  }
+
+  // merge in direction order
+  s.lev_ptr.clear();
+  s.lev_off.assign(n_dir, 0);
+  s.x_base.assign(n_dir + 1, 0);
+  s.x_cell.clear();
+  s.wo_wall.clear();
+  s.wo_gg.clear();
+  s.wo_off.assign(n_dir + 1, 0);
+  s.kcoef.clear();
+  s.scoef.clear();
+  s.max_slots = s.max_src = s.max_wo = 0;
+  for (int q = 0; q < n_dir; ++q) {
+    DirOut& o = outs[q];
+    if (o.st != OBTE_OK) { set_error(o.err); return o.st; }
+    s.lev_off[q] = (int64_t)s.lev_ptr.size();
+    s.lev_ptr.insert(s.lev_ptr.end(), o.lev.begin(), o.lev.end());
+    s.nlev[q] = (int32_t)o.lev.size() - 1;
+    s.nslots[q] = o.nslots;
+    s.max_slots = std::max(s.max_slots, o.nslots);
+    s.x_base[q + 1] = s.x_base[q] + (int64_t)o.x_cell.size();
+    s.x_cell.insert(s.x_cell.end(), o.x_cell.begin(), o.x_cell.end());
+    s.max_src = std::max(s.max_src, (int)o.x_cell.size());
+    const int32_t wo0 = (int32_t)s.wo_wall.size();
+    const int32_t ce0 = (int32_t)s.scoef.size();
+    s.wo_off[q] = wo0;
+    const size_t base = (size_t)q * n;
+    for (int64_t p = 0; p < n; ++p) {
+      const size_t it = base + p;
+      if (s.wout[it]) s.wout[it] = (((s.wout[it] >> 3) + wo0) << 3) | (s.wout[it] & 7);
+      if (s.contact[it] >= 0) s.contact[it] += ce0;
+    }
+    s.wo_wall.insert(s.wo_wall.end(), o.wo_wall.begin(), o.wo_wall.end());
+    s.wo_gg.insert(s.wo_gg.end(), o.wo_gg.begin(), o.wo_gg.end());
+    s.kcoef.insert(s.kcoef.end(), o.kcoef.begin(), o.kcoef.end());
+    s.scoef.insert(s.scoef.end(), o.scoef.begin(), o.scoef.end());
+    s.wo_off[q + 1] = (int32_t)s.wo_wall.size();
+    s.max_wo = std::max(s.max_wo, s.wo_off[q + 1] - wo0);
+    std::vector<int32_t>().swap(o.lev);
   }
   return OBTE_OK;
 }

@@ -546,7 +546,7 @@ static int choose_mcp(const Schedule& s, int rows, int num_sms, size_t optin) {
 template <typename Real>
 static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   const Schedule& s = plan->sched;
-  cudaStream_t st = plan->ctx->stream;
+  cudaStream_t st = plan->stream;
   const int rows = s.max_slots + 2 + s.max_src;
   const int mcp = choose_mcp<Real>(s, rows, plan->ctx->num_sms, plan->ctx->smem_optin);
   if (!mcp) {
@@ -607,7 +607,7 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
 obte_status ensure_tables(obte_plan plan, bool fp32) {
   if (!plan->err.p) {
     OBTE_TRY(plan->err.alloc(sizeof(int)));
-    OBTE_CUDA(cudaMemsetAsync(plan->err.p, 0, sizeof(int), plan->ctx->stream));
+    OBTE_CUDA(cudaMemsetAsync(plan->err.p, 0, sizeof(int), plan->stream));
   }
   if (fp32) {
     if (!plan->d32.ready) return upload_tables<float>(plan, plan->d32);
@@ -623,7 +623,7 @@ template <typename Real, int NF, int MCP, bool FINAL>
 static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                bool with_src, double* Jraw, double* K, double* S) {
   const Schedule& s = plan->sched;
-  cudaStream_t st = plan->ctx->stream;
+  cudaStream_t st = plan->stream;
   const int64_t total = (int64_t)s.n_dir * s.n;
   const int vblocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)plan->ctx->num_sms * 8);
   sweep_values_kernel<Real><<<vblocks, 256, 0, st>>>(
@@ -669,7 +669,7 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
                          bool final_pass, double* Jraw, double* K, double* S) {
   OBTE_TRY(ensure_tables(plan, fp32));
   const Schedule& s = plan->sched;
-  cudaStream_t st = plan->ctx->stream;
+  cudaStream_t st = plan->stream;
   if (s.ds > 3) { set_error("sigma with more than 3 components"); return OBTE_ERR_UNSUPPORTED; }
   if (s.nf > 4) { set_error("elements with more than 4 sides are not supported"); return OBTE_ERR_UNSUPPORTED; }
   OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
@@ -691,10 +691,10 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
 obte_status check_device_error(obte_plan plan) {
   if (!plan->err.p) return OBTE_OK;
   int h = 0;
-  OBTE_CUDA(cudaMemcpyAsync(&h, plan->err.p, sizeof(int), cudaMemcpyDeviceToHost, plan->ctx->stream));
-  OBTE_CUDA(cudaStreamSynchronize(plan->ctx->stream));
+  OBTE_CUDA(cudaMemcpyAsync(&h, plan->err.p, sizeof(int), cudaMemcpyDeviceToHost, plan->stream));
+  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
   if (h) {
-    OBTE_CUDA(cudaMemsetAsync(plan->err.p, 0, sizeof(int), plan->ctx->stream));
+    OBTE_CUDA(cudaMemsetAsync(plan->err.p, 0, sizeof(int), plan->stream));
     set_error("a device-side wait timed out in the sweep kernel");
     return OBTE_ERR_DEVICE_TIMEOUT;
   }

@@ -23,19 +23,23 @@ def _torch():
     return torch
 
 
-def context(device: int = 0):
-    """Library context for `device`, bound to torch's current stream there."""
+def context(device: int = 0, stream=None):
+    """Library context for `device` bound to a CUDA stream handle (default: torch's current stream).
+
+    Contexts are cached per (device, stream) so threads that use their own streams get their own
+    contexts.
+    """
     torch = _torch()
     lib = _lib.load()
-    stream = torch.cuda.current_stream(device).cuda_stream
-    ctx = _CTX.get(device)
+    if stream is None:
+        stream = torch.cuda.current_stream(device).cuda_stream
+    key = (device, int(stream or 0))
+    ctx = _CTX.get(key)
     if ctx is None:
         h = C.c_void_p()
         _lib.check(lib.obte_context_create(device, C.c_void_p(stream), C.byref(h)), "obte_context_create")
         ctx = h
-        _CTX[device] = ctx
-    else:
-        _lib.check(lib.obte_context_set_stream(ctx, C.c_void_p(stream)), "obte_context_set_stream")
+        _CTX[key] = ctx
     return ctx
 
 
@@ -187,10 +191,14 @@ class HostProblem:
 class Plan:
     """A device-resident sweep plan (orders, level sets, operator tables)."""
 
-    def __init__(self, hp: HostProblem, device: int = 0, host_only: bool = False):
+    def __init__(self, hp: HostProblem, device: int = 0, host_only: bool = False, stream=None):
+        import threading
         self.lib = _lib.load()
         self.device = device
-        self.ctx = None if host_only else context(device)
+        self.lock = threading.Lock()      # one solve at a time per plan (its scratch is shared)
+        self.ctx = None if host_only else context(device, stream)
+        self.stream = None if host_only else (stream if stream is not None else
+                                              _torch().cuda.current_stream(device).cuda_stream)
         self.hp = hp
         p, m = hp.c_structs()
         h = C.c_void_p()
@@ -200,6 +208,12 @@ class Plan:
         _lib.check(self.lib.obte_bte_state_layout(h, C.byref(n), C.byref(nd), C.byref(nx)), "state_layout")
         self.n, self.nd, self.nx = n.value, nd.value, nx.value
         self.nu = self.n + self.nd + self.nx
+
+    def set_stream(self, stream):
+        """Issue this plan's later work on `stream` (a raw cudaStream_t handle)."""
+        if int(stream or 0) != int(self.stream or 0):
+            _lib.check(self.lib.obte_bte_plan_set_stream(self.handle, C.c_void_p(stream)), "set_stream")
+            self.stream = stream
 
     def footprint(self, precision="fp64", restart=30):
         pb, sb = C.c_int64(), C.c_int64()

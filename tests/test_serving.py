@@ -1,0 +1,89 @@
+"""Serving loop scheduling on CPU with a fake backend: admission by footprint, slot limits, rejection."""
+import threading
+import time
+
+from openbte_gb300.serving import Request, Server, replay, summarize
+
+
+class FakeBackend:
+    def __init__(self):
+        self.lock = threading.Lock()
+        self.running = 0
+        self.max_running = 0
+        self.used = 0
+        self.max_used = 0
+        self.order = []
+
+    def budget(self, fraction):
+        return 100
+
+    def build(self, req):
+        time.sleep(0.001)
+        return object(), req.tag["foot"], False
+
+    def solve(self, plan, req, slot):
+        with self.lock:
+            self.running += 1
+            self.used += req.tag["foot"]
+            self.max_running = max(self.max_running, self.running)
+            self.max_used = max(self.max_used, self.used)
+            self.order.append(req.rid)
+        time.sleep(req.tag["t"])
+        with self.lock:
+            self.running -= 1
+            self.used -= req.tag["foot"]
+        return {"kappa": req.tag["kappa"], "converged": True}
+
+    def release(self, plan):
+        pass
+
+
+def _req(rid, foot, t=0.02, kappa=1.0):
+    return Request(geo=None, mat=None, bcs=None, ek=None, rid=rid, tag={"foot": foot, "t": t, "kappa": kappa})
+
+
+def test_slots_and_budget_are_respected():
+    be = FakeBackend()
+    srv = Server(backend=be, slots=3, builders=2, hbm_budget=100)
+    reqs = [_req(i, 30, kappa=float(i)) for i in range(10)]
+    res = replay(srv, reqs)
+    srv.close()
+    assert all(r.status == "ok" for r in res)
+    assert [r.kappa for r in res] == [float(i) for i in range(10)]
+    assert be.max_running <= 3 and be.max_running >= 2
+    assert be.max_used <= 100
+
+
+def test_oversized_request_is_rejected_not_queued_forever():
+    be = FakeBackend()
+    srv = Server(backend=be, slots=2, builders=1, hbm_budget=100)
+    res = replay(srv, [_req(0, 50), _req(1, 500), _req(2, 50)])
+    srv.close()
+    st = {r.rid: r.status for r in res}
+    assert st == {0: "ok", 1: "rejected", 2: "ok"}
+    assert "exceeds the HBM budget" in [r for r in res if r.rid == 1][0].error
+
+
+def test_first_fit_lets_small_requests_pass_a_large_one():
+    be = FakeBackend()
+    srv = Server(backend=be, slots=4, builders=1, hbm_budget=100)
+    # 0 occupies 60; 1 needs 60 (waits); 2 needs 30 and fits next to 0
+    res = replay(srv, [_req(0, 60, t=0.2), _req(1, 60, t=0.01), _req(2, 30, t=0.01)])
+    srv.close()
+    assert all(r.status == "ok" for r in res)
+    assert be.order.index(2) < be.order.index(1)
+    s = summarize(res)
+    assert s["completed"] == 3 and s["p99_ms"] >= s["p50_ms"]
+
+
+def test_backend_errors_are_reported_per_request():
+    class Failing(FakeBackend):
+        def solve(self, plan, req, slot):
+            if req.rid == 1:
+                raise RuntimeError("boom")
+            return super().solve(plan, req, slot)
+    srv = Server(backend=Failing(), slots=2, builders=1, hbm_budget=100)
+    res = replay(srv, [_req(0, 10), _req(1, 10), _req(2, 10)])
+    srv.close()
+    st = {r.rid: r.status for r in res}
+    assert st == {0: "ok", 1: "error", 2: "ok"}
