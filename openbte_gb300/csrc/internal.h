@@ -138,7 +138,7 @@ struct SolveWork {
   int64_t nu = 0;
   int restart = 0;
   int nb = 1;
-  DevBuf u, Fu, r, V, w, tmp, partial, hdev, Jraw, Kraw, Sraw, delta;
+  DevBuf u, Fu, r, V, w, tmp, partial, hdev, sdev, Jraw, Kraw, Sraw, delta;
 };
 }  // namespace obte
 

@@ -38,21 +38,26 @@ int vec_blocks(const obte_plan plan, int64_t n) {
   return (int)std::max<int64_t>(1, std::min(want, cap));
 }
 
-// partial[b * k + j] = sum over block b's range of V[j*ld + i] * w[i]
-__global__ void __launch_bounds__(VT) multidot_kernel(const double* __restrict__ V, int64_t ld, int k,
+// partial[b * kk + j] = sum over block b's range of V[j*ld + i] * w[i] for j < k, and w.w for
+// j == k when self != 0 (kk = k + self)
+__global__ void __launch_bounds__(VT) multidot_kernel(const double* __restrict__ V, int64_t ld, int k, int self,
                                                       const double* __restrict__ w, int64_t n,
                                                       double* __restrict__ partial) {
   __shared__ double red[VT / 32][DOT_TILE];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int jt = 0; jt < k; jt += DOT_TILE) {
+  const int kk = k + self;
+  for (int jt = 0; jt < kk; jt += DOT_TILE) {
     double acc[DOT_TILE];
 #pragma unroll
     for (int t = 0; t < DOT_TILE; ++t) acc[t] = 0.0;
     for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
       const double wi = w[i];
 #pragma unroll
-      for (int t = 0; t < DOT_TILE; ++t)
-        if (jt + t < k) acc[t] += V[(int64_t)(jt + t) * ld + i] * wi;
+      for (int t = 0; t < DOT_TILE; ++t) {
+        const int j = jt + t;
+        if (j < k) acc[t] += V[(int64_t)j * ld + i] * wi;
+        else if (j < kk) acc[t] += wi * wi;
+      }
     }
 #pragma unroll
     for (int t = 0; t < DOT_TILE; ++t) {
@@ -61,31 +66,53 @@ __global__ void __launch_bounds__(VT) multidot_kernel(const double* __restrict__
       if (lane == 0) red[warp][t] = v;
     }
     __syncthreads();
-    if (threadIdx.x < DOT_TILE && jt + (int)threadIdx.x < k) {
+    if (threadIdx.x < DOT_TILE && jt + (int)threadIdx.x < kk) {
       double v = 0;
       for (int w2 = 0; w2 < VT / 32; ++w2) v += red[w2][threadIdx.x];
-      partial[(int64_t)blockIdx.x * k + jt + threadIdx.x] = v;
+      partial[(int64_t)blockIdx.x * kk + jt + threadIdx.x] = v;
     }
     __syncthreads();
   }
 }
 
-// out[j] = sum_b partial[b * k + j], fixed order (deterministic)
-__global__ void reduce_partials_kernel(const double* __restrict__ partial, int nb, int k, double* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= k) return;
+// out[j] = sum_b partial[b * k + j]: one block per output, fixed summation tree (deterministic)
+__global__ void __launch_bounds__(VT) reduce_partials_kernel(const double* __restrict__ partial, int nb, int k,
+                                                             double* __restrict__ out) {
+  __shared__ double red[VT / 32];
+  const int j = blockIdx.x;
   double v = 0;
-  for (int b = 0; b < nb; ++b) v += partial[(int64_t)b * k + j];
-  out[j] = v;
+  for (int b = threadIdx.x; b < nb; b += VT) v += partial[(int64_t)b * k + j];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < VT / 32; ++w) t += red[w];
+    out[j] = t;
+  }
 }
 
-// w -= sum_j h[j] V[j]
+// w -= sum_j h[j] V[j]; partial[b] = sum over block b of the new w^2
 __global__ void __launch_bounds__(VT) update_kernel(double* __restrict__ w, const double* __restrict__ V, int64_t ld,
-                                                    int k, const double* __restrict__ h, int64_t n) {
+                                                    int k, const double* __restrict__ h, int64_t n,
+                                                    double* __restrict__ partial) {
+  __shared__ double red[VT / 32];
+  double ss = 0;
   for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
     double acc = w[i];
     for (int j = 0; j < k; ++j) acc -= h[j] * V[(int64_t)j * ld + i];
     w[i] = acc;
+    ss += acc * acc;
+  }
+  if (partial) {
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w2 = 0; w2 < VT / 32; ++w2) t += red[w2];
+      partial[blockIdx.x] = t;
+    }
   }
 }
 
@@ -154,16 +181,30 @@ struct Solver {
     return launch_sweep(plan, fp32, in, out, src, fin, wk.Jraw.as<double>(), wk.Kraw.as<double>(),
                         wk.Sraw.as<double>());
   }
-  // h[0..k) = V[0..k)^T w, also copied to host
-  obte_status multidot(const double* V, int k, const double* w, std::vector<double>& h) {
+  // h[0..k) = V[0..k)^T w (and h[k] = w.w when self), copied to host
+  obte_status multidot(const double* V, int k, const double* w, std::vector<double>& h, bool self = false) {
     const int64_t n = wk.nu;
-    multidot_kernel<<<wk.nb, VT, 0, st>>>(V, n, k, w, n, wk.partial.as<double>());
-    reduce_partials_kernel<<<(k + 63) / 64, 64, 0, st>>>(wk.partial.as<double>(), wk.nb, k, wk.hdev.as<double>());
+    const int kk = k + (self ? 1 : 0);
+    multidot_kernel<<<wk.nb, VT, 0, st>>>(V, n, k, self ? 1 : 0, w, n, wk.partial.as<double>());
+    reduce_partials_kernel<<<kk, VT, 0, st>>>(wk.partial.as<double>(), wk.nb, kk, wk.hdev.as<double>());
     count_launch(2);
     OBTE_CUDA(cudaGetLastError());
-    h.resize(k);
-    OBTE_CUDA(cudaMemcpyAsync(h.data(), wk.hdev.p, k * sizeof(double), cudaMemcpyDeviceToHost, st));
+    h.resize(kk);
+    OBTE_CUDA(cudaMemcpyAsync(h.data(), wk.hdev.p, kk * sizeof(double), cudaMemcpyDeviceToHost, st));
     OBTE_CUDA(cudaStreamSynchronize(st));
+    return OBTE_OK;
+  }
+  // w -= V[0..k) h (h already on the device in wk.hdev); returns ‖w‖ after the update
+  obte_status update_norm(double* w, const double* V, int k, double& nrm) {
+    const int64_t n = wk.nu;
+    update_kernel<<<wk.nb, VT, 0, st>>>(w, V, n, k, wk.hdev.as<double>(), n, wk.partial.as<double>());
+    reduce_partials_kernel<<<1, VT, 0, st>>>(wk.partial.as<double>(), wk.nb, 1, wk.sdev.as<double>());
+    count_launch(2);
+    OBTE_CUDA(cudaGetLastError());
+    double ss;
+    OBTE_CUDA(cudaMemcpyAsync(&ss, wk.sdev.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    OBTE_CUDA(cudaStreamSynchronize(st));
+    nrm = std::sqrt(std::max(ss, 0.0));
     return OBTE_OK;
   }
   obte_status norm(const double* x, double& out) {
@@ -231,23 +272,17 @@ struct Solver {
         OBTE_TRY(lincomb(1.0, vj, -1.0, wk.tmp.as<double>(), w));
         // classical Gram-Schmidt; a second pass only when the first one cancelled most of w
         // (Daniel-Gragg-Kaufman-Stewart criterion, ‖w‖ after < 0.7 ‖w‖ before)
-        double wn0;
-        OBTE_TRY(norm(w, wn0));
-        OBTE_TRY(multidot(V, j + 1, w, h));
+        OBTE_TRY(multidot(V, j + 1, w, h, true));   // h[0..j] and w.w in one pass
+        const double wn0 = std::sqrt(std::max(h[j + 1], 0.0));
+        h.resize(j + 1);
         OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, h.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
-        update_kernel<<<wk.nb, VT, 0, st>>>(w, V, n, j + 1, wk.hdev.as<double>(), n);
-        count_launch();
-        OBTE_CUDA(cudaGetLastError());
         double hn;
-        OBTE_TRY(norm(w, hn));
+        OBTE_TRY(update_norm(w, V, j + 1, hn));
         if (hn < 0.7 * wn0) {
           OBTE_TRY(multidot(V, j + 1, w, h2));
           OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, h2.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
-          update_kernel<<<wk.nb, VT, 0, st>>>(w, V, n, j + 1, wk.hdev.as<double>(), n);
-          count_launch();
-          OBTE_CUDA(cudaGetLastError());
+          OBTE_TRY(update_norm(w, V, j + 1, hn));
           for (int i = 0; i <= j; ++i) h[i] += h2[i];
-          OBTE_TRY(norm(w, hn));
         }
         // Hessenberg column j
         for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = h[i];
@@ -279,7 +314,7 @@ struct Solver {
       for (double& v : y) v = -v;   // update_kernel subtracts
       if (j > 0) {
         OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, st));
-        update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n);
+        update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n, nullptr);
         count_launch();
         OBTE_CUDA(cudaGetLastError());
       }
@@ -309,7 +344,8 @@ static obte_status alloc_work(obte_plan plan, Work& wk, int restart) {
   OBTE_TRY(wk.delta.alloc(vb));
   OBTE_TRY(wk.V.alloc(vb * (restart + 1)));
   OBTE_TRY(wk.partial.alloc((size_t)wk.nb * (restart + 1) * sizeof(double)));
-  OBTE_TRY(wk.hdev.alloc((size_t)(restart + 1) * sizeof(double)));
+  OBTE_TRY(wk.hdev.alloc((size_t)(restart + 2) * sizeof(double)));
+  OBTE_TRY(wk.sdev.alloc(8 * sizeof(double)));
   OBTE_TRY(wk.Jraw.alloc((size_t)s.n * s.ds * sizeof(double)));
   OBTE_TRY(wk.Kraw.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
   OBTE_TRY(wk.Sraw.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
