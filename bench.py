@@ -31,9 +31,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # name: (n_triangles, n_mfp, n_dir, porosity, pore, seed)
+    # name: (n_elements, n_mfp, n_dir, porosity, pore, seed); 3D: n_dir = (n_theta, n_phi)
     "c1_60k_100x96": (60000, 100, 96, 0.25, "square", 1),
     "c0_2k_30x48": (2000, 30, 48, 0.25, "square", 1),
+    "c2_100k_30x16x32": (100000, 30, (16, 32), 0.10, "sphere", 1),
 }
 L2_BYTES = 129 * 1024 * 1024
 
@@ -44,6 +45,15 @@ def problem(workload):
     from openbte_gb300.mesh import mesh_from_cell
     from openbte_gb300.material import synthetic_isotropic_2d
     n_tri, n_mfp, n_dir, phi, pore, seed = WORKLOADS[workload]
+    if pore == "sphere":
+        from openbte_gb300.geometry import porous_cube_3d
+        from openbte_gb300.material import synthetic_isotropic_3d
+        cell = porous_cube_3d(n_tri, phi, seed=seed)
+        geo = mesh_from_cell(cell)
+        mat = synthetic_isotropic_3d(n_mfp, n_dir[0], n_dir[1])
+        bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0, "Periodic_z": 0}, diffuse="Boundary")
+        ek = O.EffectiveThermalConductivity(normalization=-1.0 / cell.size, contact="Periodic_x")
+        return geo, mat, bcs, ek
     geo = mesh_from_cell(porous_cell_2d(n_tri, phi, pore, seed=seed))
     mat = synthetic_isotropic_2d(n_mfp, n_dir)
     bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")

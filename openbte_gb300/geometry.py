@@ -209,35 +209,160 @@ def porous_cell_2d(n_target: int = 2000, porosity: float = 0.25, pore: str = "sq
                           meta={"h": h, "n_outer": n_outer, "n_ring": n_ring})
 
 
+REGIONS_3D = ["Boundary", "Periodic_x_a", "Periodic_x_b", "Periodic_y_a", "Periodic_y_b",
+              "Periodic_z_a", "Periodic_z_b"]
+
+
+def porous_cube_3d(n_target: int = 100000, porosity: float = 0.10, size: float = 100.0, seed: int = 0,
+                   jitter: float = 0.2) -> PeriodicCell2D:
+    """Seeded periodic cube of side `size` (nm) with a centred spherical pore, tetrahedral Delaunay mesh.
+
+    ``n_target`` is the approximate tetrahedron count. Opposite cube faces carry the same jittered 2D
+    point set and cube edges a shared uniform grid, so the face triangulations are translates of each
+    other (checked); the pore surface is a Fibonacci point set on the sphere. Tetrahedra inside the
+    pore and flat (zero-volume) tetrahedra on the faces are removed. Returned in the same container as
+    the 2D cells (``elems`` [n, 4], ``segments`` = boundary triangles per region, ``periodic`` =
+    (slave, master) node pairs per axis).
+    """
+    rng = np.random.default_rng(seed)
+    half = size / 2.0
+    r = (3.0 * porosity * size ** 3 / (4.0 * math.pi)) ** (1.0 / 3.0)
+    vol = size ** 3 * (1.0 - porosity)
+    h = (vol * 6.3 / n_target) ** (1.0 / 3.0)          # about 6.3 tetrahedra per point
+    nb = max(4, int(round(size / h)))
+    g1 = np.linspace(-half, half, nb + 1)
+    # cube edges: uniform grids shared by the faces that meet there
+    pts = []
+    for ax in range(3):
+        for s1 in (-half, half):
+            for s2 in (-half, half):
+                e = np.zeros((nb + 1, 3))
+                e[:, ax] = g1
+                o = [a for a in range(3) if a != ax]
+                e[:, o[0]] = s1
+                e[:, o[1]] = s2
+                pts.append(e)
+    # face interiors: one jittered 2D set per axis, used on both faces of that axis
+    for ax in range(3):
+        o = [a for a in range(3) if a != ax]
+        u, v = np.meshgrid(g1[1:-1], g1[1:-1], indexing="ij")
+        uv = np.stack([u.ravel(), v.ravel()], axis=1)
+        uv = uv + rng.uniform(-jitter * h, jitter * h, size=uv.shape)
+        uv = np.clip(uv, -half + 0.3 * h, half - 0.3 * h)
+        for s in (-half, half):
+            f = np.zeros((len(uv), 3))
+            f[:, ax] = s
+            f[:, o[0]] = uv[:, 0]
+            f[:, o[1]] = uv[:, 1]
+            pts.append(f)
+    # pore surface (Fibonacci sphere)
+    ns = max(20, int(round(4.0 * math.pi * r * r / (0.8 * h * h))))
+    k = np.arange(ns) + 0.5
+    th = np.arccos(1.0 - 2.0 * k / ns)
+    ph = math.pi * (1.0 + 5.0 ** 0.5) * k
+    sph = r * np.stack([np.cos(ph) * np.sin(th), np.sin(ph) * np.sin(th), np.cos(th)], axis=1)
+    pts.append(sph)
+    # interior: jittered cubic lattice away from faces and pore
+    gi = np.arange(-half + 0.5 * h, half, h)
+    X, Y, Z = np.meshgrid(gi, gi, gi, indexing="ij")
+    lat = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    lat = lat + rng.uniform(-jitter * h, jitter * h, size=lat.shape)
+    keep = np.all(np.abs(lat) < half - 0.45 * h, axis=1) & (np.linalg.norm(lat, axis=1) > r + 0.6 * h)
+    pts.append(lat[keep])
+    P = np.vstack(pts)
+    for ax in range(3):                                # exact face coordinates
+        col = P[:, ax]
+        col[np.abs(col + half) < 1e-9 * size] = -half
+        col[np.abs(col - half) < 1e-9 * size] = half
+    P, idx = np.unique(np.round(P, 12), axis=0, return_index=True)
+    tri = Delaunay(P)
+    T = tri.simplices.astype(np.int64)
+    c = P[T].mean(axis=1)
+    T = T[np.linalg.norm(c, axis=1) > r]
+    a = P[T]
+    v6 = np.abs(np.einsum("ij,ij->i", a[:, 1] - a[:, 0], np.cross(a[:, 2] - a[:, 0], a[:, 3] - a[:, 0])))
+    T = T[v6 > 1e-9 * h ** 3]
+    used = np.unique(T)
+    remap = -np.ones(len(P), dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    nodes = P[used]
+    elems = remap[T]
+    # boundary faces = faces of exactly one tetrahedron
+    F = np.concatenate([elems[:, [1, 2, 3]], elems[:, [0, 2, 3]], elems[:, [0, 1, 3]], elems[:, [0, 1, 2]]])
+    F.sort(axis=1)
+    uf, cnt = np.unique(F, axis=0, return_counts=True)
+    bf = uf[cnt == 1]
+    tol = 1e-9 * size
+    segs = {}
+    on = {}
+    for ax, name in enumerate("xyz"):
+        on[(ax, 0)] = np.all(np.abs(nodes[bf][:, :, ax] + half) < tol, axis=1)
+        on[(ax, 1)] = np.all(np.abs(nodes[bf][:, :, ax] - half) < tol, axis=1)
+        segs[f"Periodic_{name}_a"] = bf[on[(ax, 0)]]
+        segs[f"Periodic_{name}_b"] = bf[on[(ax, 1)]]
+    outer = np.zeros(len(bf), dtype=bool)
+    for v in on.values():
+        outer |= v
+    segs["Boundary"] = bf[~outer]
+    # periodic node pairs, and a check that the face triangulations are translates
+    periodic = {}
+    for ax, name in enumerate("xyz"):
+        lo = np.where(np.abs(nodes[:, ax] + half) < tol)[0]
+        hi = np.where(np.abs(nodes[:, ax] - half) < tol)[0]
+        o = [b for b in range(3) if b != ax]
+        kl = {tuple(np.round(nodes[i, o], 9)): i for i in lo}
+        kh = {tuple(np.round(nodes[i, o], 9)): i for i in hi}
+        if set(kl) != set(kh):
+            raise RuntimeError("periodic face nodes do not match; change the seed")
+        pairs = np.array([[kl[key], kh[key]] for key in sorted(kl)], dtype=np.int64)
+        periodic[name] = pairs
+        m = dict(zip(pairs[:, 0], pairs[:, 1]))
+        ta = {tuple(sorted(m[i] for i in t)) for t in segs[f"Periodic_{name}_a"]}
+        tb = {tuple(sorted(t)) for t in segs[f"Periodic_{name}_b"]}
+        if ta != tb:
+            raise RuntimeError("periodic face triangulations differ; change the seed")
+    return PeriodicCell2D(nodes=nodes, elems=elems, segments=segs, periodic=periodic, size=size,
+                          porosity=porosity, pore="sphere", seed=seed, meta={"h": h, "r": r})
+
+
 def write_msh2(cell: PeriodicCell2D, filename: str) -> str:
     """Write `cell` as gmsh msh2 text (``filename`` gets the ``.msh`` suffix if missing)."""
     if not filename.endswith(".msh"):
         filename = filename + ".msh"
-    out = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$PhysicalNames", str(len(REGIONS) + 1)]
-    for t, name in enumerate(REGIONS, start=1):
-        out.append(f'1 {t} "{name}"')
-    bulk_tag = len(REGIONS) + 1
-    out.append(f'2 {bulk_tag} "Bulk"')
+    three = cell.elems.shape[1] == 4 and cell.nodes.shape[1] == 3
+    regions = REGIONS_3D if three else REGIONS
+    fdim, face_type, bulk_type = (2, 2, 4) if three else (1, 1, 2)
+    out = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$PhysicalNames", str(len(regions) + 1)]
+    for t, name in enumerate(regions, start=1):
+        out.append(f'{fdim} {t} "{name}"')
+    bulk_tag = len(regions) + 1
+    out.append(f'{fdim + 1} {bulk_tag} "Bulk"')
     out += ["$EndPhysicalNames", "$Nodes", str(len(cell.nodes))]
-    for i, (x, y) in enumerate(cell.nodes, start=1):
-        out.append(f"{i} {x:.17g} {y:.17g} 0")
+    for i, p in enumerate(cell.nodes, start=1):
+        z = p[2] if three else 0
+        out.append(f"{i} {p[0]:.17g} {p[1]:.17g} {z:.17g}" if three else f"{i} {p[0]:.17g} {p[1]:.17g} 0")
     out += ["$EndNodes", "$Elements"]
     lines = []
     eid = 1
-    for t, name in enumerate(REGIONS, start=1):
-        for a, b in cell.segments[name]:
-            lines.append(f"{eid} 1 2 {t} {t} {a + 1} {b + 1}")
+    for t, name in enumerate(regions, start=1):
+        for f in cell.segments[name]:
+            lines.append(f"{eid} {face_type} 2 {t} {t} " + " ".join(str(int(x) + 1) for x in f))
             eid += 1
-    for a, b, c in cell.elems:
-        lines.append(f"{eid} 2 2 {bulk_tag} 1 {a + 1} {b + 1} {c + 1}")
+    for e in cell.elems:
+        lines.append(f"{eid} {bulk_type} 2 {bulk_tag} 1 " + " ".join(str(int(x) + 1) for x in e))
         eid += 1
     out.append(str(len(lines)))
     out += lines
-    out += ["$EndElements", "$Periodic", "2"]
-    # curve entity tags: 2 = x_a, 3 = x_b, 4 = y_a, 5 = y_b
-    for axis, (slave, master) in (("x", (2, 3)), ("y", (4, 5))):
+    axes = (("x", (2, 3)), ("y", (4, 5)), ("z", (6, 7))) if three else (("x", (2, 3)), ("y", (4, 5)))
+    out += ["$EndElements", "$Periodic", str(len(axes))]
+    # entity tags: 2 = x_a, 3 = x_b, 4 = y_a, 5 = y_b (, 6 = z_a, 7 = z_b); surfaces carry an Affine line
+    for axis, (slave, master) in axes:
         pr = cell.periodic[axis]
-        out.append(f"1 {slave} {master}")
+        out.append(f"{fdim} {slave} {master}")
+        if three:
+            tr = [0.0, 0.0, 0.0]
+            tr["xyz".index(axis)] = -cell.size
+            out.append("Affine 1 0 0 {} 0 1 0 {} 0 0 1 {} 0 0 0 1".format(*tr))
         out.append(str(len(pr)))
         for s, m in pr:
             out.append(f"{s + 1} {m + 1}")

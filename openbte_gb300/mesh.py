@@ -84,18 +84,25 @@ def get_mesh(filename: str = "mesh") -> Mesh:
 
 
 def mesh_from_cell(cell) -> Mesh:
-    """Build a ``Mesh`` directly from a ``geometry.PeriodicCell2D`` (same result as write + read)."""
-    from .geometry import REGIONS
-    labels = {t: name for t, name in enumerate(REGIONS, start=1)}
-    labels[len(REGIONS) + 1] = "Bulk"
+    """Build a ``Mesh`` directly from a ``geometry`` cell, 2D or 3D (same result as write + read)."""
+    from .geometry import REGIONS, REGIONS_3D
+    three = cell.elems.shape[1] == 4 and cell.nodes.shape[1] == 3
+    regions = REGIONS_3D if three else REGIONS
+    face_type, bulk_type = (2, 4) if three else (1, 2)
+    labels = {t: name for t, name in enumerate(regions, start=1)}
+    labels[len(regions) + 1] = "Bulk"
     elements = []
-    for t, name in enumerate(REGIONS, start=1):
-        for a, b in cell.segments[name]:
-            elements.append((1, t, [int(a), int(b)]))
+    for t, name in enumerate(regions, start=1):
+        for f in cell.segments[name]:
+            elements.append((face_type, t, [int(x) for x in f]))
     for e in cell.elems:
-        elements.append((2, len(REGIONS) + 1, [int(x) for x in e]))
-    nodes = np.concatenate([cell.nodes, np.zeros((len(cell.nodes), 1))], axis=1)
-    periodic = [(1, 2, 3, cell.periodic["x"]), (1, 4, 5, cell.periodic["y"])]
+        elements.append((bulk_type, len(regions) + 1, [int(x) for x in e]))
+    if three:
+        nodes = np.asarray(cell.nodes, dtype=np.float64)
+        periodic = [(2, 2, 3, cell.periodic["x"]), (2, 4, 5, cell.periodic["y"]), (2, 6, 7, cell.periodic["z"])]
+    else:
+        nodes = np.concatenate([cell.nodes, np.zeros((len(cell.nodes), 1))], axis=1)
+        periodic = [(1, 2, 3, cell.periodic["x"]), (1, 4, 5, cell.periodic["y"])]
     return build_mesh(labels, nodes, elements, periodic)
 
 
@@ -203,13 +210,22 @@ def build_mesh(labels, nodes3, elements, periodic) -> Mesh:
                 node_side.setdefault(int(t), []).append(s)
         b_regions = [(k, set(v)) for k, v in side_physical_regions.items() if k[-2:] == "_b"]
         in_periodic = set()
+        cent = side_centroids.tolist()
+        nl = nodes.tolist()
+
+        def close(p, q):
+            # the default np.allclose test |p - q| <= 1e-8 + 1e-5 |q| on every component
+            return all(abs(x - y) <= 1e-8 + 1e-5 * abs(y) for x, y in zip(p, q))
+
         for (_, _, _, pairs) in periodic:
-            for a, b in pairs:
-                L = nodes[a] - nodes[b]
+            for a, b in pairs.tolist():
+                L = [u - v for u, v in zip(nl[a], nl[b])]
                 corr = []
-                for s1 in node_side.get(int(a), []):
-                    for s2 in node_side.get(int(b), []):
-                        if np.allclose(side_centroids[s1], side_centroids[s2] + L):
+                # candidate sides are visited in Python-set order, as the reference does
+                # (openbte/mesh.py:236-244); in 3D one node pair matches several sides
+                for s1 in set(node_side.get(int(a), [])):
+                    for s2 in set(node_side.get(int(b), [])):
+                        if close(cent[s1], [c + d for c, d in zip(cent[s2], L)]):
                             corr.append((s1, s2))
                 for s1, s2 in corr:
                     for key, value in b_regions:

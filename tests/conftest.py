@@ -22,14 +22,19 @@ def load_case(name):
     from openbte_gb300 import objects as O
     d = dict(np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False))
     segs = {k[4:]: d[k] for k in d if k.startswith("seg_")}
-    cell = PeriodicCell2D(nodes=d["nodes"], elems=d["elems"], segments=segs,
-                          periodic={"x": d["periodic_x"], "y": d["periodic_y"]}, size=float(d["size"]),
-                          porosity=float(d["porosity"]), pore=str(d["pore"]), seed=int(d["seed"]))
+    periodic = {"x": d["periodic_x"], "y": d["periodic_y"]}
+    jumps = {"Periodic_x": 1, "Periodic_y": 0}
+    if "periodic_z" in d:
+        periodic["z"] = d["periodic_z"]
+        jumps["Periodic_z"] = 0
+    cell = PeriodicCell2D(nodes=d["nodes"], elems=d["elems"], segments=segs, periodic=periodic,
+                          size=float(d["size"]), porosity=float(d["porosity"]), pore=str(d["pore"]),
+                          seed=int(d["seed"]))
     geo = mesh_from_cell(cell)
     n_mfp, n_phi = d["t_coeff"].shape
     mat = O.Material(d["kappa_bulk"], d["sigma"], d["vmfp"], d["t_coeff"], d["mfps"], (n_mfp, n_phi), 0.0, 0.0)
-    bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
-    ek = O.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
+    bcs = O.BoundaryConditions(periodic=jumps, diffuse="Boundary")
+    ek = O.EffectiveThermalConductivity(normalization=float(d.get("normalization", -1.0)), contact="Periodic_x")
     return geo, mat, bcs, ek, d
 
 

@@ -27,8 +27,8 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 sys.path.insert(0, HERE)
 
 import ref_loader  # noqa: E402
-from openbte_gb300.geometry import porous_cell_2d, write_msh2  # noqa: E402
-from openbte_gb300.material import synthetic_isotropic_2d, Gray2D  # noqa: E402
+from openbte_gb300.geometry import porous_cell_2d, porous_cube_3d, write_msh2  # noqa: E402
+from openbte_gb300.material import synthetic_isotropic_2d, synthetic_isotropic_3d, Gray2D  # noqa: E402
 
 CASES = [
     # name, n_tri, porosity, pore, seed, material kind, material args
@@ -36,6 +36,7 @@ CASES = [
     ("c0_2k", 2000, 0.25, "square", 1, "synthetic", dict(n_mfp=30, n_phi=48)),
     ("circ1k", 1000, 0.30, "circle", 2, "synthetic", dict(n_mfp=10, n_phi=24)),
     ("gray600", 600, 0.20, "square", 7, "gray", dict(MFP=100.0, n_phi=32, kappa=150.0)),
+    ("cube1k5", 1500, 0.10, "sphere", 3, "synthetic3d", dict(n_mfp=6, n_theta=4, n_phi=8)),
 ]
 
 MESH_FIELDS = ["side_elem_map", "normal_areas", "elem_volumes", "side_areas", "internal", "interp_weights",
@@ -43,16 +44,25 @@ MESH_FIELDS = ["side_elem_map", "normal_areas", "elem_volumes", "side_areas", "i
 
 
 def run_case(R, name, n_tri, porosity, pore, seed, kind, margs, tmpdir):
-    cell = porous_cell_2d(n_tri, porosity, pore, seed=seed)
+    if pore == "sphere":
+        cell = porous_cube_3d(n_tri, porosity, seed=seed)
+        periodic = {"Periodic_x": 1, "Periodic_y": 0, "Periodic_z": 0}
+    else:
+        cell = porous_cell_2d(n_tri, porosity, pore, seed=seed)
+        periodic = {"Periodic_x": 1, "Periodic_y": 0}
     path = write_msh2(cell, os.path.join(tmpdir, name))
     geo = R.mesh.get_mesh(path[:-4])
     if kind == "synthetic":
         mat = synthetic_isotropic_2d(**margs)
+    elif kind == "synthetic3d":
+        mat = synthetic_isotropic_3d(**margs)
     else:
         mat = Gray2D(**margs)
     rmat = R.objects.Material(*mat)
-    bcs = R.objects.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
-    ek = R.objects.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
+    bcs = R.objects.BoundaryConditions(periodic=periodic, diffuse="Boundary")
+    # -L_x / (contact area per unit length in 2D, contact area in 3D) / DeltaT
+    normalization = -1.0 if pore != "sphere" else -1.0 / cell.size
+    ek = R.objects.EffectiveThermalConductivity(normalization=normalization, contact="Periodic_x")
     out = io.StringIO()
     t0 = time.time()
     with contextlib.redirect_stdout(out):
@@ -67,7 +77,8 @@ def run_case(R, name, n_tri, porosity, pore, seed, kind, margs, tmpdir):
     d = dict(
         nodes=cell.nodes, elems=cell.elems, size=cell.size, porosity=cell.porosity, pore=cell.pore, seed=cell.seed,
         periodic_x=cell.periodic["x"], periodic_y=cell.periodic["y"],
-        mat_kind=kind, mat_args=repr(margs),
+        **({"periodic_z": cell.periodic["z"]} if "z" in cell.periodic else {}),
+        mat_kind=kind, mat_args=repr(margs), normalization=normalization, jumps=repr(periodic),
         mfps=mat.mfps, vmfp=mat.vmfp, sigma=mat.sigma, t_coeff=mat.t_coeff, kappa_bulk=mat.thermal_conductivity,
         fourier_T=f.variables["Temperature_Fourier"]["data"], fourier_J=f.variables["Flux_Fourier"]["data"],
         fourier_kappa_printed=kappa_fourier, fourier_kappa_returned=f.kappa_eff,

@@ -59,7 +59,7 @@ def test_sweep_equals_exact_ordinate_solves(case, precision, tol):
     np.testing.assert_allclose(o[n + len(TB):], x, rtol=0, atol=tol * scale)
 
 
-@pytest.mark.parametrize("name", ["a600", "gray600", "circ1k", "c0_2k"])
+@pytest.mark.parametrize("name", ["a600", "gray600", "circ1k", "c0_2k", "cube1k5"])
 def test_bte_fp64_matches_reference(case, name):
     from openbte_gb300 import BTE_RTA
     geo, mat, bcs, ek, d = case(name)

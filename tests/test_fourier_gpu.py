@@ -5,7 +5,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["a600", "circ1k", "gray600", "c0_2k"])
+@pytest.mark.parametrize("name", ["a600", "circ1k", "gray600", "c0_2k", "cube1k5"])
 def test_fourier_matches_reference(case, name):
     from openbte_gb300 import Fourier
     geo, mat, bcs, ek, d = case(name)

@@ -7,7 +7,7 @@ import fourier_oracle
 from openbte_gb300 import objects as O
 
 
-@pytest.mark.parametrize("name", ["a600", "circ1k", "gray600"])
+@pytest.mark.parametrize("name", ["a600", "circ1k", "gray600", "cube1k5"])
 def test_fourier_oracle_matches_reference(case, name):
     geo, mat, bcs, ek, d = case(name)
     k, T, J, it = fourier_oracle.fourier(geo, mat.thermal_conductivity, bcs, ek)
@@ -17,7 +17,7 @@ def test_fourier_oracle_matches_reference(case, name):
     assert d["fourier_kappa_returned"] == 0                           # the reference's while/else
 
 
-@pytest.mark.parametrize("name", ["a600", "gray600"])
+@pytest.mark.parametrize("name", ["a600", "gray600", "cube1k5"])
 def test_bte_oracle_matches_reference(case, name):
     geo, mat, bcs, ek, d = case(name)
     f = O.SolverResults(variables={"Temperature_Fourier": {"data": d["fourier_T"]}})

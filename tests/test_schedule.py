@@ -6,7 +6,7 @@ import sweep_order
 from openbte_gb300.runtime import HostProblem, Plan
 
 
-@pytest.mark.parametrize("name", ["a600", "c0_2k", "circ1k"])
+@pytest.mark.parametrize("name", ["a600", "c0_2k", "circ1k", "cube1k5"])
 def test_schedule_bit_exact(case, name):
     geo, mat, bcs, ek, _ = case(name)
     plan = Plan(HostProblem(geo, mat, bcs, ek), host_only=True)
