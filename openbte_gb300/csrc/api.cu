@@ -158,6 +158,8 @@ extern "C" obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision
           s.lev_ptr.size() + s.wo_wall.size()) * 4;
     b += (s.in_coef.size() + s.D.size() + s.P.size() + s.mfp.size() + s.tco.size() + s.sig.size() +
           s.wo_gg.size() + s.kcoef.size() + s.scoef.size() + s.hs.size()) * rb;
+    b += s.wo_wall.size() * 24 * rb;              // wall weights regrouped by chunk (padding to the chunk width)
+    b += (s.lev_ptr.size() + s.in_idx.size()) * 8; // unit tables and periodic prefetch lists (bound)
     return (int64_t)b;
   };
   int64_t pb = (int64_t)plan->nu * 8 + (int64_t)s.x_cell.size() * 4 + (int64_t)s.kconst.size() * 24;

@@ -124,9 +124,10 @@ obte_status build_schedule(const obte_problem* prob, const obte_material* mat, S
 struct DevSchedule {
   bool ready = false;
   int mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;
+  int emax = 0, unit_wo = 0, pf_pad = 0;   // periodic bank rows, per-unit staging sizes
   size_t smem = 0;
-  DevBuf rec, klev_ptr, klev_off, knlev, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap, Pq, si, sr,
-      wo_off, spec;
+  DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap,
+      Pq, si, sr, wo_off, spec;
   size_t bytes() const;
 };
 

@@ -13,15 +13,20 @@
 //
 // T_up lives in a ring of shared-memory rows, one per live upstream element
 // and one column per MFP (row-major by MFP).  Extra rows: a zero row for absent
-// faces, a trash row for elements nobody reads, and one row per periodic
-// source element of the direction, filled from the state vector at CTA start,
-// so inflow across a cut periodic face is an ordinary row read.  The MFP loop
-// is therefore branch-free; elements with per-MFP outputs (periodic source,
-// wall re-emission, contact) read their T back from their row afterwards.
+// faces, a trash row for elements nobody reads, and two banks of rows for the
+// inflow across cut periodic faces: while unit u runs, its threads load the
+// periodic source values unit u+1 reads from the state vector and store them
+// into bank (u+1) & 1, so inflow across a cut face is an ordinary row read and
+// the ring does not grow with the number of periodic sources (3D meshes have
+// thousands per direction).  The MFP loop is therefore branch-free; elements
+// with per-MFP outputs (periodic source, wall re-emission, contact) read their
+// T back from their row afterwards.
 //
-// Data movement per unit: the packed element records and the per-sweep values
-// (b, p) arrive in shared memory by TMA bulk copies (cp.async.bulk + mbarrier)
-// issued one unit ahead.  T never goes to HBM.  Reductions of
+// Data movement per unit: the packed element records, the per-sweep values
+// (b, p), the wall re-emission weights of the unit's wall entries and the
+// periodic prefetch list of the next unit arrive in shared memory by TMA bulk
+// copies (cp.async.bulk + mbarrier) issued two units ahead.  T never goes to
+// HBM.  Reductions of
 // openbte/bte.py:222-243 are register accumulations over the MFP loop followed
 // by one FP64 atomic per element (DeltaT', T_B', J) or per MFP (K, S).
 // Every mbarrier wait is bounded; on timeout the CTA raises the device error
@@ -56,21 +61,92 @@ template <> struct Rec<double> { static constexpr int W = 16, COEF = 6, CSTEP = 
 //   sr: wc0 wc1 wc2 pad                          (4 reals)
 static constexpr int SI = 8, SR = 4;
 
+// Level units: each level of direction q split into runs of at most kUnit elements.
+struct Units {
+  std::vector<int32_t> ptr;   // per direction: n[q] + 1 positions (relative to the direction)
+  std::vector<int64_t> off;   // [n_dir] first entry of direction q in ptr (and in kpf, kwo)
+  std::vector<int32_t> n;     // [n_dir] units of direction q
+};
+
+static void build_units(const Schedule& s, Units& un) {
+  un.ptr.clear();
+  un.off.assign(s.n_dir, 0);
+  un.n.assign(s.n_dir, 0);
+  for (int q = 0; q < s.n_dir; ++q) {
+    un.off[q] = (int64_t)un.ptr.size();
+    const int32_t* lp = s.lev_ptr.data() + s.lev_off[q];
+    un.ptr.push_back(0);
+    for (int Lv = 0; Lv < s.nlev[q]; ++Lv)
+      for (int32_t a = lp[Lv]; a < lp[Lv + 1]; a += kUnit) {
+        un.ptr.push_back(std::min(a + kUnit, lp[Lv + 1]));
+        un.n[q]++;
+      }
+  }
+}
+
 struct Packed {
   std::vector<int32_t> rec, cellmap, si, spec;
   std::vector<double> P, sr;
+  // periodic inflow prefetch: the source indices read by unit u (one entry per cut inflow face, in
+  // element then face order), each unit's list padded with -1 to a multiple of 4 ints; kpf[u] is the
+  // absolute start of unit u's list (n[q] + 1 entries per direction, indexed like Units::ptr)
+  std::vector<int32_t> pf, kpf;
+  std::vector<int32_t> kwo;   // first wall re-emission entry of unit u, relative to the direction
+  int emax = 0;               // most cut inflow faces in one unit
+  int pf_pad = 0;             // longest padded list
+  int unit_wo = 0;            // most wall re-emission entries in one unit
+  int rows = 0;               // ring rows
 };
 
-// Ring rows: [0, S) slots, S zero row, S+1 trash row, S+2+k periodic source k.
+static int ring_rows(const Schedule& s, int emax) { return s.max_slots + 2 + 2 * emax; }
+
+// Ring rows: [0, S) slots, S zero row, S+1 trash row, then two banks of emax rows that alternate
+// by unit parity: the cut inflow values of unit u live in bank u & 1, written during unit u - 1
+// (at CTA start for unit 0) from the state vector.
 template <typename Real>
-static obte_status pack(const Schedule& s, Packed& pk) {
+static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
   constexpr int W = Rec<Real>::W;
   const int S = s.max_slots;
-  const int zero_row = S, trash_row = S + 1, per_row = S + 2;
-  if (S + 2 + s.max_src >= 65535) {
+  const int zero_row = S, trash_row = S + 1, prow0 = S + 2;
+  // pass 1: per-unit counts of cut inflow faces and wall re-emission entries
+  pk.emax = pk.pf_pad = pk.unit_wo = 0;
+  pk.kwo.assign(un.ptr.size(), 0);
+  pk.kpf.assign(un.ptr.size(), 0);
+  int64_t n_pf = 0;
+  for (int q = 0; q < s.n_dir; ++q) {
+    const int32_t* up = un.ptr.data() + un.off[q];
+    int32_t wo_run = 0;
+    for (int u = 0; u < un.n[q]; ++u) {
+      int cnt = 0, wcnt = 0;
+      for (int32_t pos = up[u]; pos < up[u + 1]; ++pos) {
+        const size_t it = (size_t)q * s.n + pos;
+        for (int f = 0; f < s.nf; ++f)
+          if ((int)((uint32_t)s.in_idx[it * s.nf + f] >> ITEM_SHIFT) == ITEM_PERIODIC) ++cnt;
+        wcnt += s.wout[it] & 7;
+      }
+      const int padded = (cnt + 3) & ~3;
+      pk.kwo[un.off[q] + u] = wo_run;
+      pk.kpf[un.off[q] + u] = (int32_t)n_pf;
+      wo_run += wcnt;
+      n_pf += padded;
+      pk.emax = std::max(pk.emax, cnt);
+      pk.pf_pad = std::max(pk.pf_pad, padded);
+      pk.unit_wo = std::max(pk.unit_wo, wcnt);
+    }
+    pk.kwo[un.off[q] + un.n[q]] = wo_run;
+    pk.kpf[un.off[q] + un.n[q]] = (int32_t)n_pf;
+    if (wo_run != s.wo_off[q + 1] - s.wo_off[q]) {
+      set_error("wall re-emission entries are not in sweep order");
+      return OBTE_ERR_BAD_ARG;
+    }
+  }
+  if (n_pf >= (int64_t)1 << 31) { set_error("too many periodic inflow faces"); return OBTE_ERR_UNSUPPORTED; }
+  pk.rows = ring_rows(s, pk.emax);
+  if (pk.rows >= 65535 || s.max_src >= (1 << 30)) {
     set_error("sweep ring rows do not fit 16-bit indices");
     return OBTE_ERR_UNSUPPORTED;
   }
+  pk.pf.assign((size_t)n_pf, -1);
   const size_t total = (size_t)s.n_dir * s.n;
   pk.rec.assign(total * W, 0);
   pk.cellmap.assign(total, 0);
@@ -78,67 +154,84 @@ static obte_status pack(const Schedule& s, Packed& pk) {
   pk.P.assign(total, 0.0);
   pk.si.clear();
   pk.sr.clear();
-  for (size_t it = 0; it < total; ++it) {
-    int32_t* r = pk.rec.data() + it * W;
-    const int32_t so = s.slot[it] >= 0 ? s.slot[it] : trash_row;
-    r[0] = s.cell[it];
-    // wall re-emission entries: begin relative to the direction's first entry (staged in shared memory)
-    r[4] = s.wout[it] ? (((s.wout[it] >> 3) - s.wo_off[it / s.n]) << 3) | (s.wout[it] & 7) : 0;
-    r[5] = s.contact[it] + 1;
-    pk.cellmap[it] = s.cell[it];
-    pk.P[it] = s.P[it];
-    int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0};
-    double sr[SR] = {0, 0, 0, 0};
-    const bool outputs = s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0;
-    if (outputs && s.slot[it] < 0) {
-      set_error("element with per-MFP outputs has no ring slot");
-      return OBTE_ERR_BAD_ARG;
-    }
-    bool special = outputs;
-    double coef[4] = {0, 0, 0, 0};
-    int32_t row_in[4] = {zero_row, zero_row, zero_row, zero_row};
-    int k = 0;
-    for (int f = 0; f < s.nf; ++f) {
-      const int32_t code = s.in_idx[it * s.nf + f];
-      const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
-      const int32_t idx = code & ITEM_MASK;
-      const double g = s.in_coef[it * s.nf + f];
-      if (kind == ITEM_CELL || kind == ITEM_PERIODIC) {
-        row_in[k] = kind == ITEM_CELL ? idx : per_row + idx;
-        coef[k] = g;
-        ++k;
-      } else if (kind == ITEM_WALL) {
-        if (si[3] >= 3) { set_error("more than three wall inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
-        si[4 + si[3]] = idx;
-        sr[si[3]] = g;
-        si[3]++;
-        special = true;
+  // pass 2: records
+  for (int q = 0; q < s.n_dir; ++q) {
+    const int32_t* up = un.ptr.data() + un.off[q];
+    for (int u = 0; u < un.n[q]; ++u) {
+      int ent = 0;
+      const int bank = prow0 + (u & 1) * pk.emax;
+      int32_t* plist = pk.pf.data() + pk.kpf[un.off[q] + u];
+      for (int32_t pos = up[u]; pos < up[u + 1]; ++pos) {
+        const size_t it = (size_t)q * s.n + pos;
+        int32_t* r = pk.rec.data() + it * W;
+        const int32_t so = s.slot[it] >= 0 ? s.slot[it] : trash_row;
+        r[0] = s.cell[it];
+        // wall re-emission entries: begin relative to the direction's first entry
+        r[4] = s.wout[it] ? (((s.wout[it] >> 3) - s.wo_off[q]) << 3) | (s.wout[it] & 7) : 0;
+        r[5] = s.contact[it] + 1;
+        pk.cellmap[it] = s.cell[it];
+        pk.P[it] = s.P[it];
+        int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0};
+        double sr[SR] = {0, 0, 0, 0};
+        const bool outputs = s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0;
+        if (outputs && s.slot[it] < 0) {
+          set_error("element with per-MFP outputs has no ring slot");
+          return OBTE_ERR_BAD_ARG;
+        }
+        bool special = outputs;
+        double coef[4] = {0, 0, 0, 0};
+        int32_t row_in[4] = {zero_row, zero_row, zero_row, zero_row};
+        int k = 0;
+        for (int f = 0; f < s.nf; ++f) {
+          const int32_t code = s.in_idx[it * s.nf + f];
+          const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
+          const int32_t idx = code & ITEM_MASK;
+          const double g = s.in_coef[it * s.nf + f];
+          if (kind == ITEM_CELL || kind == ITEM_PERIODIC) {
+            if (kind == ITEM_CELL) {
+              row_in[k] = idx;
+            } else {
+              plist[ent] = idx;
+              row_in[k] = bank + ent;
+              ++ent;
+            }
+            coef[k] = g;
+            ++k;
+          } else if (kind == ITEM_WALL) {
+            if (si[3] >= 3) { set_error("more than three wall inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
+            si[4 + si[3]] = idx;
+            sr[si[3]] = g;
+            si[3]++;
+            special = true;
+          }
+        }
+        r[1] = (so & 0xFFFF) | (row_in[0] << 16);
+        r[2] = (row_in[1] & 0xFFFF) | (row_in[2] << 16);
+        r[3] = (row_in[3] & 0xFFFF) | ((s.xk[it] + 1) << 16);
+        if (special) {
+          pk.spec[it] = (int32_t)(pk.si.size() / SI);
+          pk.si.insert(pk.si.end(), si, si + SI);
+          pk.sr.insert(pk.sr.end(), sr, sr + SR);
+        }
+        if (sizeof(Real) == 4) {
+          for (int f = 0; f < 4; ++f) {
+            float v = (float)coef[f];
+            std::memcpy(&r[Rec<float>::COEF + f], &v, 4);
+          }
+          float d = (float)s.D[it];
+          std::memcpy(&r[Rec<float>::D], &d, 4);
+        } else {
+          for (int f = 0; f < 4; ++f) std::memcpy(&r[Rec<double>::COEF + 2 * f], &coef[f], 8);
+          std::memcpy(&r[Rec<double>::D], &s.D[it], 8);
+        }
       }
-    }
-    r[1] = (so & 0xFFFF) | (row_in[0] << 16);
-    r[2] = (row_in[1] & 0xFFFF) | (row_in[2] << 16);
-    r[3] = (row_in[3] & 0xFFFF) | ((s.xk[it] + 1) << 16);
-    if (special) {
-      pk.spec[it] = (int32_t)(pk.si.size() / SI);
-      pk.si.insert(pk.si.end(), si, si + SI);
-      pk.sr.insert(pk.sr.end(), sr, sr + SR);
-    }
-    if (sizeof(Real) == 4) {
-      for (int f = 0; f < 4; ++f) {
-        float v = (float)coef[f];
-        std::memcpy(&r[Rec<float>::COEF + f], &v, 4);
-      }
-      float d = (float)s.D[it];
-      std::memcpy(&r[Rec<float>::D], &d, 4);
-    } else {
-      for (int f = 0; f < 4; ++f) std::memcpy(&r[Rec<double>::COEF + 2 * f], &coef[f], 8);
-      std::memcpy(&r[Rec<double>::D], &s.D[it], 8);
     }
   }
   if (pk.si.empty()) {
     pk.si.assign(SI, 0);
     pk.sr.assign(SR, 0.0);
   }
+  if (pk.pf.empty()) pk.pf.assign(4, -1);
   return OBTE_OK;
 }
 
@@ -216,19 +309,23 @@ struct SweepParams {
   int n_chunks;            // chunks of MCP MFPs per direction
   int rows;                // ring rows
   int S;                   // slot rows before the zero/trash/periodic rows
+  int emax;                // rows per periodic bank
+  int unit_wo, pf_pad;     // staging sizes: wall entries and prefetch-list ints per unit
   const int32_t* __restrict__ rec;
   const Real* __restrict__ vals;
-  const int32_t* __restrict__ lev_ptr;
+  const int32_t* __restrict__ lev_ptr;   // unit boundaries (n[q] + 1 per direction)
   const int64_t* __restrict__ lev_off;
-  const int32_t* __restrict__ nlev;
+  const int32_t* __restrict__ nlev;      // units per direction
+  const int32_t* __restrict__ kwo;       // first wall entry of each unit (relative to the direction)
+  const int32_t* __restrict__ kpf;       // start of each unit's prefetch list in pf
+  const int32_t* __restrict__ pf;        // periodic source index per cut inflow face (-1 = padding)
   const int64_t* __restrict__ x_base;
   const int32_t* __restrict__ wo_off;   // [n_dir+1] first wall-output entry of each direction
-  int max_wo;
   const int32_t* __restrict__ wo_wall;
   const Real* __restrict__ mfp;    // [m_pad]
   const Real* __restrict__ tco;    // [n_dir * m_pad]
   const Real* __restrict__ sig;    // [n_dir * m_pad * ds]
-  const Real* __restrict__ wo_gg;  // [n_wo * m_pad]
+  const Real* __restrict__ wo_gg;  // [direction][chunk][entry][MCP]
   const Real* __restrict__ kcoef;  // [n_ce * m_pad]
   const Real* __restrict__ scoef;  // [n_ce]
   const double* __restrict__ u_in;
@@ -261,24 +358,28 @@ __device__ __forceinline__ double recip(double x) {
 }
 
 // Shared memory layout (bytes):
-//   [0,64) mbarriers  [64,72) abort flags  [128, ...) NBUF x (records, values) | sig | K S | wall weights | ring
+//   [0,64) mbarriers  [64,72) abort flags
+//   [128, ...) NBUF x records | NBUF x values | NBUF x wall weights | NBUF x prefetch lists | sig | K S | ring
 static constexpr int NBUF = 3;   // TMA pipeline depth (units in flight)
 
 template <typename Real>
 struct SmemLayout {
-  size_t rec, val, rec_stride, val_stride, sig, kacc, sacc, gg, ring, total;
-  __host__ __device__ SmemLayout(int mcp, int rows, int max_wo) {
+  size_t rec, val, gg, pfl, rec_stride, val_stride, gg_stride, pf_stride, sig, kacc, sacc, ring, total;
+  __host__ __device__ SmemLayout(int mcp, int rows, int unit_wo, int pf_pad) {
     constexpr int W = Rec<Real>::W;
     size_t o = 128;
     rec_stride = (size_t)kUnit * W * 4;
     val_stride = (size_t)(kUnit + 2) * 2 * sizeof(Real);
     val_stride = (val_stride + 15) & ~(size_t)15;
+    gg_stride = (size_t)unit_wo * mcp * sizeof(Real);      // mcp * sizeof(Real) is a multiple of 16
+    pf_stride = (size_t)pf_pad * 4;                        // pf_pad is a multiple of 4
     rec = o; o += NBUF * rec_stride;
     val = o; o += NBUF * val_stride;
+    gg = o; o += NBUF * gg_stride;
+    pfl = o; o += NBUF * pf_stride;
     sig = o; o += (size_t)mcp * 3 * sizeof(Real);
     kacc = o; o += (size_t)mcp * sizeof(Real);
     sacc = o; o += (size_t)mcp * sizeof(Real);
-    gg = o; o += (size_t)max_wo * mcp * sizeof(Real);
     o = (o + 15) & ~(size_t)15;
     ring = o; o += (size_t)mcp * rows * sizeof(Real);
     total = o;
@@ -291,13 +392,12 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
   extern __shared__ __align__(128) unsigned char smem[];
   const int rows = p.rows;
-  const SmemLayout<Real> L(MCP, rows, p.max_wo);
+  const SmemLayout<Real> L(MCP, rows, p.unit_wo, p.pf_pad);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   int* s_abort = reinterpret_cast<int*>(smem + 64);
   Real* s_sig = reinterpret_cast<Real*>(smem + L.sig);
   Real* s_k = reinterpret_cast<Real*>(smem + L.kacc);
   Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
-  Real* s_gg = reinterpret_cast<Real*>(smem + L.gg);      // [wall entry of q][MCP]
   Real* ring = reinterpret_cast<Real*>(smem + L.ring);    // [MCP][rows]
 
   const int q = blockIdx.x / p.n_chunks;
@@ -306,15 +406,19 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   const int mc = min(MCP, p.n_mfp - m0);
   const int tid = threadIdx.x;
   const int32_t* __restrict__ lev = p.lev_ptr + p.lev_off[q];
+  const int32_t* __restrict__ kwo = p.kwo + p.lev_off[q];
+  const int32_t* __restrict__ kpf = p.kpf + p.lev_off[q];
   const int nlev = p.nlev[q];
   const int32_t* __restrict__ rec_q = p.rec + (int64_t)q * p.n * W;
   // values: absolute byte offsets from the (256-B aligned) array base keep every TMA window 16-B aligned
   const unsigned char* __restrict__ val_base = reinterpret_cast<const unsigned char*>(p.vals);
   const int64_t val_q0 = (int64_t)q * p.n * VB;
   const int64_t xq = p.x_base[q];
-  const int nsrc = (int)(p.x_base[q + 1] - xq);
   const int wo0 = p.wo_off[q];
   const int nwo = p.wo_off[q + 1] - wo0;
+  // wall weights of this (direction, chunk): [entry][MCP], entries in sweep order
+  const Real* __restrict__ gg_q = p.wo_gg + ((int64_t)wo0 * p.n_chunks + (int64_t)chunk * nwo) * MCP;
+  const int prow0 = p.S + 2;
   const double* __restrict__ X = p.u_in + p.n + p.nd;
   double* __restrict__ dT_out = p.u_out;
   double* __restrict__ TB_out = p.u_out + p.n;
@@ -336,16 +440,16 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
       s_s[j] = 0;
     }
   }
-  for (int i = tid; i < nwo * MCP; i += blockDim.x) {
-    const int e = i / MCP, mm = i - e * MCP;
-    s_gg[i] = mm < mc ? p.wo_gg[(int64_t)(wo0 + e) * p.m_pad + m0 + mm] : Real(0);
-  }
-  // ring: zero the slot/zero/trash rows, fill the periodic-source rows from the state vector
+  // ring: zero everything, then bank 0 holds the cut inflow values of unit 0
+  const int npf0 = nlev > 0 ? kpf[1] - kpf[0] : 0;
   for (int i = tid; i < MCP * rows; i += blockDim.x) {
     const int mm = i / rows, row = i - mm * rows;
     Real v = 0;
-    const int k = row - (p.S + 2);
-    if (k >= 0 && k < nsrc && mm < mc) v = (Real)X[(xq + k) * p.n_mfp + m0 + mm];
+    const int j = row - prow0;
+    if (j >= 0 && j < npf0 && mm < mc) {
+      const int k = p.pf[kpf[0] + j];
+      if (k >= 0) v = (Real)X[(xq + k) * p.n_mfp + m0 + mm];
+    }
     ring[i] = v;
   }
   if (tid == 0) {
@@ -356,7 +460,8 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
   }
   __syncthreads();
 
-  // TMA of unit u into buffer u % NBUF: records [a, e) and values [a, e) (16-B aligned window)
+  // TMA of unit u into buffer u % NBUF: records [a, e), values [a, e) (16-B aligned window), the
+  // wall weights of the unit's wall entries and the prefetch list of unit u + 1
   auto issue = [&](int u) {
     const int a = lev[u], e = lev[u + 1];
     const int bi = u % NBUF;
@@ -364,11 +469,17 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
     const int64_t vb0 = (val_q0 + (int64_t)a * VB) & ~(int64_t)15;
     const int64_t vb1 = (val_q0 + (int64_t)e * VB + 15) & ~(int64_t)15;
     const unsigned vbytes = (unsigned)(vb1 - vb0);
+    const int w0 = kwo[u], w1 = kwo[u + 1];
+    const unsigned gbytes = (unsigned)(w1 - w0) * MCP * (unsigned)sizeof(Real);
+    const int f0 = u + 1 < nlev ? kpf[u + 1] : 0, f1 = u + 1 < nlev ? kpf[u + 2] : 0;
+    const unsigned pbytes = (unsigned)(f1 - f0) * 4u;
     uint64_t* bar = &bars[bi];
     fence_proxy_async();
-    mbar_expect_tx(bar, rbytes + vbytes);
+    mbar_expect_tx(bar, rbytes + vbytes + gbytes + pbytes);
     tma_load_1d(smem + L.rec + bi * L.rec_stride, rec_q + (int64_t)a * W, rbytes, bar);
     tma_load_1d(smem + L.val + bi * L.val_stride, val_base + vb0, vbytes, bar);
+    if (gbytes) tma_load_1d(smem + L.gg + bi * L.gg_stride, gg_q + (int64_t)w0 * MCP, gbytes, bar);
+    if (pbytes) tma_load_1d(smem + L.pfl + bi * L.pf_stride, p.pf + f0, pbytes, bar);
   };
   if (tid == 0)
     for (int u = 0; u < NBUF - 1 && u < nlev; ++u) issue(u);
@@ -377,101 +488,127 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
     const int bi = u % NBUF;
     const int cur = u & 1;
     const int a = lev[u], e = lev[u + 1];
+    const int wu = kwo[u];
+    const int npf = u + 1 < nlev ? kpf[u + 2] - kpf[u + 1] : 0;   // padded length of unit u+1's list
+    const int prow_next = prow0 + ((u + 1) & 1) * p.emax;
     // buffer (u + NBUF - 1) % NBUF was last read during unit u - 1, finished at the barrier below
     if (tid == 0 && u + NBUF - 1 < nlev) issue(u + NBUF - 1);
     const bool ready = mbar_wait_bounded(&bars[bi], (unsigned)(u / NBUF) & 1u);
     if (!ready) {
       s_abort[cur] = 1;
       atomicOr(p.err, 1);
-    } else if (tid < e - a) {
-      // record: W/4 vector loads
-      int32_t r[W];
-      const int4* r4 = reinterpret_cast<const int4*>(smem + L.rec + bi * L.rec_stride) + tid * (W / 4);
+    } else {
+      // cut inflow values of unit u+1: loads issued now, stored into bank (u+1)&1 after the MFP loop
+      const int32_t* s_pf = reinterpret_cast<const int32_t*>(smem + L.pfl + bi * L.pf_stride);
+      const int pk = tid < npf ? s_pf[tid] : -1;
+      double xv[MCP];
+      if (pk >= 0) {
+        const double* xs = X + (xq + pk) * p.n_mfp + m0;
 #pragma unroll
-      for (int i = 0; i < W / 4; ++i) {
-        const int4 x = r4[i];
-        r[4 * i] = x.x; r[4 * i + 1] = x.y; r[4 * i + 2] = x.z; r[4 * i + 3] = x.w;
+        for (int mm = 0; mm < MCP; ++mm) xv[mm] = mm < mc ? __ldg(xs + mm) : 0.0;
       }
-      const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
-      const Real* v = reinterpret_cast<const Real*>(smem + L.val + bi * L.val_stride) + 2 * (voff + tid);
-      const Real b = v[0], pw = v[1];
-      const int c = r[0];
-      const int so = r[1] & 0xFFFF, s0 = (int)((unsigned)r[1] >> 16);
-      const int s1 = r[2] & 0xFFFF, s2 = (int)((unsigned)r[2] >> 16);
-      const int s3 = r[3] & 0xFFFF, xk = (int)((unsigned)r[3] >> 16) - 1;
-      const int wo = r[4], ce = r[5] - 1;
-      const Real c0 = word_real<Real>(r, Rec<Real>::COEF);
-      const Real c1 = word_real<Real>(r, Rec<Real>::COEF + Rec<Real>::CSTEP);
-      const Real c2 = word_real<Real>(r, Rec<Real>::COEF + 2 * Rec<Real>::CSTEP);
-      const Real c3 = word_real<Real>(r, Rec<Real>::COEF + 3 * Rec<Real>::CSTEP);
-      const Real D = word_real<Real>(r, Rec<Real>::D);
-      Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
+      if (tid < e - a) {
+        // record: W/4 vector loads
+        int32_t r[W];
+        const int4* r4 = reinterpret_cast<const int4*>(smem + L.rec + bi * L.rec_stride) + tid * (W / 4);
 #pragma unroll
-      for (int mb = 0; mb < MCP; mb += 4) {
-        Real v0[4], v1[4], v2[4], v3[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const Real* row = ring + (size_t)(mb + j) * rows;
-          v0[j] = row[s0];
-          v1[j] = row[s1];
-          v2[j] = row[s2];
-          if (NF > 3) v3[j] = row[s3];
+        for (int i = 0; i < W / 4; ++i) {
+          const int4 x = r4[i];
+          r[4 * i] = x.x; r[4 * i + 1] = x.y; r[4 * i + 2] = x.z; r[4 * i + 3] = x.w;
         }
+        const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
+        const Real* v = reinterpret_cast<const Real*>(smem + L.val + bi * L.val_stride) + 2 * (voff + tid);
+        const Real b = v[0], pw = v[1];
+        const int c = r[0];
+        const int so = r[1] & 0xFFFF, s0 = (int)((unsigned)r[1] >> 16);
+        const int s1 = r[2] & 0xFFFF, s2 = (int)((unsigned)r[2] >> 16);
+        const int s3 = r[3] & 0xFFFF, xk = (int)((unsigned)r[3] >> 16) - 1;
+        const int wo = r[4], ce = r[5] - 1;
+        const Real c0 = word_real<Real>(r, Rec<Real>::COEF);
+        const Real c1 = word_real<Real>(r, Rec<Real>::COEF + Rec<Real>::CSTEP);
+        const Real c2 = word_real<Real>(r, Rec<Real>::COEF + 2 * Rec<Real>::CSTEP);
+        const Real c3 = word_real<Real>(r, Rec<Real>::COEF + 3 * Rec<Real>::CSTEP);
+        const Real D = word_real<Real>(r, Rec<Real>::D);
+        Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int mm = mb + j;
-          Real s = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
-          if (NF > 3) s += c3 * v3[j];
-          const Real T = (b + lam[mm] * (pw - s)) * recip(Real(1) + lam[mm] * D);
-          ring[(size_t)mm * rows + so] = T;
-          dacc += tt[mm] * T;
-          if (FINAL) {
-            j0 += s_sig[mm * 3] * T;
-            j1 += s_sig[mm * 3 + 1] * T;
-            j2 += s_sig[mm * 3 + 2] * T;
+        for (int mb = 0; mb < MCP; mb += 4) {
+          Real v0[4], v1[4], v2[4], v3[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const Real* row = ring + (size_t)(mb + j) * rows;
+            v0[j] = row[s0];
+            v1[j] = row[s1];
+            v2[j] = row[s2];
+            if (NF > 3) v3[j] = row[s3];
           }
-        }
-      }
-      atomicAdd(&dT_out[c], (double)dacc);
-      if (FINAL) {
-        atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
-        if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
-        if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
-      }
-      // per-MFP outputs of special elements, read back from their own row (shared memory only)
-      if (xk >= 0 || wo != 0 || (FINAL && ce >= 0)) {
-        const int wb = wo >> 3, wn = wo & 7;
-        // gg of absent entries (and padded MFPs) are zero: read the first entry's row instead
-        const Real* g0 = s_gg + wb * MCP;
-        const Real* g1 = s_gg + (wn > 1 ? wb + 1 : wb) * MCP;
-        const Real* g2 = s_gg + (wn > 2 ? wb + 2 : wb) * MCP;
-        Real Ts[MCP];
 #pragma unroll
-        for (int mm = 0; mm < MCP; ++mm) Ts[mm] = ring[(size_t)mm * rows + so];
-        Real w0 = 0, w1 = 0, w2 = 0;
-#pragma unroll
-        for (int mm = 0; mm < MCP; ++mm) {
-          w0 += g0[mm] * Ts[mm];
-          w1 += g1[mm] * Ts[mm];
-          w2 += g2[mm] * Ts[mm];
-        }
-        if (xk >= 0) {
-#pragma unroll
-          for (int mm = 0; mm < MCP; ++mm)
-            if (mm < mc) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)Ts[mm];
-        }
-        if (FINAL && ce >= 0) {
-#pragma unroll
-          for (int mm = 0; mm < MCP; ++mm) {
-            if (mm < mc) {
-              atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * Ts[mm]);
-              atomicAdd(&s_s[mm], p.scoef[ce] * Ts[mm]);
+          for (int j = 0; j < 4; ++j) {
+            const int mm = mb + j;
+            Real s = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
+            if (NF > 3) s += c3 * v3[j];
+            const Real T = (b + lam[mm] * (pw - s)) * recip(Real(1) + lam[mm] * D);
+            ring[(size_t)mm * rows + so] = T;
+            dacc += tt[mm] * T;
+            if (FINAL) {
+              j0 += s_sig[mm * 3] * T;
+              j1 += s_sig[mm * 3 + 1] * T;
+              j2 += s_sig[mm * 3 + 2] * T;
             }
           }
         }
-        if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
-        if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 1]], (double)w1);
-        if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 2]], (double)w2);
+        atomicAdd(&dT_out[c], (double)dacc);
+        if (FINAL) {
+          atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
+          if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
+          if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
+        }
+        // per-MFP outputs of special elements, read back from their own row (shared memory only)
+        if (xk >= 0 || wo != 0 || (FINAL && ce >= 0)) {
+          const int wb = wo >> 3, wn = wo & 7;
+          // staged weights of this unit's entries; absent entries read the first entry's row (unused)
+          const Real* s_gg = reinterpret_cast<const Real*>(smem + L.gg + bi * L.gg_stride) + (wb - wu) * MCP;
+          const Real* g0 = s_gg;
+          const Real* g1 = s_gg + (wn > 1 ? MCP : 0);
+          const Real* g2 = s_gg + (wn > 2 ? 2 * MCP : 0);
+          Real Ts[MCP];
+#pragma unroll
+          for (int mm = 0; mm < MCP; ++mm) Ts[mm] = ring[(size_t)mm * rows + so];
+          Real w0 = 0, w1 = 0, w2 = 0;
+#pragma unroll
+          for (int mm = 0; mm < MCP; ++mm) {
+            w0 += g0[mm] * Ts[mm];
+            w1 += g1[mm] * Ts[mm];
+            w2 += g2[mm] * Ts[mm];
+          }
+          if (xk >= 0) {
+#pragma unroll
+            for (int mm = 0; mm < MCP; ++mm)
+              if (mm < mc) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)Ts[mm];
+          }
+          if (FINAL && ce >= 0) {
+#pragma unroll
+            for (int mm = 0; mm < MCP; ++mm) {
+              if (mm < mc) {
+                atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * Ts[mm]);
+                atomicAdd(&s_s[mm], p.scoef[ce] * Ts[mm]);
+              }
+            }
+          }
+          if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
+          if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 1]], (double)w1);
+          if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 2]], (double)w2);
+        }
+      }
+      // bank (u+1)&1 was last read during unit u-1
+      if (pk >= 0) {
+#pragma unroll
+        for (int mm = 0; mm < MCP; ++mm) ring[(size_t)mm * rows + prow_next + tid] = (Real)xv[mm];
+      }
+      for (int i = tid + kUnit; i < npf; i += kUnit) {   // units with more than kUnit cut inflow faces
+        const int k = s_pf[i];
+        if (k < 0) continue;
+        const double* xs = X + (xq + k) * p.n_mfp + m0;
+        for (int mm = 0; mm < MCP; ++mm) ring[(size_t)mm * rows + prow_next + i] = mm < mc ? (Real)xs[mm] : Real(0);
       }
     }
     __syncthreads();
@@ -495,8 +632,8 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
 // ---- table upload ---------------------------------------------------------------
 
 size_t DevSchedule::bytes() const {
-  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &mfp, &tco, &sig, &wo_wall, &wo_gg, &kcoef, &scoef, &hs,
-                         &vals, &cellmap, &Pq, &si, &sr, &wo_off};
+  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &kwo, &kpf, &pf, &mfp, &tco, &sig, &wo_wall, &wo_gg,
+                         &kcoef, &scoef, &hs, &vals, &cellmap, &Pq, &si, &sr, &wo_off, &spec};
   size_t b = 0;
   for (auto* x : all) b += x->bytes;
   return b;
@@ -519,7 +656,7 @@ constexpr int Widths<double>::v[];
 // Choose the chunk width: minimise waves x (per-unit overhead + chunk width) / resident CTAs,
 // under the shared-memory budget.  OBTE_SWEEP_MCP forces a width (tuning).
 template <typename Real>
-static int choose_mcp(const Schedule& s, int rows, int num_sms, size_t optin) {
+static int choose_mcp(const Schedule& s, int rows, int unit_wo, int pf_pad, int num_sms, size_t optin) {
   const char* env = std::getenv("OBTE_SWEEP_MCP");
   const int forced = env ? std::atoi(env) : 0;
   double best = 1e300;
@@ -527,7 +664,7 @@ static int choose_mcp(const Schedule& s, int rows, int num_sms, size_t optin) {
   for (int i = 0; i < Widths<Real>::N; ++i) {
     const int w = Widths<Real>::v[i];
     if (forced && w != forced) continue;
-    const size_t sm = SmemLayout<Real>(w, rows, s.max_wo).total;
+    const size_t sm = SmemLayout<Real>(w, rows, unit_wo, pf_pad).total;
     if (sm > optin) continue;
     const int per_sm = std::max(1, std::min(8, (int)((228 * 1024) / (sm + 1024))));
     const int chunks = (s.n_mfp + w - 1) / w;
@@ -547,8 +684,13 @@ template <typename Real>
 static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   const Schedule& s = plan->sched;
   cudaStream_t st = plan->stream;
-  const int rows = s.max_slots + 2 + s.max_src;
-  const int mcp = choose_mcp<Real>(s, rows, plan->ctx->num_sms, plan->ctx->smem_optin);
+  // split levels into units of at most kUnit elements (slots were assigned per level, so this stays valid)
+  Units un;
+  build_units(s, un);
+  Packed pk;
+  OBTE_TRY(pack<Real>(s, un, pk));
+  const int rows = pk.rows;
+  const int mcp = choose_mcp<Real>(s, rows, pk.unit_wo, pk.pf_pad, plan->ctx->num_sms, plan->ctx->smem_optin);
   if (!mcp) {
     set_error("sweep front needs more shared memory than one CTA can have (" + std::to_string(rows) + " rows)");
     return OBTE_ERR_UNSUPPORTED;
@@ -558,34 +700,22 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   d.n_chunks = (s.n_mfp + mcp - 1) / mcp;
   d.zero_slot = s.max_slots;
   d.rows = rows;
-  d.smem = SmemLayout<Real>(mcp, rows, s.max_wo).total;
-  // split levels into units of at most kUnit elements (slots were assigned per level, so this stays valid)
-  std::vector<int32_t> kptr;
-  std::vector<int64_t> koff(s.n_dir);
-  std::vector<int32_t> kn(s.n_dir);
-  for (int q = 0; q < s.n_dir; ++q) {
-    koff[q] = (int64_t)kptr.size();
-    const int32_t* lp = s.lev_ptr.data() + s.lev_off[q];
-    int units = 0;
-    kptr.push_back(0);
-    for (int Lv = 0; Lv < s.nlev[q]; ++Lv)
-      for (int32_t a = lp[Lv]; a < lp[Lv + 1]; a += kUnit) {
-        kptr.push_back(std::min(a + kUnit, lp[Lv + 1]));
-        ++units;
-      }
-    kn[q] = units;
-  }
-  Packed pk;
-  OBTE_TRY(pack<Real>(s, pk));
+  d.emax = pk.emax;
+  d.unit_wo = pk.unit_wo;
+  d.pf_pad = pk.pf_pad;
+  d.smem = SmemLayout<Real>(mcp, rows, pk.unit_wo, pk.pf_pad).total;
   OBTE_TRY(upload(d.rec, pk.rec, st));
   OBTE_TRY(upload(d.cellmap, pk.cellmap, st));
   OBTE_TRY(upload(d.Pq, pk.P, st));
   OBTE_TRY(upload(d.si, pk.si, st));
   OBTE_TRY(upload(d.spec, pk.spec, st));
   OBTE_TRY(upload_real<Real>(d.sr, pk.sr, st));
-  OBTE_TRY(upload(d.klev_ptr, kptr, st));
-  OBTE_TRY(upload(d.klev_off, koff, st));
-  OBTE_TRY(upload(d.knlev, kn, st));
+  OBTE_TRY(upload(d.klev_ptr, un.ptr, st));
+  OBTE_TRY(upload(d.klev_off, un.off, st));
+  OBTE_TRY(upload(d.knlev, un.n, st));
+  OBTE_TRY(upload(d.kwo, pk.kwo, st));
+  OBTE_TRY(upload(d.kpf, pk.kpf, st));
+  OBTE_TRY(upload(d.pf, pk.pf, st));
   std::vector<int32_t> wo = s.wo_wall;
   if (wo.empty()) wo.push_back(0);
   OBTE_TRY(upload(d.wo_wall, wo, st));
@@ -593,7 +723,22 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   OBTE_TRY(upload_real<Real>(d.mfp, s.mfp, st));
   OBTE_TRY(upload_real<Real>(d.tco, s.tco, st));
   OBTE_TRY(upload_real<Real>(d.sig, s.sig, st));
-  OBTE_TRY(upload_real<Real>(d.wo_gg, s.wo_gg, st));
+  {
+    // wall weights regrouped [direction][chunk][entry][mcp] so one unit's entries are one contiguous copy
+    const int64_t n_wo = (int64_t)s.wo_wall.size();
+    std::vector<double> gg((size_t)n_wo * d.n_chunks * mcp, 0.0);
+    for (int q = 0; q < s.n_dir; ++q) {
+      const int64_t w0 = s.wo_off[q], nw = s.wo_off[q + 1] - w0;
+      for (int c = 0; c < d.n_chunks; ++c)
+        for (int64_t e = 0; e < nw; ++e)
+          for (int j = 0; j < mcp; ++j) {
+            const int m = c * mcp + j;
+            if (m < s.n_mfp)
+              gg[(size_t)(((w0 * d.n_chunks + (int64_t)c * nw) + e) * mcp + j)] = s.wo_gg[(size_t)(w0 + e) * s.m_pad + m];
+          }
+    }
+    OBTE_TRY(upload_real<Real>(d.wo_gg, gg, st));
+  }
   OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
   OBTE_TRY(upload_real<Real>(d.scoef, s.scoef, st));
   if (!s.hs.empty()) OBTE_TRY(upload(d.hs, s.hs, st));
@@ -637,11 +782,12 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
   p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;
+  p.emax = d.emax; p.unit_wo = d.unit_wo; p.pf_pad = d.pf_pad;
   p.rec = d.rec.as<int32_t>(); p.vals = d.vals.as<Real>();
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
+  p.kwo = d.kwo.as<int32_t>(); p.kpf = d.kpf.as<int32_t>(); p.pf = d.pf.as<int32_t>();
   p.x_base = plan->x_base_dev.as<int64_t>();
   p.wo_off = d.wo_off.as<int32_t>();
-  p.max_wo = s.max_wo;
   p.wo_wall = d.wo_wall.as<int32_t>();
   p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_gg = d.wo_gg.as<Real>();
   p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
