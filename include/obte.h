@@ -168,6 +168,28 @@ obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opts, const do
  */
 obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
                            int32_t with_source);
+/*
+ * The same sweep as obte_bte_sweep, with the same arguments and result, for
+ * callers that cannot allocate device memory when they sweep: a host
+ * framework that has reserved nearly all of the GPU's memory for its own pool
+ * (where cudaMalloc fails or forces that pool to give memory back), or a
+ * latency-bound loop where cudaMalloc / cudaFree would synchronise the device.
+ * This call allocates nothing: its scratch (the per-sweep values, n_dir x
+ * n_elems x 8 bytes in FP32 modes or x 16 in FP64, plus 288 bytes) lives in an
+ * 8 MiB array inside the library, which every GPU that loads the library holds
+ * until the process exits.  A larger problem is rejected with
+ * OBTE_ERR_UNSUPPORTED (use obte_bte_sweep).  The plan's device tables for the
+ * precision must already exist: building them allocates, so run obte_bte_sweep
+ * or obte_bte_solve once in that precision at set-up, or this returns
+ * OBTE_ERR_BAD_ARG.  The first call on a device looks up the array's device
+ * address (once per device); make that first call before any stream capture.
+ * All calls share the one array: calls whose GPU work overlaps (other threads,
+ * other streams, other plans) race on it and must be serialised by the caller.
+ * Each call synchronises the plan's stream before it returns.
+ * No counterpart in the reference (it has no device code).
+ */
+obte_status obte_bte_sweep_static(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
+                                  int32_t with_source);
 /* Sizes of the state vector pieces: n_elems, n_diffuse, n_x. */
 obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x);
 /*

@@ -97,6 +97,7 @@ SIGNATURES = [
     ("obte_bte_solve", C.c_int, [C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.POINTER(SolveInfo)]),
     ("obte_bte_sweep", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
+    ("obte_bte_sweep_static", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
     ("obte_bte_state_layout", C.c_int, [C.c_void_p, p_i64, p_i64, p_i64]),
     ("obte_bte_schedule", C.c_int, [C.c_void_p, C.c_int32, p_i64, p_i64, p_i64, p_i64]),
     ("obte_fourier_plan_create", C.c_int, [C.c_void_p, C.POINTER(FourierProblem), C.POINTER(C.c_void_p)]),

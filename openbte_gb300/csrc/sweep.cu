@@ -38,6 +38,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "internal.h"
 
@@ -848,3 +849,158 @@ obte_status check_device_error(obte_plan plan) {
 }
 
 }  // namespace obte
+
+// ---- sweep on library-owned static scratch ---------------------------------------------
+//
+// obte_bte_sweep keeps its per-sweep scratch (the (b, p) values the sweep kernel streams by
+// TMA, and the device error word) in buffers the plan allocates on first use.  Some callers
+// cannot allocate device memory when they sweep: a host framework that has reserved nearly
+// all of the GPU's memory for its own pool (cudaMalloc then fails or forces that pool to give
+// memory back), or a latency-bound loop in which cudaMalloc / cudaFree would synchronise the
+// device and stall work on other streams.  obte_bte_sweep_static runs the same two kernels
+// with that scratch in the fixed array below instead, and allocates nothing.
+//
+// The array is a file-scope __device__ variable: every GPU that loads this library holds
+// kStaticScratchBytes of it until the process exits.  Its name in host code is only a
+// host-side stand-in, so host code passes the kernels the device address that
+// cudaGetSymbolAddress returns, looked up once per device (with that device current) on
+// the first call on that device.  Layout: [0, 256) device error word, [256, ...) the values.
+// All calls share the array, and it keeps the previous call's contents; each call clears
+// the error word before its kernels run, and the values are written in full by
+// sweep_values_kernel before the sweep kernel reads them.
+namespace obte {
+
+static constexpr size_t kStaticScratchBytes = (size_t)8 << 20;
+static constexpr size_t kStaticValsOffset = 256;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_addr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of g_static_scratch on `device`, which must be the current device.
+static obte_status static_scratch_address(int device, void** out) {
+  if (device < 0 || device >= kMaxDevices) { set_error("device ordinal out of range"); return OBTE_ERR_BAD_ARG; }
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[device]) {
+    void* p = nullptr;
+    OBTE_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+    g_static_addr[device] = p;
+  }
+  *out = g_static_addr[device];
+  return OBTE_OK;
+}
+
+template <typename Real, int NF, int MCP>
+static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
+                                      bool with_src, Real* vals, int* err) {
+  const Schedule& s = plan->sched;
+  cudaStream_t st = plan->stream;
+  const int64_t total = (int64_t)s.n_dir * s.n;
+  const int vblocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)plan->ctx->num_sms * 8);
+  sweep_values_kernel<Real><<<vblocks, 256, 0, st>>>(
+      d.cellmap.as<int32_t>(), d.Pq.as<double>(), d.spec.as<int32_t>(), d.si.as<int32_t>(), d.sr.as<Real>(), u_in,
+      s.n, s.hs.empty() ? nullptr : d.hs.as<double>(), with_src ? 1 : 0, total, vals);
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  auto kern = bte_sweep_kernel<Real, NF, MCP, false>;
+  OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
+  SweepParams<Real> p;
+  p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
+  p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;
+  p.emax = d.emax; p.unit_wo = d.unit_wo; p.pf_pad = d.pf_pad;
+  p.rec = d.rec.as<int32_t>(); p.vals = vals;
+  p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
+  p.kwo = d.kwo.as<int32_t>(); p.kpf = d.kpf.as<int32_t>(); p.pf = d.pf.as<int32_t>();
+  p.x_base = plan->x_base_dev.as<int64_t>();
+  p.wo_off = d.wo_off.as<int32_t>();
+  p.wo_wall = d.wo_wall.as<int32_t>();
+  p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_gg = d.wo_gg.as<Real>();
+  p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
+  p.u_in = u_in; p.u_out = u_out; p.Jraw = nullptr; p.K = nullptr; p.S_out = nullptr;
+  p.err = err;
+  kern<<<s.n_dir * d.n_chunks, kUnit, d.smem, st>>>(p);
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  return OBTE_OK;
+}
+
+template <typename Real, int MCP>
+static obte_status launch_static_w(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
+                                   bool with_src, Real* vals, int* err) {
+  if (plan->sched.nf == 3) return launch_static_impl<Real, 3, MCP>(plan, d, u_in, u_out, with_src, vals, err);
+  return launch_static_impl<Real, 4, MCP>(plan, d, u_in, u_out, with_src, vals, err);
+}
+
+// Runs with the plan's device current; the caller restores its own.
+static obte_status sweep_static_on_device(obte_plan plan, bool fp32, const double* u_in, double* u_out,
+                                          bool with_src) {
+  const Schedule& s = plan->sched;
+  const DevSchedule& d = fp32 ? plan->d32 : plan->d64;
+  cudaStream_t st = plan->stream;
+  void* base = nullptr;
+  OBTE_TRY(static_scratch_address(plan->ctx->device, &base));
+  int* err = static_cast<int*>(base);
+  void* vals = static_cast<unsigned char*>(base) + kStaticValsOffset;
+  OBTE_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
+  obte_status rc = OBTE_ERR_UNSUPPORTED;
+#define OBTE_SW(R, M) \
+  case M: rc = launch_static_w<R, M>(plan, d, u_in, u_out, with_src, static_cast<R*>(vals), err); break
+  if (fp32) {
+    switch (d.mcp) { OBTE_SW(float, 4); OBTE_SW(float, 8); OBTE_SW(float, 12); OBTE_SW(float, 16); OBTE_SW(float, 24); }
+  } else {
+    switch (d.mcp) { OBTE_SW(double, 4); OBTE_SW(double, 8); OBTE_SW(double, 12); OBTE_SW(double, 16); }
+  }
+#undef OBTE_SW
+  if (rc == OBTE_ERR_UNSUPPORTED) set_error("no compiled sweep kernel for this chunk width");
+  if (rc != OBTE_OK) return rc;
+  int h = 0;
+  OBTE_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  OBTE_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("a device-side wait timed out in the sweep kernel");
+    return OBTE_ERR_DEVICE_TIMEOUT;
+  }
+  return OBTE_OK;
+}
+
+}  // namespace obte
+
+using namespace obte;
+
+extern "C" obte_status obte_bte_sweep_static(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
+                                             int32_t with_source) {
+  if (!plan || !u_in || !u_out) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  if (!plan->ctx) { set_error("host-only plan cannot sweep"); return OBTE_ERR_BAD_ARG; }
+  if (precision != OBTE_FP64 && precision != OBTE_FP32 && precision != OBTE_FP32_REFINE) {
+    set_error("bad precision"); return OBTE_ERR_BAD_ARG;
+  }
+  const Schedule& s = plan->sched;
+  const bool fp32 = precision != OBTE_FP64;
+  const size_t need = kStaticValsOffset + (size_t)s.n_dir * (size_t)s.n * 2 * (fp32 ? sizeof(float) : sizeof(double)) + 32;
+  if (need > kStaticScratchBytes) {
+    set_error("obte_bte_sweep_static: this problem needs " + std::to_string(need) + " bytes of scratch (n_dir x n_elems x " +
+              std::to_string(fp32 ? 8 : 16) + " + 288), more than the " + std::to_string(kStaticScratchBytes) +
+              " bytes of static scratch the library holds; use obte_bte_sweep");
+    return OBTE_ERR_UNSUPPORTED;
+  }
+  if (s.ds > 3) { set_error("sigma with more than 3 components"); return OBTE_ERR_UNSUPPORTED; }
+  if (s.nf > 4) { set_error("elements with more than 4 sides are not supported"); return OBTE_ERR_UNSUPPORTED; }
+  if (!(fp32 ? plan->d32.ready : plan->d64.ready)) {
+    set_error("obte_bte_sweep_static: the plan's device tables for this precision are not built yet; building them "
+              "allocates, so run obte_bte_sweep or obte_bte_solve once in this precision at set-up");
+    return OBTE_ERR_BAD_ARG;
+  }
+  int prev = -1;
+  OBTE_CUDA(cudaGetDevice(&prev));
+  if (prev != plan->ctx->device) OBTE_CUDA(cudaSetDevice(plan->ctx->device));
+  const obte_status rc = sweep_static_on_device(plan, fp32, u_in, u_out, with_source != 0);
+  if (prev != plan->ctx->device) {
+    const cudaError_t e = cudaSetDevice(prev);
+    if (rc == OBTE_OK && e != cudaSuccess) return cuda_fail(e, "cudaSetDevice", __FILE__, __LINE__);
+  }
+  return rc;
+}
