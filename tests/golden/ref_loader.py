@@ -162,3 +162,102 @@ def load(in_process: bool = True):
                                material=material, utils=utils)
     _LOADED["ns"] = ns
     return ns
+
+
+# ---- the inverse-design modules (openbte/inverse/bte.py, openbte/inverse/matinverse.py) ----------
+#
+# They use jax only as an array library (jnp.einsum / zeros / power, functional ``.at[].add``) and
+# for ``jit`` / ``custom_vjp`` decorators; the gradient itself is written out by hand
+# (openbte/inverse/bte.py:27-95).  jax is absent here, so ``jax.numpy`` is replaced by a numpy
+# module whose arrays support ``.at[idx].add(v)`` (np.add.at on a copy) and the decorators become
+# identities.  The arithmetic is then the reference's own, in float64 (it enables jax x64,
+# openbte/inverse/matinverse.py:33).
+
+class _JArr(np.ndarray):
+    @property
+    def at(self):
+        return _At(self)
+
+
+class _At:
+    def __init__(self, a):
+        self.a = a
+
+    def __getitem__(self, idx):
+        return _AtIdx(self.a, idx)
+
+
+class _AtIdx:
+    def __init__(self, a, idx):
+        self.a, self.idx = a, idx
+
+    def add(self, v):
+        out = np.array(self.a, dtype=np.result_type(self.a, np.asarray(v)), copy=True)
+        np.add.at(out, self.idx, np.asarray(v))
+        return out.view(_JArr)
+
+    def set(self, v):
+        out = np.array(self.a, copy=True)
+        out[self.idx] = np.asarray(v)
+        return out.view(_JArr)
+
+
+def _w(x):
+    return np.asarray(x).view(_JArr)
+
+
+def _numpy_jax():
+    jnp = types.ModuleType("jax.numpy")
+    for name in ["array", "zeros", "ones", "einsum", "power", "multiply", "sqrt", "concatenate", "fliplr",
+                 "zeros_like", "ones_like", "arange", "exp", "sum", "linalg"]:
+        f = getattr(np, name)
+        if callable(f):
+            jnp.__dict__[name] = (lambda f: (lambda *a, **k: _w(f(*a, **k))))(f)
+        else:
+            jnp.__dict__[name] = f
+    jnp.allclose = np.allclose
+    jnp.dot = lambda *a, **k: _w(np.dot(*a, **k))
+    jnp.float64 = np.float64
+    jax = types.ModuleType("jax")
+    jax.numpy = jnp
+    jax.jit = lambda f=None, **k: f if f is not None else (lambda g: g)
+    jax.custom_vjp = lambda f: f
+    jax.value_and_grad = lambda f, **k: f
+    jax.config = types.SimpleNamespace(update=lambda *a, **k: None)
+    jsig = types.ModuleType("jax.scipy.signal")
+    jsig.convolve2d = None
+    jsc = types.ModuleType("jax.scipy")
+    jsc.signal = jsig
+    jax.scipy = jsc
+    return {"jax": jax, "jax.numpy": jnp, "jax.scipy": jsc, "jax.scipy.signal": jsig}
+
+
+def load_inverse():
+    """Return the reference's inverse-design modules (bte, matinverse) on the numpy jax stand-in."""
+    if "inv" in _LOADED:
+        return _LOADED["inv"]
+    load()
+    saved = {k: sys.modules.get(k) for k in ["jax", "jax.numpy", "jax.scipy", "jax.scipy.signal"]}
+    sys.modules.update(_numpy_jax())
+    mpl = sys.modules["matplotlib"]
+    mpl.interactive = lambda *a, **k: None
+    mpl.rcParams = {}
+    sys.modules["matplotlib.pylab"].__dict__.setdefault("figure", _Anything())
+    _stub("nlopt")
+    pkg = sys.modules["openbte"]
+    inv = types.ModuleType("openbte.inverse")
+    inv.__path__ = [os.path.join(REF_ROOT, "openbte", "inverse")]
+    sys.modules["openbte.inverse"] = inv
+    pkg.inverse = inv
+    try:
+        mi = importlib.import_module("openbte.inverse.matinverse")
+        ib = importlib.import_module("openbte.inverse.bte")
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    ns = types.SimpleNamespace(bte=ib, matinverse=mi, asarray=_w)
+    _LOADED["inv"] = ns
+    return ns
