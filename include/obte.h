@@ -80,6 +80,13 @@ typedef struct {
   double normalization;           /* EffectiveThermalConductivity.normalization   */
   int32_t is_nanowire;            /* BoundaryConditions.is_nanowire               */
   const double* heat_source;      /* [n_elems] or NULL (HeatSource data)          */
+  /* Transmission-interface model (openbte/inverse/bte.py:145-163): fraction t in (0, 1] of the
+   * inflow across each internal side that comes from the neighbour; NULL = 1 everywhere.  With
+   * reflect_internal = 1 the rest, 1 - t, is the element's own outgoing flux at that side,
+   * diffusely re-emitted (one reflected-temperature unknown per directed internal side, placed
+   * after the diffuse walls in the T_B part of the state).                                     */
+  const double* side_transmission;
+  int32_t reflect_internal;
 } obte_problem;
 
 /* Ordinate data (openbte/objects.py:500-509). All host arrays. */
@@ -190,6 +197,20 @@ obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const double* u_in
  */
 obte_status obte_bte_sweep_static(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
                                   int32_t with_source);
+
+/*
+ * Inverse design: dkappa_eff/dt_s for every side of a plan created with side_transmission
+ * (replaces compute_kappa_and_gradient, openbte/inverse/bte.py:27-95, for MFP-resolved
+ * materials).  Solves like obte_bte_solve (same opts and dT0), keeps the per-ordinate
+ * temperatures of the final sweep and evaluates the adjoint from them: the adjoint of
+ * direction q is the forward solution of its reverse, so no second solve runs.
+ *   grad_t  device [n_sides]; 0 on sides that are not internal.
+ * Needs a direction set closed under reversal, sigma = a t_coeff mfp s (isotropic), the
+ * periodic jump only on the contact sides, and no isothermal, heat-source or nanowire terms
+ * (else OBTE_ERR_UNSUPPORTED).  info->kappa_eff is kappa_eff.
+ */
+obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_opts* opts, const double* dT0,
+                                    double* grad_t, obte_solve_info* info);
 /* Sizes of the state vector pieces: n_elems, n_diffuse, n_x. */
 obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x);
 /*

@@ -36,7 +36,7 @@ class Problem(C.Structure):
         ("n_mixed", C.c_int64), ("mixed_sides", p_i64), ("mixed_value", p_f64),
         ("contact_kind", C.c_int32), ("n_contact", C.c_int64), ("contact_sides", p_i64),
         ("contact_alpha", C.c_double), ("normalization", C.c_double), ("is_nanowire", C.c_int32),
-        ("heat_source", p_f64),
+        ("heat_source", p_f64), ("side_transmission", p_f64), ("reflect_internal", C.c_int32),
     ]
 
 
@@ -98,6 +98,8 @@ SIGNATURES = [
                                  C.c_void_p, C.POINTER(SolveInfo)]),
     ("obte_bte_sweep", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
     ("obte_bte_sweep_static", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
+    ("obte_bte_kappa_gradient", C.c_int, [C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p,
+                                          C.POINTER(SolveInfo)]),
     ("obte_bte_state_layout", C.c_int, [C.c_void_p, p_i64, p_i64, p_i64]),
     ("obte_bte_schedule", C.c_int, [C.c_void_p, C.c_int32, p_i64, p_i64, p_i64, p_i64]),
     ("obte_fourier_plan_create", C.c_int, [C.c_void_p, C.POINTER(FourierProblem), C.POINTER(C.c_void_p)]),

@@ -48,6 +48,7 @@ template obte_status upload<int32_t>(DevBuf&, const std::vector<int32_t>&, cudaS
 template obte_status upload<int64_t>(DevBuf&, const std::vector<int64_t>&, cudaStream_t);
 template obte_status upload<double>(DevBuf&, const std::vector<double>&, cudaStream_t);
 template obte_status upload<float>(DevBuf&, const std::vector<float>&, cudaStream_t);
+template obte_status upload<int8_t>(DevBuf&, const std::vector<int8_t>&, cudaStream_t);
 
 }  // namespace obte
 

@@ -112,6 +112,18 @@ struct Schedule {
   // offset weights (energy-conservation left null vector)
   std::vector<double> ell_T, ell_B;
   std::vector<int32_t> diffuse_cell;  // [nd] element of each wall side
+  // transmission-interface data for dkappa/dt (present when side transmissions were given)
+  bool tim = false;
+  int64_t n_sides = 0;
+  std::vector<double> dirs;                  // [n_dir * dim] unit directions
+  std::vector<int32_t> tim_side;             // [ni] side id of internal side k
+  std::vector<int32_t> tim_e1, tim_e2;       // [ni] its elements (area vector points from e1)
+  std::vector<int32_t> tim_w1, tim_w2;       // [ni] reflecting wall of the e1 / e2 directed face (-1: none)
+  std::vector<double> tim_na;                // [ni * dim] area vector
+  std::vector<double> tim_jump;              // [ni] periodic jump (0 off periodic sides)
+  std::vector<char> tim_contact;             // [ni] 1 = contact side
+  double contact_alpha = 0, normalization = 0;
+  bool extra_sources = false;                // isothermal walls, heat source or nanowire terms
 };
 
 obte_status build_schedule(const obte_problem* prob, const obte_material* mat, Schedule& s);
@@ -141,6 +153,14 @@ struct SolveWork {
   int nb = 1;
   DevBuf u, Fu, r, V, w, tmp, partial, hdev, sdev, Jraw, Kraw, Sraw, delta;
 };
+
+// Transmission-interface gradient: per internal side tables, ordinate tables and the final-pass
+// per-ordinate temperatures (built on the first gradient call of a plan).
+struct TimDevice {
+  bool ready = false;
+  double kfac = 0;      // adjoint scale nrm * a / jump (sigma = a tau L s)
+  DevBuf side, e1, e2, w1, w2, na, jump, contact, dirs, tl, sig, refl, xs, K;
+};
 }  // namespace obte
 
 struct obte_plan_s {
@@ -157,6 +177,8 @@ struct obte_plan_s {
   int64_t nx = 0;                   // periodic-inflow unknowns (source cells x n_mfp)
   int64_t nu = 0;                   // state length
   bool has_solution = false;        // work->u holds the last converged state
+  float* xstore = nullptr;          // set during a gradient solve: final-pass per-ordinate temperatures
+  std::unique_ptr<obte::TimDevice> tim;   // transmission-interface gradient tables and scratch
 };
 
 namespace obte {

@@ -71,9 +71,19 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     is_per[pb->periodic_sides[k]] = 1;
   }
   const int64_t nfd = 2 * ni;
+  // side transmission (transmission-interface model); 1 = plain internal side
+  std::vector<double> t_side(ns, 1.0);
+  if (pb->side_transmission) {
+    for (int64_t k = 0; k < ns; ++k) {
+      const double t = pb->side_transmission[k];
+      if (!(t > 0 && t <= 1)) { set_error("side transmission outside (0, 1]"); return OBTE_ERR_BAD_ARG; }
+      t_side[k] = t;
+    }
+  }
+  const bool reflect = pb->reflect_internal != 0;
   std::vector<int32_t> f_row(nfd), f_nb(nfd);
   std::vector<char> f_cut(nfd);
-  std::vector<double> f_k(nfd * dim);
+  std::vector<double> f_k(nfd * dim), f_t(nfd);
   for (int64_t t = 0; t < ni; ++t) {
     const int64_t sd = pb->internal[t];
     if (!in_range(sd, ns)) { set_error("internal side out of range"); return OBTE_ERR_BAD_ARG; }
@@ -81,23 +91,42 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     if (i == j) { set_error("internal side with a single element"); return OBTE_ERR_BAD_ARG; }
     f_row[t] = (int32_t)i; f_nb[t] = (int32_t)j; f_cut[t] = is_per[sd];
     f_row[ni + t] = (int32_t)j; f_nb[ni + t] = (int32_t)i; f_cut[ni + t] = is_per[sd];
+    f_t[t] = f_t[ni + t] = t_side[sd];
     for (int d = 0; d < dim; ++d) {
       f_k[t * dim + d] = na[sd * dim + d] / vol[i];
       f_k[(ni + t) * dim + d] = -na[sd * dim + d] / vol[j];
     }
   }
-  // ---- walls ----
-  const int64_t nd = pb->n_diffuse;
+  // ---- walls: diffuse walls, then (reflect) one reflecting wall per directed internal face ----
+  //   w_db = area vector / volume of the wall's element; w_na = area vector; w_scale scales the
+  //   inflow (1 for diffuse walls, 1 - t for reflection); only diffuse walls take outflow into D
+  const int64_t nd0 = pb->n_diffuse;
+  const int64_t nd = nd0 + (reflect ? nfd : 0);
   s.nd = nd;
   std::vector<int32_t> w_cell(nd);
-  std::vector<double> w_db(nd * dim);
-  for (int64_t w = 0; w < nd; ++w) {
+  std::vector<double> w_db(nd * dim), w_na(nd * dim), w_scale(nd, 1.0);
+  for (int64_t w = 0; w < nd0; ++w) {
     const int64_t sd = pb->diffuse_sides[w];
     if (!in_range(sd, ns)) { set_error("diffuse side out of range"); return OBTE_ERR_BAD_ARG; }
     const int64_t i = sem[2 * sd];
     w_cell[w] = (int32_t)i;
-    for (int d = 0; d < dim; ++d) w_db[w * dim + d] = na[sd * dim + d] / vol[i];
+    for (int d = 0; d < dim; ++d) {
+      w_db[w * dim + d] = na[sd * dim + d] / vol[i];
+      w_na[w * dim + d] = na[sd * dim + d];
+    }
   }
+  if (reflect)
+    for (int64_t f = 0; f < nfd; ++f) {
+      const int64_t w = nd0 + f;
+      const int64_t sd = pb->internal[f % ni];
+      const double sg = f < ni ? 1.0 : -1.0;
+      w_cell[w] = f_row[f];
+      w_scale[w] = 1.0 - f_t[f];
+      for (int d = 0; d < dim; ++d) {
+        w_db[w * dim + d] = f_k[f * dim + d];
+        w_na[w * dim + d] = sg * na[sd * dim + d];
+      }
+    }
   s.diffuse_cell = w_cell;
   // re-emission weights GG (bte.py:73-78): -GG[m,q,w] = Gbp / (-sum_mq Gbm)
   std::vector<double> gbm_sum(nd, 0.0);
@@ -115,7 +144,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   // ---- contact (bte.py:132-158) ----
   std::vector<int32_t> c_e1, c_e2;
   std::vector<double> c_na;  // [nc * dim]
-  std::vector<double> c_area;
+  std::vector<double> c_area, c_t;   // c_t: transmission of the contact side (heat flux across it scales by t)
   const int ck = pb->contact_kind;
   const double nrm = pb->normalization;
   if (ck == OBTE_CONTACT_PERIODIC || ck == OBTE_CONTACT_MIXED) {
@@ -124,6 +153,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       if (!in_range(sd, ns)) { set_error("contact side out of range"); return OBTE_ERR_BAD_ARG; }
       c_e1.push_back((int32_t)sem[2 * sd]);
       c_e2.push_back(ck == OBTE_CONTACT_PERIODIC ? (int32_t)sem[2 * sd + 1] : -1);
+      c_t.push_back(t_side[sd]);
       double a2 = 0;
       for (int d = 0; d < dim; ++d) { c_na.push_back(na[sd * dim + d]); a2 += na[sd * dim + d] * na[sd * dim + d]; }
       c_area.push_back(std::sqrt(a2));
@@ -172,17 +202,46 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.ell_T.assign(vol, vol + n);
   s.ell_B.assign(nd, 0.0);
   for (int64_t w = 0; w < nd; ++w) {
-    const int64_t sd = pb->diffuse_sides[w];
     double acc = 0;
     for (int q = 0; q < n_dir; ++q) {
       double sn = 0;
-      for (int d = 0; d < dim; ++d) sn += mt->vmfp[(int64_t)q * dd + d] * na[sd * dim + d];
+      for (int d = 0; d < dim; ++d) sn += mt->vmfp[(int64_t)q * dd + d] * w_na[w * dim + d];
       if (sn < 0)
         for (int m = 0; m < n_mfp; ++m) acc += mt->t_coeff[(int64_t)m * n_dir + q] * mt->mfps[m] * (-sn);
     }
-    s.ell_B[w] = acc;
+    s.ell_B[w] = acc * w_scale[w];
   }
 
+
+  // transmission-interface tables for the gradient dkappa/dt
+  s.n_sides = ns;
+  s.dirs.assign((size_t)n_dir * dim, 0.0);
+  for (int q = 0; q < n_dir; ++q)
+    for (int d = 0; d < dim; ++d) s.dirs[(size_t)q * dim + d] = mt->vmfp[(int64_t)q * dd + d];
+  s.tim = pb->side_transmission != nullptr;
+  s.contact_alpha = pb->contact_alpha;
+  s.extra_sources = pb->n_mixed > 0 || pb->is_nanowire || pb->heat_source != nullptr;
+  s.normalization = nrm;
+  if (s.tim) {
+    std::vector<double> jump_of(ns, 0.0);
+    for (int64_t k = 0; k < pb->n_periodic; ++k) jump_of[pb->periodic_sides[k]] = pb->periodic_jump[k];
+    std::vector<char> is_contact(ns, 0);
+    if (ck == OBTE_CONTACT_PERIODIC)
+      for (int64_t k = 0; k < pb->n_contact; ++k) is_contact[pb->contact_sides[k]] = 1;
+    s.tim_side.resize(ni); s.tim_e1.resize(ni); s.tim_e2.resize(ni); s.tim_w1.resize(ni); s.tim_w2.resize(ni);
+    s.tim_na.resize((size_t)ni * dim); s.tim_jump.resize(ni); s.tim_contact.resize(ni);
+    for (int64_t t = 0; t < ni; ++t) {
+      const int64_t sd = pb->internal[t];
+      s.tim_side[t] = (int32_t)sd;
+      s.tim_e1[t] = f_row[t];
+      s.tim_e2[t] = f_nb[t];
+      s.tim_w1[t] = reflect ? (int32_t)(nd0 + t) : -1;
+      s.tim_w2[t] = reflect ? (int32_t)(nd0 + ni + t) : -1;
+      for (int d = 0; d < dim; ++d) s.tim_na[(size_t)t * dim + d] = na[sd * dim + d];
+      s.tim_jump[t] = is_per[sd] ? jump_of[sd] : 0.0;
+      s.tim_contact[t] = is_contact[sd];
+    }
+  }
 
   // mixed sides are validated up front (the per-direction workers do not report errors for them)
   for (int64_t k = 0; k < pb->n_mixed; ++k)
@@ -225,8 +284,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       g[f] = v;
       if (v > 0) D[f_row[f]] += v;
     }
-    // diffuse walls (bte.py:80-84)
-    for (int64_t w = 0; w < nd; ++w) {
+    // diffuse walls (bte.py:80-84); reflecting walls sit on internal faces, whose outflow is in D already
+    for (int64_t w = 0; w < nd0; ++w) {
       double v = 0;
       for (int d = 0; d < dim; ++d) v += sq[d] * w_db[w * dim + d];
       if (v > 0) D[w_cell[w]] += v;
@@ -250,8 +309,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         v1 += sq[d] * na[sd * dim + d] / vol[i];
         v2 += sq[d] * (-na[sd * dim + d]) / vol[j];
       }
-      P[i] += -std::min(v1, 0.0) * jump;
-      P[j] += std::min(v2, 0.0) * jump;
+      P[i] += -std::min(v1, 0.0) * jump * t_side[sd];
+      P[j] += std::min(v2, 0.0) * jump * t_side[sd];
     }
     if (pb->is_nanowire)
       for (int64_t e = 0; e < n; ++e) P[e] += -sq[2];
@@ -368,7 +427,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         if (k >= nf) { o.st = OBTE_ERR_BAD_ARG; o.err = "more inflow faces than element sides"; return; }
         if (f_cut[f]) s.in_idx[it * nf + k] = pack_item(ITEM_PERIODIC, src_idx[f_nb[f]]);
         else s.in_idx[it * nf + k] = pack_item(ITEM_CELL, slot_of[f_nb[f]]);
-        s.in_coef[it * nf + k] = g[f];
+        s.in_coef[it * nf + k] = g[f] * f_t[f];
         ++k;
       }
       for (int32_t w : wall_in[e]) {
@@ -376,7 +435,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         double v = 0;
         for (int d = 0; d < dim; ++d) v += sq[d] * w_db[(int64_t)w * dim + d];
         s.in_idx[it * nf + k] = pack_item(ITEM_WALL, w);
-        s.in_coef[it * nf + k] = v;
+        s.in_coef[it * nf + k] = v * w_scale[w];
         ++k;
       }
       auto si = src_idx.find(e);
@@ -407,7 +466,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
             } else {
               for (auto& pr : co->second) {
                 const double sn = sigma_n(m, q, pr.first);
-                kc += pr.second == 1 ? std::max(sn, 0.0) : std::min(sn, 0.0);
+                kc += (pr.second == 1 ? std::max(sn, 0.0) : std::min(sn, 0.0)) * c_t[pr.first];
               }
             }
           }
@@ -428,7 +487,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     if (ck == OBTE_CONTACT_PERIODIC || ck == OBTE_CONTACT_MIXED)
       for (int m = 0; m < n_mfp; ++m) {
         double acc = 0;
-        for (int64_t k = 0; k < nc; ++k) acc += std::min(sigma_n(m, q, k), 0.0);
+        for (int64_t k = 0; k < nc; ++k) acc += std::min(sigma_n(m, q, k), 0.0) * c_t[k];
         s.kconst[(size_t)m * n_dir + q] = pb->contact_alpha * acc * nrm;
       }
   };

@@ -335,6 +335,7 @@ struct SweepParams {
   double* __restrict__ K;
   double* __restrict__ S_out;
   int* __restrict__ err;
+  float* __restrict__ Xs;   // final pass only: per-ordinate temperatures [n_dir][n][n_mfp], or null
 };
 
 template <typename Real>
@@ -550,6 +551,7 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
             const Real T = (b + lam[mm] * (pw - s)) * recip(Real(1) + lam[mm] * D);
             ring[(size_t)mm * rows + so] = T;
             dacc += tt[mm] * T;
+            if (FINAL && p.Xs != nullptr && mm < mc) p.Xs[((int64_t)q * p.n + c) * p.n_mfp + m0 + mm] = (float)T;
             if (FINAL) {
               j0 += s_sig[mm * 3] * T;
               j1 += s_sig[mm * 3 + 1] * T;
@@ -794,6 +796,7 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
   p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S_out = S;
   p.err = plan->err.as<int>();
+  p.Xs = FINAL ? plan->xstore : nullptr;
   const int grid = s.n_dir * d.n_chunks;
   kern<<<grid, kUnit, d.smem, st>>>(p);
   count_launch();
@@ -921,6 +924,7 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
   p.u_in = u_in; p.u_out = u_out; p.Jraw = nullptr; p.K = nullptr; p.S_out = nullptr;
   p.err = err;
+  p.Xs = nullptr;
   kern<<<s.n_dir * d.n_chunks, kUnit, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());

@@ -25,7 +25,7 @@ kappa / kappa_bulk equals the reference's kappa (openbte/inverse/bte.py:27-40, d
 
 Gradients: the explicit adjoint (A^T lam = dkappa/dX, dkappa/dt = d_t kappa - lam . d_t r), and the
 same through the reflection identity used on the GPU: with weights V tau the operator is
-symmetric up to reversing every direction, so lam_mq(c) = (nrm alpha a / jump) V_c tau_mq X_m,qbar(c)
+symmetric up to reversing every direction, so lam_mq(c) = (nrm a / jump) V_c tau_mq X_m,qbar(c)
 with sigma = a tau L s (the reference's G = -T[reflection], openbte/inverse/bte.py:33).
 """
 from __future__ import annotations
@@ -232,7 +232,7 @@ def flux_scale(mat):
 
 
 def gradient_reflection(X, grid, t, mat, nrm=-1.0, alpha=1.0, jump=1.0):
-    """dkappa/dt per side through lam_mq(c) = (nrm alpha a / jump) V_c tau_mq X_m,qbar(c) (a = flux_scale):
+    """dkappa/dt per side through lam_mq(c) = (nrm a / jump) V_c tau_mq X_m,qbar(c) (a = flux_scale):
     per directed face E_f = sum_{q in(f)} (s_q . n_f) sum_m tau_mq L_m X_m,qbar(c) (X_mq(j) + J_f - R_f)."""
     c, j, nv, side, jsign = _faces(grid)
     s = mat["dirs"]
@@ -247,7 +247,7 @@ def gradient_reflection(X, grid, t, mat, nrm=-1.0, alpha=1.0, jump=1.0):
                        (X[:, qs, j[fi]] + jump * jsign[fi] - R[fi]))
     G = np.zeros(len(grid["e1"]))
     np.add.at(G, side, E)
-    return dkappa_dt_explicit(X, grid, t, mat, nrm, alpha) - (nrm * alpha * flux_scale(mat) / jump) * G
+    return dkappa_dt_explicit(X, grid, t, mat, nrm, alpha) - (nrm * flux_scale(mat) / jump) * G
 
 
 def kappa_and_gradient(rho, grid, mat, nrm=-1.0, method="reflection"):
