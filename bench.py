@@ -35,6 +35,8 @@ WORKLOADS = {
     "c1_60k_100x96": (60000, 100, 96, 0.25, "square", 1),
     "c0_2k_30x48": (2000, 30, 48, 0.25, "square", 1),
     "c2_100k_30x16x32": (100000, 30, (16, 32), 0.10, "sphere", 1),
+    # inverse design: pixels per side, n_mfp, n_dir, density-field seed
+    "c4_inverse_128x50x64": (128, 50, 64, None, "pixels", 0),
 }
 L2_BYTES = 129 * 1024 * 1024
 
@@ -229,9 +231,107 @@ def cpu_baseline(geo, mat, bcs, ek, budget_s=20.0, seed=0):
             "seconds_per_solve": t_solve}
 
 
+def density_field(n, seed):
+    """Seeded smoothed Gaussian random field on an n x n periodic grid, mapped to [0, 1] (pixel order i*n + j)."""
+    rng = np.random.default_rng(seed)
+    z = rng.standard_normal((n, n))
+    k = np.fft.fftfreq(n)
+    kk = k[:, None] ** 2 + k[None, :] ** 2
+    z = np.real(np.fft.ifft2(np.fft.fft2(z) * np.exp(-kk * (n / 8.0) ** 2)))
+    return ((z - z.min()) / (z.max() - z.min())).reshape(-1)
+
+
+def cpu_baseline_inverse(n_full, n_mfp_full, n_dir_full, budget_s=20.0):
+    """The oracle's TIM solve + adjoint gradient (sparse direct solve, one core) on small seeded pixel
+    grids of the same model, extrapolated linearly in unknowns to the full problem."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import tim_oracle
+    from openbte_gb300.material import lognormal_kappa
+    n, nm, nq = 8, 4, 8
+    mfps = np.logspace(0, 4, nm)
+    mat = tim_oracle.material(mfps, lognormal_kappa(mfps), nq)
+    grid = tim_oracle.pixel_grid(n, 100.0)
+    rho = density_field(n, 1)
+    t0, k = time.time(), 0
+    while k < 1 or (time.time() - t0 < budget_s / 2 and k < 5):
+        tim_oracle.kappa_and_gradient(rho, grid, mat, method="adjoint")
+        k += 1
+    per = (time.time() - t0) / k
+    scale = (n_full ** 2 * n_mfp_full * n_dir_full) / (n * n * nm * nq)
+    return {"value": 1.0 / (per * scale), "unit": "gradient evals/s", "cores": 1, "kind": "port",
+            "sample": f"{n}x{n} pixels, {nm} MFPs x {nq} directions (oracle sparse direct solve + explicit "
+                      f"adjoint, {per:.2f} s each), extrapolated linearly in unknowns by {scale:.0f}x"}
+
+
+def run_inverse(args, dev):
+    """Config 4: kappa_eff and dkappa/drho of a 128^2 pixel cell (50 MFPs x 64 directions) per step."""
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.inverse import IsotropicMaterial, PixelSolver
+    n, n_mfp, n_dir, _, _, seed = WORKLOADS[args.workload]
+    lib = _lib.load()
+    rho = density_field(n, seed)
+    mat = IsotropicMaterial.lognormal(n_mfp, n_dir)
+    solver = PixelSolver(n, mat, size=100.0, precision=args.precision, rtol=1e-8, restart=100)
+    ref = PixelSolver(n, mat, size=100.0, precision="fp64", rtol=1e-10, restart=100)
+    kap64, _ = ref.kappa_and_gradient(rho)
+    for _ in range(args.warmup):
+        solver.kappa_and_gradient(rho)
+    torch.cuda.synchronize()
+    l0 = lib.obte_launch_count()
+    lat, kaps = [], []
+    with Clocks(dev.index or 0) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            k, g = solver.kappa_and_gradient(rho)      # host rho in; kappa and the gradient back on the host
+            gh = g.cpu().numpy()
+            lat.append(time.perf_counter() - t0)
+            kaps.append(k)
+    launches = (lib.obte_launch_count() - l0) / args.steps
+    info = solver.last_info
+    t = float(np.median(lat))
+    line = {
+        "metric": "inverse-design gradient evals/s (kappa_eff + dkappa/drho over all pixels, FP32+refine)",
+        "value": 1.0 / t, "unit": "gradient evals/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded smoothed Gaussian random field)",
+        "config": {"workload": args.workload, "pixels": n * n, "n_mfp": n_mfp, "n_dir": n_dir,
+                   "unknowns_per_sweep": n * n * n_mfp * n_dir, "precision": args.precision, "rtol": 1e-8,
+                   "l2": "inputs and per-ordinate field (210 MB) larger than L2", "parallelism": "single"},
+        "kappa_eff": kaps[-1], "kappa_fp64": kap64, "kappa_rel_err_vs_fp64": abs(kaps[-1] - kap64) / abs(kap64),
+        "sweeps_per_eval": info.n_sweeps, "fp64_sweeps_per_eval": info.n_sweeps_fp64,
+        "gradient_abs_max": float(np.abs(gh).max()),
+        "e2e": {"value": 1.0 / t, "unit": "gradient evals/s",
+                "h2d_bytes_per_step": int(n * n * 8 + solver.last_upload_bytes),
+                "d2h_bytes_per_step": int(n * n * 8 + 2 * n * n * 8)},
+        "gpu_launches": int(round(launches)),
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_inverse(n, n_mfp, n_dir)
+    print(json.dumps(line))
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.workload.startswith("c4_"):
+        n, n_mfp, n_dir = WORKLOADS[args.workload][:3]
+        t0 = time.time()
+        cbs = [cpu_baseline_inverse(n, n_mfp, n_dir, budget_s=max(2.0, 20.0 / max(1, args.steps + args.warmup)))
+               for _ in range(args.warmup + args.steps)]
+        v = float(np.median([c["value"] for c in cbs[args.warmup:]]))
+        print(json.dumps({"impl": "reference", "metric": "inverse-design gradient evals/s (kappa_eff + dkappa/drho "
+                          "over all pixels, FP32+refine)", "value": v, "unit": "gradient evals/s", "n_gpus": 0,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": {"workload": args.workload},
+                          "cpu_baseline": {"value": v, "unit": "gradient evals/s", "cores": 1, "kind": "port",
+                                           "sample": cbs[-1]["sample"]},
+                          "e2e": {"value": v, "unit": "gradient evals/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}, "wall_s": time.time() - t0}))
         return
     geo, mat, bcs, ek = problem(args.workload)
     t0 = time.time()
@@ -284,6 +384,12 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload.startswith("c4_"):
+        if rank == 0:
+            run_inverse(args, dev)
+        if world > 1:
+            dist.destroy_process_group()
+        return
 
     from openbte_gb300 import _lib
     from openbte_gb300.bte import BTE_RTA, solve_plan
@@ -312,7 +418,7 @@ def main():
             ev[1].synchronize()
             ms[prec] = ev[0].elapsed_time(ev[1]) / max(1, args.profile_sweeps - args.profile_sweeps // 2)
         print(json.dumps({"profile_sweeps": args.profile_sweeps, "workload": args.workload,
-                          "ms_per_sweep": ms, "mcp_env": os.environ.get("OBTE_SWEEP_MCP")}))
+                          "ms_per_sweep": ms, "group_env": os.environ.get("OBTE_SWEEP_G")}))
         return
     dT0 = torch.zeros(geo.n_elems, dtype=torch.float64, device=dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)

@@ -158,8 +158,7 @@ extern "C" obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision
     b += (s.cell.size() + s.slot.size() + s.xk.size() + s.wout.size() + s.contact.size() + s.in_idx.size() +
           s.lev_ptr.size() + s.wo_wall.size()) * 4;
     b += (s.in_coef.size() + s.D.size() + s.P.size() + s.mfp.size() + s.tco.size() + s.sig.size() +
-          s.wo_gg.size() + s.kcoef.size() + s.scoef.size() + s.hs.size()) * rb;
-    b += s.wo_wall.size() * 24 * rb;              // wall weights regrouped by chunk (padding to the chunk width)
+          s.wo_wall.size() * 4 + s.kcoef.size() + s.scoef.size() + s.hs.size()) * rb;
     b += (s.lev_ptr.size() + s.in_idx.size()) * 8; // unit tables and periodic prefetch lists (bound)
     return (int64_t)b;
   };

@@ -4,7 +4,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <algorithm>
 #include <memory>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -30,6 +35,43 @@ obte_status cuda_fail(cudaError_t e, const char* what, const char* file, int lin
 
 // Count of kernel launches issued by this library (instrumentation for the bench).
 void count_launch(int n = 1);
+
+// Host worker count: OBTE_HOST_THREADS, else the hardware concurrency (at most 32).
+inline int host_threads() {
+  int t = (int)std::thread::hardware_concurrency();
+  if (const char* env = std::getenv("OBTE_HOST_THREADS")) t = std::atoi(env);
+  return std::max(1, std::min(t, 32));
+}
+
+// f(i) for i in [0, n) over host threads in contiguous blocks (results must not depend on the split).
+template <typename F>
+void parallel_for(int64_t n, F&& f) {
+  const int nt = (int)std::min<int64_t>(host_threads(), std::max<int64_t>(1, n / 64));
+  if (nt <= 1) {
+    for (int64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&, t] {
+      for (int64_t i = n * t / nt; i < n * (t + 1) / nt; ++i) f(i);
+    });
+  for (auto& th : pool) th.join();
+}
+
+// Wall time of a host phase, printed to stderr at scope exit when OBTE_TRACE is set.
+struct PhaseTimer {
+  const char* name;
+  std::chrono::steady_clock::time_point t0;
+  bool on;
+  explicit PhaseTimer(const char* n)
+      : name(n), t0(std::chrono::steady_clock::now()), on(std::getenv("OBTE_TRACE") != nullptr) {}
+  ~PhaseTimer() {
+    if (on)
+      std::fprintf(stderr, "[obte trace] %s %.1f ms\n", name,
+                   std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  }
+};
 
 // ---- device buffer ------------------------------------------------------------
 struct DevBuf {
@@ -94,7 +136,8 @@ struct Schedule {
   std::vector<int32_t> x_cell;     // [x_base[n_dir]] element of each source slot
   // wall outputs: entries (q, wall) with their re-emission weights
   std::vector<int32_t> wo_wall;    // [n_wo]
-  std::vector<double> wo_gg;       // [n_wo * m_pad]  (-GG, i.e. >= 0)
+  std::vector<double> w_db;        // [nd * dim] wall area vector / volume of its element
+  std::vector<double> gbm_sum;     // [nd] sum over ordinates of min(sigma . w_db, 0)
   std::vector<int32_t> wo_off;     // [n_dir+1] first wall-output entry of each direction
   int max_wo = 0;                  // most wall-output entries of one direction
   // contact
@@ -135,10 +178,11 @@ obte_status build_schedule(const obte_problem* prob, const obte_material* mat, S
 //   si/sr    side table of special elements (periodic inflow, wall/periodic/contact outputs)
 struct DevSchedule {
   bool ready = false;
-  int mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;
+  int G = 1, mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;   // G lanes per element, mcp MFPs per CTA
   int emax = 0, unit_wo = 0, pf_pad = 0;   // periodic bank rows, per-unit staging sizes
+  int nbuf = 3;                            // TMA pipeline depth
   size_t smem = 0;
-  DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, mfp, tco, sig, wo_wall, wo_gg, kcoef, scoef, hs, vals, cellmap,
+  DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, mfp, tco, sig, wo_wall, wo_geo, kcoef, scoef, hs, vals, cellmap,
       Pq, si, sr, wo_off, spec;
   size_t bytes() const;
 };

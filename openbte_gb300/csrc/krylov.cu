@@ -21,6 +21,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "internal.h"
@@ -92,15 +95,31 @@ __global__ void __launch_bounds__(VT) reduce_partials_kernel(const double* __res
   }
 }
 
-// w -= sum_j h[j] V[j]; partial[b] = sum over block b of the new w^2
+// w -= sum_j h[j] V[j]; partial[b] = sum over block b of the new w^2.  The coefficients sit in
+// shared memory and the basis is read eight vectors at a time, so each thread keeps eight
+// independent loads in flight instead of one load per dependent FMA.
+constexpr int MAX_BASIS = 256;
 __global__ void __launch_bounds__(VT) update_kernel(double* __restrict__ w, const double* __restrict__ V, int64_t ld,
                                                     int k, const double* __restrict__ h, int64_t n,
                                                     double* __restrict__ partial) {
   __shared__ double red[VT / 32];
+  __shared__ double hs[MAX_BASIS];
+  for (int j = threadIdx.x; j < k; j += VT) hs[j] = h[j];
+  __syncthreads();
   double ss = 0;
   for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
     double acc = w[i];
-    for (int j = 0; j < k; ++j) acc -= h[j] * V[(int64_t)j * ld + i];
+    int j = 0;
+    for (; j + 8 <= k; j += 8) {
+      double v[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) v[t] = V[(int64_t)(j + t) * ld + i];
+      double s = 0;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) s += hs[j + t] * v[t];
+      acc -= s;
+    }
+    for (; j < k; ++j) acc -= hs[j] * V[(int64_t)j * ld + i];
     w[i] = acc;
     ss += acc * acc;
   }
@@ -173,7 +192,24 @@ struct Solver {
   int max_sweeps;
   cudaStream_t st;
 
-  Solver(obte_plan p, Work& w, int ms) : plan(p), wk(w), max_sweeps(ms), st(p->stream) {}
+  Solver(obte_plan p, Work& w, int ms) : plan(p), wk(w), max_sweeps(ms), st(p->stream) {
+    trace = std::getenv("OBTE_TRACE") != nullptr;
+    if (trace)
+      for (auto& e : ev) cudaEventCreate(&e);
+  }
+  ~Solver() {
+    if (trace) {
+      std::fprintf(stderr, "[obte trace] iterations %d: sweep %.1f ms, orthogonalisation %.1f ms (GPU), wall %.1f ms\n",
+                   t_iters, t_sweep, t_gs, t_wall);
+      for (auto& e : ev) cudaEventDestroy(e);
+    }
+  }
+  // optional per-iteration timing (OBTE_TRACE): GPU time of the sweep and of the Gram-Schmidt work
+  bool trace = false;
+  cudaEvent_t ev[3] = {};
+  float t_sweep = 0, t_gs = 0;
+  double t_wall = 0;
+  int t_iters = 0;
 
   obte_status sweep(bool fp32, const double* in, double* out, bool src, bool fin = false) {
     ++sweeps;
@@ -268,7 +304,10 @@ struct Solver {
       double est = beta;
       for (; j < m && sweeps < max_sweeps; ++j) {
         double* vj = V + (int64_t)j * n;
+        const auto w0 = std::chrono::steady_clock::now();
+        if (trace) cudaEventRecord(ev[0], st);
         OBTE_TRY(sweep(fp32, vj, wk.tmp.as<double>(), false));
+        if (trace) cudaEventRecord(ev[1], st);
         OBTE_TRY(lincomb(1.0, vj, -1.0, wk.tmp.as<double>(), w));
         // classical Gram-Schmidt; a second pass only when the first one cancelled most of w
         // (Daniel-Gragg-Kaufman-Stewart criterion, ‖w‖ after < 0.7 ‖w‖ before)
@@ -302,6 +341,17 @@ struct Solver {
         g[j] = cs[j] * g[j];
         est = std::fabs(g[j + 1]);
         if (hn > 0) OBTE_TRY(lincomb(1.0 / hn, w, 0.0, w, V + (int64_t)(j + 1) * n));
+        if (trace) {
+          cudaEventRecord(ev[2], st);
+          cudaEventSynchronize(ev[2]);
+          float a = 0, b = 0;
+          cudaEventElapsedTime(&a, ev[0], ev[1]);
+          cudaEventElapsedTime(&b, ev[1], ev[2]);
+          t_sweep += a;
+          t_gs += b;
+          t_wall += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+          ++t_iters;
+        }
         if (est <= tol || hn == 0) { ++j; break; }
       }
       // y = H^-1 g (upper triangular j x j), x += V y
@@ -331,6 +381,7 @@ struct Solver {
 }  // namespace
 
 static obte_status alloc_work(obte_plan plan, Work& wk, int restart) {
+  PhaseTimer timer("alloc_work");
   const Schedule& s = plan->sched;
   wk.nu = plan->nu;
   wk.restart = restart;

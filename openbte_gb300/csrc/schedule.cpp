@@ -34,6 +34,7 @@ bool in_range(int64_t v, int64_t n) { return v >= 0 && v < n; }
 }  // namespace
 
 obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Schedule& s) {
+  PhaseTimer timer("build_schedule");
   if (!pb || !mt) { set_error("null problem/material"); return OBTE_ERR_BAD_ARG; }
   const int dim = pb->dim;
   if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3"); return OBTE_ERR_BAD_ARG; }
@@ -135,12 +136,14 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     for (int d = 0; d < dim; ++d) v += mt->sigma[((int64_t)m * n_dir + q) * ds + d] * w_db[w * dim + d];
     return v;
   };
-  for (int64_t w = 0; w < nd; ++w) {
+  parallel_for(nd, [&](int64_t w) {
     double acc = 0;
     for (int m = 0; m < n_mfp; ++m)
       for (int q = 0; q < n_dir; ++q) acc += std::min(gb_of(m, q, w), 0.0);
     gbm_sum[w] = acc;
-  }
+  });
+  s.w_db = w_db;
+  s.gbm_sum = gbm_sum;
   // ---- contact (bte.py:132-158) ----
   std::vector<int32_t> c_e1, c_e2;
   std::vector<double> c_na;  // [nc * dim]
@@ -262,7 +265,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
 
   struct DirOut {
     std::vector<int32_t> lev, x_cell, wo_wall;
-    std::vector<double> wo_gg, kcoef, scoef;
+    std::vector<double> kcoef, scoef;
     int nslots = 0;
     obte_status st = OBTE_OK;
     std::string err;
@@ -443,14 +446,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       if (!wall_out[e].empty()) {
         const int32_t begin = (int32_t)o.wo_wall.size();
         if (wall_out[e].size() > 7) { o.st = OBTE_ERR_BAD_ARG; o.err = "too many wall sides on one element"; return; }
-        for (int32_t w : wall_out[e]) {
-          o.wo_wall.push_back(w);
-          for (int m = 0; m < m_pad; ++m) {
-            double v = 0;
-            if (m < n_mfp && gbm_sum[w] != 0) v = std::max(gb_of(m, q, w), 0.0) / (-gbm_sum[w]);
-            o.wo_gg.push_back(v);
-          }
-        }
+        for (int32_t w : wall_out[e]) o.wo_wall.push_back(w);
         s.wout[it] = (begin << 3) | (int32_t)wall_out[e].size();
       }
       // contact coefficients
@@ -518,7 +514,6 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.x_base.assign(n_dir + 1, 0);
   s.x_cell.clear();
   s.wo_wall.clear();
-  s.wo_gg.clear();
   s.wo_off.assign(n_dir + 1, 0);
   s.kcoef.clear();
   s.scoef.clear();
@@ -544,7 +539,6 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       if (s.contact[it] >= 0) s.contact[it] += ce0;
     }
     s.wo_wall.insert(s.wo_wall.end(), o.wo_wall.begin(), o.wo_wall.end());
-    s.wo_gg.insert(s.wo_gg.end(), o.wo_gg.begin(), o.wo_gg.end());
     s.kcoef.insert(s.kcoef.end(), o.kcoef.begin(), o.kcoef.end());
     s.scoef.insert(s.scoef.end(), o.scoef.begin(), o.scoef.end());
     s.wo_off[q + 1] = (int32_t)s.wo_wall.size();

@@ -312,6 +312,7 @@ struct SweepParams {
   int S;                   // slot rows before the zero/trash/periodic rows
   int emax;                // rows per periodic bank
   int unit_wo, pf_pad;     // staging sizes: wall entries and prefetch-list ints per unit
+  int nbuf;                // TMA pipeline depth (units staged at once)
   const int32_t* __restrict__ rec;
   const Real* __restrict__ vals;
   const int32_t* __restrict__ lev_ptr;   // unit boundaries (n[q] + 1 per direction)
@@ -326,7 +327,7 @@ struct SweepParams {
   const Real* __restrict__ mfp;    // [m_pad]
   const Real* __restrict__ tco;    // [n_dir * m_pad]
   const Real* __restrict__ sig;    // [n_dir * m_pad * ds]
-  const Real* __restrict__ wo_gg;  // [direction][chunk][entry][MCP]
+  const Real* __restrict__ wo_geo; // [wall entry][4]: wall area vector / volume (x, y, z), 1 / (-sum_mq min(sigma.w, 0))
   const Real* __restrict__ kcoef;  // [n_ce * m_pad]
   const Real* __restrict__ scoef;  // [n_ce]
   const double* __restrict__ u_in;
@@ -361,24 +362,26 @@ __device__ __forceinline__ double recip(double x) {
 
 // Shared memory layout (bytes):
 //   [0,64) mbarriers  [64,72) abort flags
-//   [128, ...) NBUF x records | NBUF x values | NBUF x wall weights | NBUF x prefetch lists | sig | K S | ring
-static constexpr int NBUF = 3;   // TMA pipeline depth (units in flight)
+//   [128, ...) nbuf x records | nbuf x values | nbuf x wall weights | nbuf x prefetch lists | sig | K S | ring
+// nbuf = TMA pipeline depth: unit u + nbuf - 1 is issued while unit u runs (at most kMaxBuf mbarriers)
+static constexpr int kMaxBuf = 8;
+static constexpr int kDefaultBuf = 3;
 
 template <typename Real>
 struct SmemLayout {
   size_t rec, val, gg, pfl, rec_stride, val_stride, gg_stride, pf_stride, sig, kacc, sacc, ring, total;
-  __host__ __device__ SmemLayout(int mcp, int rows, int unit_wo, int pf_pad) {
+  __host__ __device__ SmemLayout(int mcp, int rows, int unit_wo, int pf_pad, int nbuf) {
     constexpr int W = Rec<Real>::W;
     size_t o = 128;
     rec_stride = (size_t)kUnit * W * 4;
     val_stride = (size_t)(kUnit + 2) * 2 * sizeof(Real);
     val_stride = (val_stride + 15) & ~(size_t)15;
-    gg_stride = (size_t)unit_wo * mcp * sizeof(Real);      // mcp * sizeof(Real) is a multiple of 16
+    gg_stride = (size_t)unit_wo * 4 * sizeof(Real);        // 4 Reals per wall entry (16-B multiple)
     pf_stride = (size_t)pf_pad * 4;                        // pf_pad is a multiple of 4
-    rec = o; o += NBUF * rec_stride;
-    val = o; o += NBUF * val_stride;
-    gg = o; o += NBUF * gg_stride;
-    pfl = o; o += NBUF * pf_stride;
+    rec = o; o += nbuf * rec_stride;
+    val = o; o += nbuf * val_stride;
+    gg = o; o += nbuf * gg_stride;
+    pfl = o; o += nbuf * pf_stride;
     sig = o; o += (size_t)mcp * 3 * sizeof(Real);
     kacc = o; o += (size_t)mcp * sizeof(Real);
     sacc = o; o += (size_t)mcp * sizeof(Real);
@@ -388,138 +391,173 @@ struct SmemLayout {
   }
 };
 
-template <typename Real, int NF, int MCP, bool FINAL>
-__global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real> p) {
-  constexpr int W = Rec<Real>::W;
+// 16-byte vectors of the ring: 4 floats or 2 doubles per lane.
+template <typename Real> struct V16;
+template <> struct V16<float> { static constexpr int K = 4; };
+template <> struct V16<double> { static constexpr int K = 2; };
+
+__device__ __forceinline__ void vload(const float* p, float (&x)[4]) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+}
+__device__ __forceinline__ void vload(const double* p, double (&x)[2]) {
+  const double2 v = *reinterpret_cast<const double2*>(p);
+  x[0] = v.x; x[1] = v.y;
+}
+__device__ __forceinline__ void vstore(float* p, const float (&x)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(x[0], x[1], x[2], x[3]);
+}
+__device__ __forceinline__ void vstore(double* p, const double (&x)[2]) {
+  *reinterpret_cast<double2*>(p) = make_double2(x[0], x[1]);
+}
+
+// Sum over the G lanes of an element group (aligned groups of G lanes inside a warp).
+template <int G, typename T>
+__device__ __forceinline__ T group_sum(T v, unsigned mask) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  return v;
+}
+
+// One CTA = direction q x a chunk of MC = G * KV mean free paths, 128 G threads.  Every element of
+// a unit is owned by a group of G consecutive threads; lane l of the group computes the KV MFPs
+// [l KV, (l+1) KV) of the chunk.  The ring is [row][MC] (MFP fastest), so an upstream read is one
+// 16-byte shared load per lane and a group of 8 reads one full 128-byte row.
+template <typename Real, int NF, int G, bool FINAL>
+__global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<Real> p) {
+  constexpr int RW = Rec<Real>::W;               // record words
+  constexpr int KV = V16<Real>::K;               // MFPs per lane
+  constexpr int MC = G * KV;                     // MFPs per CTA
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
   extern __shared__ __align__(128) unsigned char smem[];
   const int rows = p.rows;
-  const SmemLayout<Real> L(MCP, rows, p.unit_wo, p.pf_pad);
+  const int nbuf = p.nbuf;
+  const SmemLayout<Real> L(MC, rows, p.unit_wo, p.pf_pad, nbuf);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   int* s_abort = reinterpret_cast<int*>(smem + 64);
-  Real* s_sig = reinterpret_cast<Real*>(smem + L.sig);
   Real* s_k = reinterpret_cast<Real*>(smem + L.kacc);
   Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
-  Real* ring = reinterpret_cast<Real*>(smem + L.ring);    // [MCP][rows]
+  Real* ring = reinterpret_cast<Real*>(smem + L.ring);    // [rows][MC]
 
   const int q = blockIdx.x / p.n_chunks;
   const int chunk = blockIdx.x - q * p.n_chunks;
-  const int m0 = chunk * MCP;
-  const int mc = min(MCP, p.n_mfp - m0);
+  const int m0 = chunk * MC;
+  const int mc = min(MC, p.n_mfp - m0);
   const int tid = threadIdx.x;
+  const int el = tid / G;                        // element of the unit owned by this group
+  const int lane = tid - el * G;
+  const int mo = lane * KV;                      // first MFP of this lane (within the chunk)
+  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((tid & 31) & ~(G - 1)));
   const int32_t* __restrict__ lev = p.lev_ptr + p.lev_off[q];
   const int32_t* __restrict__ kwo = p.kwo + p.lev_off[q];
   const int32_t* __restrict__ kpf = p.kpf + p.lev_off[q];
   const int nlev = p.nlev[q];
-  const int32_t* __restrict__ rec_q = p.rec + (int64_t)q * p.n * W;
+  const int32_t* __restrict__ rec_q = p.rec + (int64_t)q * p.n * RW;
   // values: absolute byte offsets from the (256-B aligned) array base keep every TMA window 16-B aligned
   const unsigned char* __restrict__ val_base = reinterpret_cast<const unsigned char*>(p.vals);
   const int64_t val_q0 = (int64_t)q * p.n * VB;
   const int64_t xq = p.x_base[q];
   const int wo0 = p.wo_off[q];
   const int nwo = p.wo_off[q + 1] - wo0;
-  // wall weights of this (direction, chunk): [entry][MCP], entries in sweep order
-  const Real* __restrict__ gg_q = p.wo_gg + ((int64_t)wo0 * p.n_chunks + (int64_t)chunk * nwo) * MCP;
+  // wall weights of this (direction, chunk): [entry][MC], entries in sweep order
+  const Real* __restrict__ gg_q = p.wo_geo + (int64_t)wo0 * 4;
   const int prow0 = p.S + 2;
   const double* __restrict__ X = p.u_in + p.n + p.nd;
   double* __restrict__ dT_out = p.u_out;
   double* __restrict__ TB_out = p.u_out + p.n;
   double* __restrict__ X_out = p.u_out + p.n + p.nd;
 
-  // per-chunk ordinate data in registers; padded MFPs get L = t = 0 (harmless T = b)
-  Real lam[MCP], tt[MCP];
+  // this lane's ordinate data in registers; padded MFPs get L = t = sigma = 0 (harmless T = b)
+  Real lam[KV], tt[KV], sg[KV][3];
 #pragma unroll
-  for (int j = 0; j < MCP; ++j) {
-    const bool ok = j < mc;
-    lam[j] = ok ? p.mfp[m0 + j] : Real(0);
-    tt[j] = ok ? p.tco[(int64_t)q * p.m_pad + m0 + j] : Real(0);
+  for (int j = 0; j < KV; ++j) {
+    const bool ok = mo + j < mc;
+    const int64_t m = m0 + mo + j;
+    lam[j] = ok ? p.mfp[m] : Real(0);
+    tt[j] = ok ? p.tco[(int64_t)q * p.m_pad + m] : Real(0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) sg[j][d] = (ok && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m) * p.ds + d] : Real(0);
   }
-  if (FINAL) {
-    for (int j = tid; j < MCP; j += blockDim.x) {
-      for (int d = 0; d < 3; ++d)
-        s_sig[j * 3 + d] = (j < mc && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m0 + j) * p.ds + d] : Real(0);
-      s_k[j] = 0;
-      s_s[j] = 0;
-    }
-  }
+  if (FINAL)
+    for (int j = tid; j < MC; j += blockDim.x) { s_k[j] = 0; s_s[j] = 0; }
   // ring: zero everything, then bank 0 holds the cut inflow values of unit 0
   const int npf0 = nlev > 0 ? kpf[1] - kpf[0] : 0;
-  for (int i = tid; i < MCP * rows; i += blockDim.x) {
-    const int mm = i / rows, row = i - mm * rows;
+  for (int i = tid; i < MC * rows; i += blockDim.x) {
+    const int row = i / MC, col = i - row * MC;
     Real v = 0;
     const int j = row - prow0;
-    if (j >= 0 && j < npf0 && mm < mc) {
+    if (j >= 0 && j < npf0 && col < mc) {
       const int k = p.pf[kpf[0] + j];
-      if (k >= 0) v = (Real)X[(xq + k) * p.n_mfp + m0 + mm];
+      if (k >= 0) v = (Real)X[(xq + k) * p.n_mfp + m0 + col];
     }
     ring[i] = v;
   }
   if (tid == 0) {
-    for (int i = 0; i < NBUF; ++i) mbar_init(&bars[i], 1);
+    for (int i = 0; i < nbuf; ++i) mbar_init(&bars[i], 1);
     s_abort[0] = 0;
     s_abort[1] = 0;
     fence_mbar_init();
   }
   __syncthreads();
 
-  // TMA of unit u into buffer u % NBUF: records [a, e), values [a, e) (16-B aligned window), the
+  // TMA of unit u into buffer bi: records [a, e), values [a, e) (16-B aligned window), the
   // wall weights of the unit's wall entries and the prefetch list of unit u + 1
-  auto issue = [&](int u) {
+  auto issue = [&](int u, int bi) {
     const int a = lev[u], e = lev[u + 1];
-    const int bi = u % NBUF;
-    const unsigned rbytes = (unsigned)(e - a) * W * 4u;
+    const unsigned rbytes = (unsigned)(e - a) * RW * 4u;
     const int64_t vb0 = (val_q0 + (int64_t)a * VB) & ~(int64_t)15;
     const int64_t vb1 = (val_q0 + (int64_t)e * VB + 15) & ~(int64_t)15;
     const unsigned vbytes = (unsigned)(vb1 - vb0);
     const int w0 = kwo[u], w1 = kwo[u + 1];
-    const unsigned gbytes = (unsigned)(w1 - w0) * MCP * (unsigned)sizeof(Real);
+    const unsigned gbytes = (unsigned)(w1 - w0) * 4u * (unsigned)sizeof(Real);
     const int f0 = u + 1 < nlev ? kpf[u + 1] : 0, f1 = u + 1 < nlev ? kpf[u + 2] : 0;
     const unsigned pbytes = (unsigned)(f1 - f0) * 4u;
     uint64_t* bar = &bars[bi];
     fence_proxy_async();
     mbar_expect_tx(bar, rbytes + vbytes + gbytes + pbytes);
-    tma_load_1d(smem + L.rec + bi * L.rec_stride, rec_q + (int64_t)a * W, rbytes, bar);
+    tma_load_1d(smem + L.rec + bi * L.rec_stride, rec_q + (int64_t)a * RW, rbytes, bar);
     tma_load_1d(smem + L.val + bi * L.val_stride, val_base + vb0, vbytes, bar);
-    if (gbytes) tma_load_1d(smem + L.gg + bi * L.gg_stride, gg_q + (int64_t)w0 * MCP, gbytes, bar);
+    if (gbytes) tma_load_1d(smem + L.gg + bi * L.gg_stride, gg_q + (int64_t)w0 * 4, gbytes, bar);
     if (pbytes) tma_load_1d(smem + L.pfl + bi * L.pf_stride, p.pf + f0, pbytes, bar);
   };
   if (tid == 0)
-    for (int u = 0; u < NBUF - 1 && u < nlev; ++u) issue(u);
+    for (int u = 0; u < nbuf - 1 && u < nlev; ++u) issue(u, u);
 
+  int bi = 0;            // buffer of unit u (u mod nbuf)
+  unsigned phase = 0;    // parity of its mbarrier phase ((u / nbuf) & 1)
   for (int u = 0; u < nlev; ++u) {
-    const int bi = u % NBUF;
     const int cur = u & 1;
     const int a = lev[u], e = lev[u + 1];
     const int wu = kwo[u];
     const int npf = u + 1 < nlev ? kpf[u + 2] - kpf[u + 1] : 0;   // padded length of unit u+1's list
     const int prow_next = prow0 + ((u + 1) & 1) * p.emax;
-    // buffer (u + NBUF - 1) % NBUF was last read during unit u - 1, finished at the barrier below
-    if (tid == 0 && u + NBUF - 1 < nlev) issue(u + NBUF - 1);
-    const bool ready = mbar_wait_bounded(&bars[bi], (unsigned)(u / NBUF) & 1u);
+    // buffer (u + nbuf - 1) mod nbuf was last read during unit u - 1, finished at the barrier below
+    if (tid == 0 && u + nbuf - 1 < nlev) issue(u + nbuf - 1, bi == 0 ? nbuf - 1 : bi - 1);
+    const bool ready = mbar_wait_bounded(&bars[bi], phase);
     if (!ready) {
       s_abort[cur] = 1;
       atomicOr(p.err, 1);
     } else {
       // cut inflow values of unit u+1: loads issued now, stored into bank (u+1)&1 after the MFP loop
       const int32_t* s_pf = reinterpret_cast<const int32_t*>(smem + L.pfl + bi * L.pf_stride);
-      const int pk = tid < npf ? s_pf[tid] : -1;
-      double xv[MCP];
+      const int pk = el < npf ? s_pf[el] : -1;
+      double xv[KV];
       if (pk >= 0) {
-        const double* xs = X + (xq + pk) * p.n_mfp + m0;
+        const double* xs = X + (xq + pk) * p.n_mfp + m0 + mo;
 #pragma unroll
-        for (int mm = 0; mm < MCP; ++mm) xv[mm] = mm < mc ? __ldg(xs + mm) : 0.0;
+        for (int j = 0; j < KV; ++j) xv[j] = mo + j < mc ? __ldg(xs + j) : 0.0;
       }
-      if (tid < e - a) {
-        // record: W/4 vector loads
-        int32_t r[W];
-        const int4* r4 = reinterpret_cast<const int4*>(smem + L.rec + bi * L.rec_stride) + tid * (W / 4);
+      if (el < e - a) {
+        // record: RW/4 vector loads (the G lanes of the group read the same record)
+        int32_t r[RW];
+        const int4* r4 = reinterpret_cast<const int4*>(smem + L.rec + bi * L.rec_stride) + el * (RW / 4);
 #pragma unroll
-        for (int i = 0; i < W / 4; ++i) {
+        for (int i = 0; i < RW / 4; ++i) {
           const int4 x = r4[i];
           r[4 * i] = x.x; r[4 * i + 1] = x.y; r[4 * i + 2] = x.z; r[4 * i + 3] = x.w;
         }
         const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
-        const Real* v = reinterpret_cast<const Real*>(smem + L.val + bi * L.val_stride) + 2 * (voff + tid);
+        const Real* v = reinterpret_cast<const Real*>(smem + L.val + bi * L.val_stride) + 2 * (voff + el);
         const Real b = v[0], pw = v[1];
         const int c = r[0];
         const int so = r[1] & 0xFFFF, s0 = (int)((unsigned)r[1] >> 16);
@@ -531,87 +569,97 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
         const Real c2 = word_real<Real>(r, Rec<Real>::COEF + 2 * Rec<Real>::CSTEP);
         const Real c3 = word_real<Real>(r, Rec<Real>::COEF + 3 * Rec<Real>::CSTEP);
         const Real D = word_real<Real>(r, Rec<Real>::D);
+        Real v0[KV], v1[KV], v2[KV], v3[KV];
+        vload(ring + (size_t)s0 * MC + mo, v0);
+        vload(ring + (size_t)s1 * MC + mo, v1);
+        vload(ring + (size_t)s2 * MC + mo, v2);
+        if (NF > 3) vload(ring + (size_t)s3 * MC + mo, v3);
+        Real T[KV];
         Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
 #pragma unroll
-        for (int mb = 0; mb < MCP; mb += 4) {
-          Real v0[4], v1[4], v2[4], v3[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const Real* row = ring + (size_t)(mb + j) * rows;
-            v0[j] = row[s0];
-            v1[j] = row[s1];
-            v2[j] = row[s2];
-            if (NF > 3) v3[j] = row[s3];
-          }
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int mm = mb + j;
-            Real s = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
-            if (NF > 3) s += c3 * v3[j];
-            const Real T = (b + lam[mm] * (pw - s)) * recip(Real(1) + lam[mm] * D);
-            ring[(size_t)mm * rows + so] = T;
-            dacc += tt[mm] * T;
-            if (FINAL && p.Xs != nullptr && mm < mc) p.Xs[((int64_t)q * p.n + c) * p.n_mfp + m0 + mm] = (float)T;
-            if (FINAL) {
-              j0 += s_sig[mm * 3] * T;
-              j1 += s_sig[mm * 3 + 1] * T;
-              j2 += s_sig[mm * 3 + 2] * T;
-            }
+        for (int j = 0; j < KV; ++j) {
+          Real sm = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
+          if (NF > 3) sm += c3 * v3[j];
+          T[j] = (b + lam[j] * (pw - sm)) * recip(Real(1) + lam[j] * D);
+          dacc += tt[j] * T[j];
+          if (FINAL) {
+            j0 += sg[j][0] * T[j];
+            j1 += sg[j][1] * T[j];
+            j2 += sg[j][2] * T[j];
           }
         }
-        atomicAdd(&dT_out[c], (double)dacc);
+        vstore(ring + (size_t)so * MC + mo, T);
+        if (FINAL && p.Xs != nullptr) {
+#pragma unroll
+          for (int j = 0; j < KV; ++j)
+            if (mo + j < mc) p.Xs[((int64_t)q * p.n + c) * p.n_mfp + m0 + mo + j] = (float)T[j];
+        }
+        dacc = group_sum<G>(dacc, gmask);
+        if (lane == 0) atomicAdd(&dT_out[c], (double)dacc);
         if (FINAL) {
-          atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
-          if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
-          if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
+          j0 = group_sum<G>(j0, gmask);
+          j1 = group_sum<G>(j1, gmask);
+          j2 = group_sum<G>(j2, gmask);
+          if (lane == 0) {
+            atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
+            if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
+            if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
+          }
         }
-        // per-MFP outputs of special elements, read back from their own row (shared memory only)
-        if (xk >= 0 || wo != 0 || (FINAL && ce >= 0)) {
-          const int wb = wo >> 3, wn = wo & 7;
-          // staged weights of this unit's entries; absent entries read the first entry's row (unused)
-          const Real* s_gg = reinterpret_cast<const Real*>(smem + L.gg + bi * L.gg_stride) + (wb - wu) * MCP;
-          const Real* g0 = s_gg;
-          const Real* g1 = s_gg + (wn > 1 ? MCP : 0);
-          const Real* g2 = s_gg + (wn > 2 ? 2 * MCP : 0);
-          Real Ts[MCP];
+        // per-MFP outputs of special elements (the group is uniform in these conditions)
+        if (xk >= 0) {
 #pragma unroll
-          for (int mm = 0; mm < MCP; ++mm) Ts[mm] = ring[(size_t)mm * rows + so];
+          for (int j = 0; j < KV; ++j)
+            if (mo + j < mc) X_out[(xq + xk) * p.n_mfp + m0 + mo + j] = (double)T[j];
+        }
+        if (wo != 0) {
+          const int wb = wo >> 3, wn = wo & 7;
+          // re-emission weight max(sigma . w, 0) / (-sum min(sigma . w, 0)) from the staged wall geometry
+          // (bte.py:73-78); absent entries read the first entry (unused)
+          const Real* gw = reinterpret_cast<const Real*>(smem + L.gg + bi * L.gg_stride) + (size_t)(wb - wu) * 4;
+          const Real* gw1 = gw + (wn > 1 ? 4 : 0);
+          const Real* gw2 = gw + (wn > 2 ? 8 : 0);
           Real w0 = 0, w1 = 0, w2 = 0;
 #pragma unroll
-          for (int mm = 0; mm < MCP; ++mm) {
-            w0 += g0[mm] * Ts[mm];
-            w1 += g1[mm] * Ts[mm];
-            w2 += g2[mm] * Ts[mm];
+          for (int j = 0; j < KV; ++j) {
+            const Real a0 = sg[j][0] * gw[0] + sg[j][1] * gw[1] + sg[j][2] * gw[2];
+            const Real a1 = sg[j][0] * gw1[0] + sg[j][1] * gw1[1] + sg[j][2] * gw1[2];
+            const Real a2 = sg[j][0] * gw2[0] + sg[j][1] * gw2[1] + sg[j][2] * gw2[2];
+            w0 += (a0 > Real(0) ? a0 * gw[3] : Real(0)) * T[j];
+            w1 += (a1 > Real(0) ? a1 * gw1[3] : Real(0)) * T[j];
+            w2 += (a2 > Real(0) ? a2 * gw2[3] : Real(0)) * T[j];
           }
-          if (xk >= 0) {
-#pragma unroll
-            for (int mm = 0; mm < MCP; ++mm)
-              if (mm < mc) X_out[(xq + xk) * p.n_mfp + m0 + mm] = (double)Ts[mm];
+          w0 = group_sum<G>(w0, gmask);
+          if (wn > 1) w1 = group_sum<G>(w1, gmask);
+          if (wn > 2) w2 = group_sum<G>(w2, gmask);
+          if (lane == 0) {
+            atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
+            if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 1]], (double)w1);
+            if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 2]], (double)w2);
           }
-          if (FINAL && ce >= 0) {
+        }
+        if (FINAL && ce >= 0) {
 #pragma unroll
-            for (int mm = 0; mm < MCP; ++mm) {
-              if (mm < mc) {
-                atomicAdd(&s_k[mm], p.kcoef[(int64_t)ce * p.m_pad + m0 + mm] * Ts[mm]);
-                atomicAdd(&s_s[mm], p.scoef[ce] * Ts[mm]);
-              }
+          for (int j = 0; j < KV; ++j) {
+            if (mo + j < mc) {
+              atomicAdd(&s_k[mo + j], p.kcoef[(int64_t)ce * p.m_pad + m0 + mo + j] * T[j]);
+              atomicAdd(&s_s[mo + j], p.scoef[ce] * T[j]);
             }
           }
-          if (wn > 0) atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
-          if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 1]], (double)w1);
-          if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 2]], (double)w2);
         }
       }
       // bank (u+1)&1 was last read during unit u-1
       if (pk >= 0) {
+        Real xr[KV];
 #pragma unroll
-        for (int mm = 0; mm < MCP; ++mm) ring[(size_t)mm * rows + prow_next + tid] = (Real)xv[mm];
+        for (int j = 0; j < KV; ++j) xr[j] = (Real)xv[j];
+        vstore(ring + (size_t)(prow_next + el) * MC + mo, xr);
       }
-      for (int i = tid + kUnit; i < npf; i += kUnit) {   // units with more than kUnit cut inflow faces
+      for (int i = el + kUnit; i < npf; i += kUnit) {   // units with more than kUnit cut inflow faces
         const int k = s_pf[i];
         if (k < 0) continue;
-        const double* xs = X + (xq + k) * p.n_mfp + m0;
-        for (int mm = 0; mm < MCP; ++mm) ring[(size_t)mm * rows + prow_next + i] = mm < mc ? (Real)xs[mm] : Real(0);
+        const double* xs = X + (xq + k) * p.n_mfp + m0 + mo;
+        for (int j = 0; j < KV; ++j) ring[(size_t)(prow_next + i) * MC + mo + j] = mo + j < mc ? (Real)xs[j] : Real(0);
       }
     }
     __syncthreads();
@@ -619,10 +667,11 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
     if (s_abort[cur]) {
       // let the copies this CTA still has in flight land before leaving (bounded)
       if (tid == 0)
-        for (int w = u + 1; w < nlev && w < u + NBUF; ++w) mbar_wait_bounded(&bars[w % NBUF], (unsigned)(w / NBUF) & 1u);
+        for (int w = u + 1; w < nlev && w < u + nbuf; ++w) mbar_wait_bounded(&bars[w % nbuf], (unsigned)(w / nbuf) & 1u);
       __syncthreads();
       return;
     }
+    if (++bi == nbuf) { bi = 0; phase ^= 1u; }
   }
   if (FINAL) {
     for (int j = tid; j < mc; j += blockDim.x) {
@@ -635,7 +684,7 @@ __global__ void __launch_bounds__(kUnit) bte_sweep_kernel(const SweepParams<Real
 // ---- table upload ---------------------------------------------------------------
 
 size_t DevSchedule::bytes() const {
-  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &kwo, &kpf, &pf, &mfp, &tco, &sig, &wo_wall, &wo_gg,
+  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &kwo, &kpf, &pf, &mfp, &tco, &sig, &wo_wall, &wo_geo,
                          &kcoef, &scoef, &hs, &vals, &cellmap, &Pq, &si, &sr, &wo_off, &spec};
   size_t b = 0;
   for (auto* x : all) b += x->bytes;
@@ -649,55 +698,49 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
   return upload(b, h, st);
 }
 
-// Chunk widths compiled for each precision.
-template <typename Real> struct Widths;
-template <> struct Widths<float> { static constexpr int N = 5; static constexpr int v[N] = {4, 8, 12, 16, 24}; };
-template <> struct Widths<double> { static constexpr int N = 4; static constexpr int v[N] = {4, 8, 12, 16}; };
-constexpr int Widths<float>::v[];
-constexpr int Widths<double>::v[];
+// Lane-group sizes compiled for each precision (chunk width = G x V16<Real>::K MFPs).
+static constexpr int kGroups[] = {1, 2, 4, 8};
 
-// Choose the chunk width: minimise waves x (per-unit overhead + chunk width) / resident CTAs,
-// under the shared-memory budget.  OBTE_SWEEP_MCP forces a width (tuning).
+// Choose the lane-group size G.  Measured on the 60k-triangle (100 MFP x 96 directions) and the
+// 110k-tetrahedron (30 x 512) benchmark meshes: G = 1 is fastest (2.32 ms / 10.5 ms per FP32 sweep
+// against 2.40 / 16.7 ms at G = 2 and 2.90 ms at G = 8), because each CTA is a chain of level
+// barriers and more, smaller CTAs per SM keep more chains in flight.  Larger groups stay available
+// through OBTE_SWEEP_G (tuning); a size whose shared memory does not fit is skipped.
 template <typename Real>
-static int choose_mcp(const Schedule& s, int rows, int unit_wo, int pf_pad, int num_sms, size_t optin) {
-  const char* env = std::getenv("OBTE_SWEEP_MCP");
-  const int forced = env ? std::atoi(env) : 0;
-  double best = 1e300;
-  int best_w = 0;
-  for (int i = 0; i < Widths<Real>::N; ++i) {
-    const int w = Widths<Real>::v[i];
-    if (forced && w != forced) continue;
-    const size_t sm = SmemLayout<Real>(w, rows, unit_wo, pf_pad).total;
-    if (sm > optin) continue;
-    const int per_sm = std::max(1, std::min(8, (int)((228 * 1024) / (sm + 1024))));
-    const int chunks = (s.n_mfp + w - 1) / w;
-    const int64_t ctas = (int64_t)s.n_dir * chunks;
-    const int64_t slots = (int64_t)num_sms * per_sm;
-    const int64_t waves = (ctas + slots - 1) / slots;
-    // per-CTA time ~ units x (overhead + w); resident CTAs share the SM's issue slots
-    // measured on a 60k-element mesh: per-unit overhead ~ 16 MFP-iterations; co-resident CTAs overlap
-    const double per_cta = 16.0 + w;
-    const double cost = (double)waves * per_cta / std::sqrt((double)std::min<int64_t>(per_sm, 4));
-    if (cost < best) { best = cost; best_w = w; }
+static int choose_group(const Schedule& s, int rows, int unit_wo, int pf_pad, int nbuf, int num_sms, size_t optin) {
+  (void)s; (void)num_sms;
+  const char* env = std::getenv("OBTE_SWEEP_G");
+  const int forced = env ? std::atoi(env) : 1;
+  for (int G : kGroups) {
+    if (G != forced) continue;
+    if (SmemLayout<Real>(G * V16<Real>::K, rows, unit_wo, pf_pad, nbuf).total <= optin) return G;
   }
-  return best_w;
+  return SmemLayout<Real>(V16<Real>::K, rows, unit_wo, pf_pad, nbuf).total <= optin ? 1 : 0;
 }
 
 template <typename Real>
 static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
+  PhaseTimer timer(sizeof(Real) == 4 ? "upload_tables fp32" : "upload_tables fp64");
   const Schedule& s = plan->sched;
   cudaStream_t st = plan->stream;
   // split levels into units of at most kUnit elements (slots were assigned per level, so this stays valid)
   Units un;
   build_units(s, un);
   Packed pk;
-  OBTE_TRY(pack<Real>(s, un, pk));
+  {
+    PhaseTimer tp("pack");
+    OBTE_TRY(pack<Real>(s, un, pk));
+  }
   const int rows = pk.rows;
-  const int mcp = choose_mcp<Real>(s, rows, pk.unit_wo, pk.pf_pad, plan->ctx->num_sms, plan->ctx->smem_optin);
-  if (!mcp) {
+  const char* nb_env = std::getenv("OBTE_SWEEP_NBUF");
+  const int nbuf = nb_env ? std::max(2, std::min(kMaxBuf, std::atoi(nb_env))) : kDefaultBuf;
+  const int G = choose_group<Real>(s, rows, pk.unit_wo, pk.pf_pad, nbuf, plan->ctx->num_sms, plan->ctx->smem_optin);
+  if (!G) {
     set_error("sweep front needs more shared memory than one CTA can have (" + std::to_string(rows) + " rows)");
     return OBTE_ERR_UNSUPPORTED;
   }
+  const int mcp = G * V16<Real>::K;
+  d.G = G;
   d.mc = mcp;
   d.mcp = mcp;
   d.n_chunks = (s.n_mfp + mcp - 1) / mcp;
@@ -706,7 +749,8 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   d.emax = pk.emax;
   d.unit_wo = pk.unit_wo;
   d.pf_pad = pk.pf_pad;
-  d.smem = SmemLayout<Real>(mcp, rows, pk.unit_wo, pk.pf_pad).total;
+  d.nbuf = nbuf;
+  d.smem = SmemLayout<Real>(mcp, rows, pk.unit_wo, pk.pf_pad, nbuf).total;
   OBTE_TRY(upload(d.rec, pk.rec, st));
   OBTE_TRY(upload(d.cellmap, pk.cellmap, st));
   OBTE_TRY(upload(d.Pq, pk.P, st));
@@ -728,19 +772,15 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   OBTE_TRY(upload_real<Real>(d.sig, s.sig, st));
   {
     // wall weights regrouped [direction][chunk][entry][mcp] so one unit's entries are one contiguous copy
+    // per wall entry: area vector / volume of the wall's element and 1 / (-sum_mq min(sigma . w, 0))
     const int64_t n_wo = (int64_t)s.wo_wall.size();
-    std::vector<double> gg((size_t)n_wo * d.n_chunks * mcp, 0.0);
-    for (int q = 0; q < s.n_dir; ++q) {
-      const int64_t w0 = s.wo_off[q], nw = s.wo_off[q + 1] - w0;
-      for (int c = 0; c < d.n_chunks; ++c)
-        for (int64_t e = 0; e < nw; ++e)
-          for (int j = 0; j < mcp; ++j) {
-            const int m = c * mcp + j;
-            if (m < s.n_mfp)
-              gg[(size_t)(((w0 * d.n_chunks + (int64_t)c * nw) + e) * mcp + j)] = s.wo_gg[(size_t)(w0 + e) * s.m_pad + m];
-          }
-    }
-    OBTE_TRY(upload_real<Real>(d.wo_gg, gg, st));
+    std::vector<Real> geo(std::max<size_t>((size_t)n_wo * 4, 4), Real(0));
+    parallel_for(n_wo, [&](int64_t e) {
+      const int32_t w = s.wo_wall[e];
+      for (int k = 0; k < s.dim; ++k) geo[(size_t)e * 4 + k] = (Real)s.w_db[(size_t)w * s.dim + k];
+      geo[(size_t)e * 4 + 3] = s.gbm_sum[w] != 0 ? (Real)(1.0 / (-s.gbm_sum[w])) : Real(0);
+    });
+    OBTE_TRY(upload(d.wo_geo, geo, st));
   }
   OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
   OBTE_TRY(upload_real<Real>(d.scoef, s.scoef, st));
@@ -767,7 +807,7 @@ obte_status ensure_tables(obte_plan plan, bool fp32) {
 
 // ---- launch -----------------------------------------------------------------------
 
-template <typename Real, int NF, int MCP, bool FINAL>
+template <typename Real, int NF, int G, bool FINAL>
 static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                bool with_src, double* Jraw, double* K, double* S) {
   const Schedule& s = plan->sched;
@@ -780,39 +820,39 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
       d.vals.as<Real>());
   count_launch();
   OBTE_CUDA(cudaGetLastError());
-  auto kern = bte_sweep_kernel<Real, NF, MCP, FINAL>;
+  auto kern = bte_sweep_kernel<Real, NF, G, FINAL>;
   OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
   p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;
-  p.emax = d.emax; p.unit_wo = d.unit_wo; p.pf_pad = d.pf_pad;
+  p.emax = d.emax; p.unit_wo = d.unit_wo; p.pf_pad = d.pf_pad; p.nbuf = d.nbuf;
   p.rec = d.rec.as<int32_t>(); p.vals = d.vals.as<Real>();
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
   p.kwo = d.kwo.as<int32_t>(); p.kpf = d.kpf.as<int32_t>(); p.pf = d.pf.as<int32_t>();
   p.x_base = plan->x_base_dev.as<int64_t>();
   p.wo_off = d.wo_off.as<int32_t>();
   p.wo_wall = d.wo_wall.as<int32_t>();
-  p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_gg = d.wo_gg.as<Real>();
+  p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_geo = d.wo_geo.as<Real>();
   p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
   p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S_out = S;
   p.err = plan->err.as<int>();
   p.Xs = FINAL ? plan->xstore : nullptr;
   const int grid = s.n_dir * d.n_chunks;
-  kern<<<grid, kUnit, d.smem, st>>>(p);
+  kern<<<grid, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
   return OBTE_OK;
 }
 
-template <typename Real, int MCP>
+template <typename Real, int G>
 static obte_status launch_w(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out, bool with_src,
                             bool final_pass, double* Jraw, double* K, double* S) {
   if (plan->sched.nf == 3) {
-    if (final_pass) return launch_impl<Real, 3, MCP, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
-    return launch_impl<Real, 3, MCP, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+    if (final_pass) return launch_impl<Real, 3, G, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+    return launch_impl<Real, 3, G, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
   }
-  if (final_pass) return launch_impl<Real, 4, MCP, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
-  return launch_impl<Real, 4, MCP, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  if (final_pass) return launch_impl<Real, 4, G, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  return launch_impl<Real, 4, G, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
 }
 
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
@@ -825,15 +865,15 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
   OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
   if (final_pass) OBTE_CUDA(cudaMemsetAsync(Jraw, 0, (size_t)s.n * s.ds * sizeof(double), st));
   const DevSchedule& d = fp32 ? plan->d32 : plan->d64;
-#define OBTE_W(R, M) \
-  case M: return launch_w<R, M>(plan, d, u_in, u_out, with_src, final_pass, Jraw, K, S)
+#define OBTE_W(R, G) \
+  case G: return launch_w<R, G>(plan, d, u_in, u_out, with_src, final_pass, Jraw, K, S)
   if (fp32) {
-    switch (d.mcp) { OBTE_W(float, 4); OBTE_W(float, 8); OBTE_W(float, 12); OBTE_W(float, 16); OBTE_W(float, 24); }
+    switch (d.G) { OBTE_W(float, 1); OBTE_W(float, 2); OBTE_W(float, 4); OBTE_W(float, 8); }
   } else {
-    switch (d.mcp) { OBTE_W(double, 4); OBTE_W(double, 8); OBTE_W(double, 12); OBTE_W(double, 16); }
+    switch (d.G) { OBTE_W(double, 1); OBTE_W(double, 2); OBTE_W(double, 4); OBTE_W(double, 8); }
   }
 #undef OBTE_W
-  set_error("no compiled sweep kernel for this chunk width");
+  set_error("no compiled sweep kernel for this lane-group size");
   return OBTE_ERR_UNSUPPORTED;
 }
 
@@ -896,7 +936,7 @@ static obte_status static_scratch_address(int device, void** out) {
   return OBTE_OK;
 }
 
-template <typename Real, int NF, int MCP>
+template <typename Real, int NF, int G>
 static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                       bool with_src, Real* vals, int* err) {
   const Schedule& s = plan->sched;
@@ -908,34 +948,34 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
       s.n, s.hs.empty() ? nullptr : d.hs.as<double>(), with_src ? 1 : 0, total, vals);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
-  auto kern = bte_sweep_kernel<Real, NF, MCP, false>;
+  auto kern = bte_sweep_kernel<Real, NF, G, false>;
   OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
   p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;
-  p.emax = d.emax; p.unit_wo = d.unit_wo; p.pf_pad = d.pf_pad;
+  p.emax = d.emax; p.unit_wo = d.unit_wo; p.pf_pad = d.pf_pad; p.nbuf = d.nbuf;
   p.rec = d.rec.as<int32_t>(); p.vals = vals;
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
   p.kwo = d.kwo.as<int32_t>(); p.kpf = d.kpf.as<int32_t>(); p.pf = d.pf.as<int32_t>();
   p.x_base = plan->x_base_dev.as<int64_t>();
   p.wo_off = d.wo_off.as<int32_t>();
   p.wo_wall = d.wo_wall.as<int32_t>();
-  p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_gg = d.wo_gg.as<Real>();
+  p.mfp = d.mfp.as<Real>(); p.tco = d.tco.as<Real>(); p.sig = d.sig.as<Real>(); p.wo_geo = d.wo_geo.as<Real>();
   p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
   p.u_in = u_in; p.u_out = u_out; p.Jraw = nullptr; p.K = nullptr; p.S_out = nullptr;
   p.err = err;
   p.Xs = nullptr;
-  kern<<<s.n_dir * d.n_chunks, kUnit, d.smem, st>>>(p);
+  kern<<<s.n_dir * d.n_chunks, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
   return OBTE_OK;
 }
 
-template <typename Real, int MCP>
+template <typename Real, int G>
 static obte_status launch_static_w(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                    bool with_src, Real* vals, int* err) {
-  if (plan->sched.nf == 3) return launch_static_impl<Real, 3, MCP>(plan, d, u_in, u_out, with_src, vals, err);
-  return launch_static_impl<Real, 4, MCP>(plan, d, u_in, u_out, with_src, vals, err);
+  if (plan->sched.nf == 3) return launch_static_impl<Real, 3, G>(plan, d, u_in, u_out, with_src, vals, err);
+  return launch_static_impl<Real, 4, G>(plan, d, u_in, u_out, with_src, vals, err);
 }
 
 // Runs with the plan's device current; the caller restores its own.
@@ -951,15 +991,15 @@ static obte_status sweep_static_on_device(obte_plan plan, bool fp32, const doubl
   OBTE_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
   OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
   obte_status rc = OBTE_ERR_UNSUPPORTED;
-#define OBTE_SW(R, M) \
-  case M: rc = launch_static_w<R, M>(plan, d, u_in, u_out, with_src, static_cast<R*>(vals), err); break
+#define OBTE_SW(R, G) \
+  case G: rc = launch_static_w<R, G>(plan, d, u_in, u_out, with_src, static_cast<R*>(vals), err); break
   if (fp32) {
-    switch (d.mcp) { OBTE_SW(float, 4); OBTE_SW(float, 8); OBTE_SW(float, 12); OBTE_SW(float, 16); OBTE_SW(float, 24); }
+    switch (d.G) { OBTE_SW(float, 1); OBTE_SW(float, 2); OBTE_SW(float, 4); OBTE_SW(float, 8); }
   } else {
-    switch (d.mcp) { OBTE_SW(double, 4); OBTE_SW(double, 8); OBTE_SW(double, 12); OBTE_SW(double, 16); }
+    switch (d.G) { OBTE_SW(double, 1); OBTE_SW(double, 2); OBTE_SW(double, 4); OBTE_SW(double, 8); }
   }
 #undef OBTE_SW
-  if (rc == OBTE_ERR_UNSUPPORTED) set_error("no compiled sweep kernel for this chunk width");
+  if (rc == OBTE_ERR_UNSUPPORTED) set_error("no compiled sweep kernel for this lane-group size");
   if (rc != OBTE_OK) return rc;
   int h = 0;
   OBTE_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -90,6 +90,7 @@ tim_gradient_kernel(const float* __restrict__ X, const double* __restrict__ TB, 
 
 // Host checks of the adjoint identity's assumptions, then the device tables.
 static obte_status ensure_tim(obte_plan plan) {
+  PhaseTimer timer("ensure_tim");
   if (!plan->tim) plan->tim.reset(new TimDevice());
   TimDevice& T = *plan->tim;
   if (T.ready) return OBTE_OK;

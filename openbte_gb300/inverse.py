@@ -101,7 +101,7 @@ class PixelSolver:
     """kappa_eff and dkappa/drho of an n x n pixel cell (one plan per density field)."""
 
     def __init__(self, n: int, material: IsotropicMaterial, size: float = 1.0, direction=(1, 0), device: int = 0,
-                 precision: str = "fp32_refine", rtol: float = 1e-8, restart: int = 30, max_sweeps: int = 2000):
+                 precision: str = "fp32_refine", rtol: float = 1e-8, restart: int = 100, max_sweeps: int = 3000):
         if tuple(direction) not in ((1, 0), (0, 1)):
             raise NotImplementedError("kappa along x ([1, 0]) or y ([0, 1])")
         self.lib = _lib.load()
@@ -117,6 +117,7 @@ class PixelSolver:
         self.contact = np.nonzero(jump_sides)[0].astype(np.int64)
         self.empty = np.zeros(1, dtype=np.int64)
         self.last_info = None
+        self.last_upload_bytes = 0
 
     def _problem(self, t_host):
         g = self.grid
@@ -149,6 +150,10 @@ class PixelSolver:
         h = C.c_void_p()
         _lib.check(self.lib.obte_bte_plan_create(ctx, C.byref(prob), C.byref(mat), C.byref(h)), "obte_bte_plan_create")
         try:
+            pb, sb = C.c_int64(), C.c_int64()
+            _lib.check(self.lib.obte_bte_plan_footprint(h, _lib.PRECISION[self.precision], self.restart, C.byref(pb),
+                                                        C.byref(sb)), "obte_bte_plan_footprint")
+            self.last_upload_bytes = pb.value      # device tables built from the host schedule (an upper bound)
             opts = _lib.SolveOpts(precision=_lib.PRECISION[self.precision], rtol=self.rtol, max_sweeps=self.max_sweeps,
                                   restart=self.restart, refine_steps=20, inner_rtol=1e-5, warm_start=0)
             dT0 = torch.zeros(self.grid["n_elems"], dtype=torch.float64, device=dev)
