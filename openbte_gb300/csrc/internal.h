@@ -196,6 +196,7 @@ struct SolveWork {
   int restart = 0;
   int nb = 1;
   DevBuf u, Fu, r, V, w, tmp, partial, hdev, sdev, Jraw, Kraw, Sraw, delta;
+  DevBuf V32, w32;   // FP32 basis and working vector (stages with FP32 sweeps), allocated on first use
 };
 
 // Transmission-interface gradient: per internal side tables, ordinate tables and the final-pass

@@ -15,8 +15,11 @@
 // value at the initial guess, reproducing the reference's temperature level.
 //
 // Precision modes: FP64 sweeps; FP32 sweeps; FP32 sweeps inside an iterative
-// refinement whose residual F(u) - u is evaluated with FP64 sweeps.  Vectors,
-// reductions and the Hessenberg system are FP64 in every mode.
+// refinement whose residual F(u) - u is evaluated with FP64 sweeps.  The
+// solution, residuals, cross-block reductions and the Hessenberg system are
+// FP64 in every mode; the Krylov basis is FP32 in stages that sweep in FP32 to a
+// relative tolerance of 1e-6 or looser (the inner solves of the refinement),
+// FP64 otherwise.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -133,6 +136,116 @@ __global__ void __launch_bounds__(VT) update_kernel(double* __restrict__ w, cons
       partial[blockIdx.x] = t;
     }
   }
+}
+
+// ---- FP32 Krylov basis (stages whose sweeps are FP32) ------------------------------------------
+// On GB300 the FP64 pipe cannot keep up with HBM for one FMA per 8 loaded bytes, so the Gram-Schmidt
+// passes of the FP32 stages keep the basis V and the new vector w in FP32: FP32 products and
+// per-thread sums, FP64 across threads and blocks.  The sweep still takes FP64 input (one widening
+// pass per Krylov vector) and the solution x stays FP64.
+
+// partial[b * kk + j] = block b's part of V[j] . w (j < k) and of w . w (j == k when self)
+__global__ void __launch_bounds__(VT) multidot32_kernel(const float* __restrict__ V, int64_t ld, int k, int self,
+                                                        const float* __restrict__ w, int64_t n,
+                                                        double* __restrict__ partial) {
+  __shared__ double red[VT / 32][DOT_TILE];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int kk = k + self;
+  for (int jt = 0; jt < kk; jt += DOT_TILE) {
+    const float* vp[DOT_TILE];
+#pragma unroll
+    for (int t = 0; t < DOT_TILE; ++t) vp[t] = jt + t < k ? V + (int64_t)(jt + t) * ld : w;   // self / padding read w
+    float acc[DOT_TILE];
+#pragma unroll
+    for (int t = 0; t < DOT_TILE; ++t) acc[t] = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
+      const float wi = w[i];
+#pragma unroll
+      for (int t = 0; t < DOT_TILE; ++t) acc[t] = fmaf(vp[t][i], wi, acc[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < DOT_TILE; ++t) {
+      double v = (double)acc[t];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][t] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < DOT_TILE && jt + (int)threadIdx.x < kk) {
+      double v = 0;
+      for (int w2 = 0; w2 < VT / 32; ++w2) v += red[w2][threadIdx.x];
+      partial[(int64_t)blockIdx.x * kk + jt + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// w -= sum_j h[j] V[j] (FP32); partial[b] = block b's part of the new w . w
+__global__ void __launch_bounds__(VT) update32_kernel(float* __restrict__ w, const float* __restrict__ V, int64_t ld,
+                                                      int k, const double* __restrict__ h, int64_t n,
+                                                      double* __restrict__ partial) {
+  __shared__ double red[VT / 32];
+  __shared__ float hs[MAX_BASIS];
+  for (int j = threadIdx.x; j < k; j += VT) hs[j] = (float)h[j];
+  __syncthreads();
+  float ss = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
+    float acc = w[i];
+    int j = 0;
+    for (; j + 8 <= k; j += 8) {
+      float v[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) v[t] = V[(int64_t)(j + t) * ld + i];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) acc = fmaf(-hs[j + t], v[t], acc);
+    }
+    for (; j < k; ++j) acc = fmaf(-hs[j], V[(int64_t)j * ld + i], acc);
+    w[i] = acc;
+    ss = fmaf(acc, acc, ss);
+  }
+  double sd = (double)ss;
+  for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sd;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w2 = 0; w2 < VT / 32; ++w2) t += red[w2];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// x += sum_j y[j] V[j] (FP32 combination, FP64 accumulate into x)
+__global__ void __launch_bounds__(VT) xupdate32_kernel(double* __restrict__ x, const float* __restrict__ V, int64_t ld,
+                                                       int k, const double* __restrict__ y, int64_t n) {
+  __shared__ float ys[MAX_BASIS];
+  for (int j = threadIdx.x; j < k; j += VT) ys[j] = (float)y[j];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
+    float s = 0.f;
+    for (int j = 0; j < k; ++j) s = fmaf(ys[j], V[(int64_t)j * ld + i], s);
+    x[i] += (double)s;
+  }
+}
+
+// y = (float)(a * x)
+__global__ void scale_to_f32_kernel(double a, const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (float)(a * x[i]);
+}
+// y = a * x (FP32)
+__global__ void scale32_kernel(float a, const float* __restrict__ x, float* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i];
+}
+// y = (double)x
+__global__ void widen_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+// w = (float)(a - b)
+__global__ void diff_to_f32_kernel(const double* __restrict__ a, const double* __restrict__ b, float* __restrict__ w,
+                                   int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = (float)(a[i] - b[i]);
 }
 
 // y = a*x + b*y
@@ -275,11 +388,142 @@ struct Solver {
     return OBTE_OK;
   }
 
+  // Restarted GMRES with the FP32 basis (see multidot32_kernel); same contract as gmres().
+  obte_status gmres32(const double* rhs, double* x, double tol_rel, double tol_abs, double& res_out, bool& ok) {
+    const int64_t n = wk.nu;
+    const int m = wk.restart;
+    if (!wk.V32.p) {
+      OBTE_TRY(wk.V32.alloc((size_t)n * (m + 1) * sizeof(float)));
+      OBTE_TRY(wk.w32.alloc((size_t)n * sizeof(float)));
+    }
+    float* V = wk.V32.as<float>();
+    float* w = wk.w32.as<float>();
+    double* vj64 = wk.w.as<double>();
+    double* r = wk.r.as<double>();
+    const int nb = wk.nb;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), h, h2;
+    ok = false;
+    OBTE_TRY(residual(true, rhs, x, r));
+    double beta;
+    OBTE_TRY(norm(r, beta));
+    res_out = beta;
+    auto dots = [&](int k, bool self, std::vector<double>& out) -> obte_status {
+      const int kk = k + (self ? 1 : 0);
+      multidot32_kernel<<<nb, VT, 0, st>>>(V, n, k, self ? 1 : 0, w, n, wk.partial.as<double>());
+      reduce_partials_kernel<<<kk, VT, 0, st>>>(wk.partial.as<double>(), nb, kk, wk.hdev.as<double>());
+      count_launch(2);
+      OBTE_CUDA(cudaGetLastError());
+      out.resize(kk);
+      OBTE_CUDA(cudaMemcpyAsync(out.data(), wk.hdev.p, kk * sizeof(double), cudaMemcpyDeviceToHost, st));
+      OBTE_CUDA(cudaStreamSynchronize(st));
+      return OBTE_OK;
+    };
+    auto project = [&](int k, const std::vector<double>& coef, double& nrm) -> obte_status {
+      OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, coef.data(), k * sizeof(double), cudaMemcpyHostToDevice, st));
+      update32_kernel<<<nb, VT, 0, st>>>(w, V, n, k, wk.hdev.as<double>(), n, wk.partial.as<double>());
+      reduce_partials_kernel<<<1, VT, 0, st>>>(wk.partial.as<double>(), nb, 1, wk.sdev.as<double>());
+      count_launch(2);
+      OBTE_CUDA(cudaGetLastError());
+      double ss;
+      OBTE_CUDA(cudaMemcpyAsync(&ss, wk.sdev.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+      OBTE_CUDA(cudaStreamSynchronize(st));
+      nrm = std::sqrt(std::max(ss, 0.0));
+      return OBTE_OK;
+    };
+    while (true) {
+      double xn;
+      OBTE_TRY(norm(x, xn));
+      const double tol = std::max(tol_abs, tol_rel * std::max(xn, beta));
+      if (beta <= tol) { ok = true; return OBTE_OK; }
+      if (sweeps >= max_sweeps) return OBTE_OK;
+      scale_to_f32_kernel<<<nb, VT, 0, st>>>(1.0 / beta, r, V, n);
+      count_launch();
+      std::fill(g.begin(), g.end(), 0.0);
+      g[0] = beta;
+      int j = 0;
+      double est = beta;
+      for (; j < m && sweeps < max_sweeps; ++j) {
+        const auto w0 = std::chrono::steady_clock::now();
+        if (trace) cudaEventRecord(ev[0], st);
+        widen_kernel<<<nb, VT, 0, st>>>(V + (int64_t)j * n, vj64, n);
+        count_launch();
+        OBTE_TRY(sweep(true, vj64, wk.tmp.as<double>(), false));
+        if (trace) cudaEventRecord(ev[1], st);
+        diff_to_f32_kernel<<<nb, VT, 0, st>>>(vj64, wk.tmp.as<double>(), w, n);
+        count_launch();
+        OBTE_CUDA(cudaGetLastError());
+        // classical Gram-Schmidt with one conditional re-orthogonalisation (as in gmres())
+        OBTE_TRY(dots(j + 1, true, h));
+        const double wn0 = std::sqrt(std::max(h[j + 1], 0.0));
+        h.resize(j + 1);
+        double hn;
+        OBTE_TRY(project(j + 1, h, hn));
+        if (hn < 0.7 * wn0) {
+          OBTE_TRY(dots(j + 1, false, h2));
+          OBTE_TRY(project(j + 1, h2, hn));
+          for (int i = 0; i <= j; ++i) h[i] += h2[i];
+        }
+        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = h[i];
+        H[(size_t)(j + 1) * m + j] = hn;
+        for (int i = 0; i < j; ++i) {
+          const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
+          H[(size_t)i * m + j] = cs[i] * a + sn[i] * b;
+          H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+        }
+        const double a = H[(size_t)j * m + j], b = H[(size_t)(j + 1) * m + j];
+        const double rr = std::hypot(a, b);
+        cs[j] = rr > 0 ? a / rr : 1.0;
+        sn[j] = rr > 0 ? b / rr : 0.0;
+        H[(size_t)j * m + j] = rr;
+        H[(size_t)(j + 1) * m + j] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        est = std::fabs(g[j + 1]);
+        if (hn > 0) {
+          scale32_kernel<<<nb, VT, 0, st>>>((float)(1.0 / hn), w, V + (int64_t)(j + 1) * n, n);
+          count_launch();
+        }
+        if (trace) {
+          cudaEventRecord(ev[2], st);
+          cudaEventSynchronize(ev[2]);
+          float ta = 0, tb = 0;
+          cudaEventElapsedTime(&ta, ev[0], ev[1]);
+          cudaEventElapsedTime(&tb, ev[1], ev[2]);
+          t_sweep += ta;
+          t_gs += tb;
+          t_wall += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+          ++t_iters;
+        }
+        if (est <= tol || hn == 0) { ++j; break; }
+      }
+      std::vector<double> y(j, 0.0);
+      for (int i = j - 1; i >= 0; --i) {
+        double acc = g[i];
+        for (int k = i + 1; k < j; ++k) acc -= H[(size_t)i * m + k] * y[k];
+        y[i] = H[(size_t)i * m + i] != 0 ? acc / H[(size_t)i * m + i] : 0.0;
+      }
+      if (j > 0) {
+        OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, st));
+        xupdate32_kernel<<<nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n);
+        count_launch();
+        OBTE_CUDA(cudaGetLastError());
+      }
+      OBTE_TRY(residual(true, rhs, x, r));
+      OBTE_TRY(norm(r, beta));
+      res_out = beta;
+      if (beta <= tol) { ok = true; return OBTE_OK; }
+      if (sweeps >= max_sweeps) return OBTE_OK;
+    }
+  }
+
   // Restarted GMRES on (I - K) x = rhs, FP64 vectors, sweeps in the given precision.
   // Stops when the residual norm <= max(tol_abs, tol_rel * scale) with scale = max(‖x‖, ‖r‖)
   // taken at each (re)start, or when the sweep cap is hit.
   obte_status gmres(bool fp32, const double* rhs, double* x, double tol_rel, double tol_abs, double& res_out,
                     bool& ok) {
+    // stages with FP32 sweeps and a tolerance no tighter than 1e-6 run on the FP32 basis
+    if (fp32 && !std::getenv("OBTE_FP64_BASIS") && (tol_rel >= 1e-6 || (tol_rel == 0 && tol_abs > 0)))
+      return gmres32(rhs, x, tol_rel, tol_abs, res_out, ok);
     const int64_t n = wk.nu;
     const int m = wk.restart;
     double* V = wk.V.as<double>();
@@ -406,7 +650,7 @@ static obte_status alloc_work(obte_plan plan, Work& wk, int restart) {
 int64_t solve_scratch_bytes(obte_plan plan, int restart) {
   const Schedule& s = plan->sched;
   const int64_t vb = plan->nu * (int64_t)sizeof(double);
-  return vb * (6 + restart + 1) + (int64_t)s.n * s.ds * 8 + 2LL * s.n_mfp * s.n_dir * 8 +
+  return vb * (6 + restart + 1) + plan->nu * 4LL * (restart + 2) + (int64_t)s.n * s.ds * 8 + 2LL * s.n_mfp * s.n_dir * 8 +
          (int64_t)plan->ctx->num_sms * 4 * (restart + 1) * 8;
 }
 
