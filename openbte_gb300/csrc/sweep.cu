@@ -365,7 +365,9 @@ __device__ __forceinline__ double recip(double x) {
 //   [128, ...) nbuf x records | nbuf x values | nbuf x wall weights | nbuf x prefetch lists | sig | K S | ring
 // nbuf = TMA pipeline depth: unit u + nbuf - 1 is issued while unit u runs (at most kMaxBuf mbarriers)
 static constexpr int kMaxBuf = 8;
-static constexpr int kDefaultBuf = 3;
+// 2 units staged: measured 2.19 ms per FP32 sweep on the 60k-triangle benchmark against 2.46 ms with 3
+// (the smaller staging area lets 6 instead of 5 CTAs share an SM); deeper pipelines were no faster.
+static constexpr int kDefaultBuf = 2;
 
 template <typename Real>
 struct SmemLayout {
