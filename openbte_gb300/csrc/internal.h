@@ -179,10 +179,10 @@ obte_status build_schedule(const obte_problem* prob, const obte_material* mat, S
 struct DevSchedule {
   bool ready = false;
   int G = 1, mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;   // G lanes per element, mcp MFPs per CTA
-  int emax = 0, unit_wo = 0, pf_pad = 0;   // periodic bank rows, per-unit staging sizes
+  int emax = 0, unit_wo = 0, pf_pad = 0, unit_sx = 0;   // periodic bank rows, per-unit staging sizes
   int nbuf = 2;                            // TMA pipeline depth
   size_t smem = 0;
-  DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, mfp, tco, sig, wo_wall, wo_geo, kcoef, scoef, hs, vals, cellmap,
+  DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, sx, ksx, mfp, tco, sig, wo_wall, wo_geo, kcoef, scoef, hs, vals, cellmap,
       Pq, si, sr, wo_off, spec;
   size_t bytes() const;
 };

@@ -47,15 +47,19 @@ namespace obte {
 static constexpr int kUnit = 128;      // elements per level unit = threads per CTA
 
 // ---- packed element records -------------------------------------------------------
-// Integer words (both precisions), ring rows and indices in 16-bit halves:
-//   w0 cell | w1 so, s0 | w2 s1, s2 | w3 s3, xk+1 | w4 wout | w5 contact+1
-// then the reals c0 c1 c2 c3 D:  FP32 words 6..10 (+1 pad) = 12 words (48 B);
-//                                FP64 words 6..15          = 16 words (64 B).
-// so = output row, s* = inflow rows, xk = periodic source index, wout = wall re-emission
-// entries (begin << 3 | count, begin relative to the direction), contact = kappa entry.
-template <typename Real> struct Rec;
-template <> struct Rec<float> { static constexpr int W = 12, COEF = 6, CSTEP = 1, D = 10; };
-template <> struct Rec<double> { static constexpr int W = 16, COEF = 6, CSTEP = 2, D = 14; };
+// 32-bit words, ring rows in 16-bit halves:
+//   w0 cell | w1 so, s0 | w2 s1, s2 | w3 s3, sp | the reals c0 .. c(NF-1), D | padding to 16 B
+// so = output row, s* = inflow rows (s3 only for NF = 4), sp = 1 + index of the element's output entry
+// among its unit's entries (0: no per-MFP outputs).  Triangles: 32 B (FP32) / 48 B (FP64);
+// tetrahedra: 48 B / 64 B.  Output entries (int4: periodic source index xk, wall re-emission entries
+// (begin << 3 | count, begin relative to the direction), contact entry, 0) are a separate per-unit table.
+__host__ __device__ constexpr int rec_words(int real_bytes, int nf) {
+  return ((4 + (nf + 1) * (real_bytes / 4)) + 3) & ~3;
+}
+template <typename Real, int NF> struct Rec {
+  static constexpr int CSTEP = sizeof(Real) / 4, COEF = 4, D = COEF + NF * CSTEP;
+  static constexpr int W = rec_words(sizeof(Real), NF);
+};
 
 // special-element table
 //   si: xk wout contact nwall w0 w1 w2 pad     (8 ints)
@@ -92,6 +96,8 @@ struct Packed {
   // element then face order), each unit's list padded with -1 to a multiple of 4 ints; kpf[u] is the
   // absolute start of unit u's list (n[q] + 1 entries per direction, indexed like Units::ptr)
   std::vector<int32_t> pf, kpf;
+  std::vector<int32_t> sx, ksx;  // output entries (4 ints each) in sweep order; first entry of unit u
+  int unit_sx = 0;               // most output entries in one unit
   std::vector<int32_t> kwo;   // first wall re-emission entry of unit u, relative to the direction
   int emax = 0;               // most cut inflow faces in one unit
   int pf_pad = 0;             // longest padded list
@@ -106,28 +112,34 @@ static int ring_rows(const Schedule& s, int emax) { return s.max_slots + 2 + 2 *
 // (at CTA start for unit 0) from the state vector.
 template <typename Real>
 static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
-  constexpr int W = Rec<Real>::W;
+  const int W = rec_words(sizeof(Real), s.nf);
+  constexpr int CSTEP = sizeof(Real) / 4, COEF = 4;
   const int S = s.max_slots;
   const int zero_row = S, trash_row = S + 1, prow0 = S + 2;
   // pass 1: per-unit counts of cut inflow faces and wall re-emission entries
-  pk.emax = pk.pf_pad = pk.unit_wo = 0;
+  pk.emax = pk.pf_pad = pk.unit_wo = pk.unit_sx = 0;
   pk.kwo.assign(un.ptr.size(), 0);
   pk.kpf.assign(un.ptr.size(), 0);
-  int64_t n_pf = 0;
+  pk.ksx.assign(un.ptr.size(), 0);
+  int64_t n_pf = 0, n_sx = 0;
   for (int q = 0; q < s.n_dir; ++q) {
     const int32_t* up = un.ptr.data() + un.off[q];
     int32_t wo_run = 0;
     for (int u = 0; u < un.n[q]; ++u) {
-      int cnt = 0, wcnt = 0;
+      int cnt = 0, wcnt = 0, scnt = 0;
       for (int32_t pos = up[u]; pos < up[u + 1]; ++pos) {
         const size_t it = (size_t)q * s.n + pos;
         for (int f = 0; f < s.nf; ++f)
           if ((int)((uint32_t)s.in_idx[it * s.nf + f] >> ITEM_SHIFT) == ITEM_PERIODIC) ++cnt;
         wcnt += s.wout[it] & 7;
+        scnt += (s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0) ? 1 : 0;
       }
       const int padded = (cnt + 3) & ~3;
       pk.kwo[un.off[q] + u] = wo_run;
       pk.kpf[un.off[q] + u] = (int32_t)n_pf;
+      pk.ksx[un.off[q] + u] = (int32_t)n_sx;
+      n_sx += scnt;
+      pk.unit_sx = std::max(pk.unit_sx, scnt);
       wo_run += wcnt;
       n_pf += padded;
       pk.emax = std::max(pk.emax, cnt);
@@ -136,12 +148,16 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
     }
     pk.kwo[un.off[q] + un.n[q]] = wo_run;
     pk.kpf[un.off[q] + un.n[q]] = (int32_t)n_pf;
+    pk.ksx[un.off[q] + un.n[q]] = (int32_t)n_sx;
     if (wo_run != s.wo_off[q + 1] - s.wo_off[q]) {
       set_error("wall re-emission entries are not in sweep order");
       return OBTE_ERR_BAD_ARG;
     }
   }
-  if (n_pf >= (int64_t)1 << 31) { set_error("too many periodic inflow faces"); return OBTE_ERR_UNSUPPORTED; }
+  if (n_pf >= (int64_t)1 << 31 || n_sx >= (int64_t)1 << 31) {
+    set_error("too many periodic inflow faces or output entries"); return OBTE_ERR_UNSUPPORTED;
+  }
+  pk.sx.assign((size_t)std::max<int64_t>(n_sx, 1) * 4, 0);
   pk.rows = ring_rows(s, pk.emax);
   if (pk.rows >= 65535 || s.max_src >= (1 << 30)) {
     set_error("sweep ring rows do not fit 16-bit indices");
@@ -159,17 +175,15 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
   for (int q = 0; q < s.n_dir; ++q) {
     const int32_t* up = un.ptr.data() + un.off[q];
     for (int u = 0; u < un.n[q]; ++u) {
-      int ent = 0;
+      int ent = 0, sent = 0;
       const int bank = prow0 + (u & 1) * pk.emax;
       int32_t* plist = pk.pf.data() + pk.kpf[un.off[q] + u];
+      int32_t* slist = pk.sx.data() + (size_t)pk.ksx[un.off[q] + u] * 4;
       for (int32_t pos = up[u]; pos < up[u + 1]; ++pos) {
         const size_t it = (size_t)q * s.n + pos;
         int32_t* r = pk.rec.data() + it * W;
         const int32_t so = s.slot[it] >= 0 ? s.slot[it] : trash_row;
         r[0] = s.cell[it];
-        // wall re-emission entries: begin relative to the direction's first entry
-        r[4] = s.wout[it] ? (((s.wout[it] >> 3) - s.wo_off[q]) << 3) | (s.wout[it] & 7) : 0;
-        r[5] = s.contact[it] + 1;
         pk.cellmap[it] = s.cell[it];
         pk.P[it] = s.P[it];
         int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0};
@@ -206,25 +220,30 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
             special = true;
           }
         }
+        int sp = 0;
+        if (outputs) {
+          // wall re-emission entries: begin relative to the direction's first entry
+          int32_t* e = slist + (size_t)sent * 4;
+          e[0] = s.xk[it];
+          e[1] = s.wout[it] ? (((s.wout[it] >> 3) - s.wo_off[q]) << 3) | (s.wout[it] & 7) : 0;
+          e[2] = s.contact[it];
+          e[3] = 0;
+          sp = ++sent;
+        }
         r[1] = (so & 0xFFFF) | (row_in[0] << 16);
         r[2] = (row_in[1] & 0xFFFF) | (row_in[2] << 16);
-        r[3] = (row_in[3] & 0xFFFF) | ((s.xk[it] + 1) << 16);
+        r[3] = (row_in[3] & 0xFFFF) | (sp << 16);
         if (special) {
           pk.spec[it] = (int32_t)(pk.si.size() / SI);
           pk.si.insert(pk.si.end(), si, si + SI);
           pk.sr.insert(pk.sr.end(), sr, sr + SR);
         }
-        if (sizeof(Real) == 4) {
-          for (int f = 0; f < 4; ++f) {
-            float v = (float)coef[f];
-            std::memcpy(&r[Rec<float>::COEF + f], &v, 4);
-          }
-          float d = (float)s.D[it];
-          std::memcpy(&r[Rec<float>::D], &d, 4);
-        } else {
-          for (int f = 0; f < 4; ++f) std::memcpy(&r[Rec<double>::COEF + 2 * f], &coef[f], 8);
-          std::memcpy(&r[Rec<double>::D], &s.D[it], 8);
+        for (int f = 0; f < s.nf; ++f) {
+          const Real v = (Real)coef[f];
+          std::memcpy(&r[COEF + f * CSTEP], &v, sizeof(Real));
         }
+        const Real dv = (Real)s.D[it];
+        std::memcpy(&r[COEF + s.nf * CSTEP], &dv, sizeof(Real));
       }
     }
   }
@@ -321,6 +340,9 @@ struct SweepParams {
   const int32_t* __restrict__ kwo;       // first wall entry of each unit (relative to the direction)
   const int32_t* __restrict__ kpf;       // start of each unit's prefetch list in pf
   const int32_t* __restrict__ pf;        // periodic source index per cut inflow face (-1 = padding)
+  const int32_t* __restrict__ ksx;       // first output entry of each unit (absolute)
+  const int32_t* __restrict__ sx;        // output entries: xk, wall entries, contact, 0
+  int unit_sx;                           // most output entries in one unit
   const int64_t* __restrict__ x_base;
   const int32_t* __restrict__ wo_off;   // [n_dir+1] first wall-output entry of each direction
   const int32_t* __restrict__ wo_wall;
@@ -371,19 +393,22 @@ static constexpr int kDefaultBuf = 2;
 
 template <typename Real>
 struct SmemLayout {
-  size_t rec, val, gg, pfl, rec_stride, val_stride, gg_stride, pf_stride, sig, kacc, sacc, ring, total;
-  __host__ __device__ SmemLayout(int mcp, int rows, int unit_wo, int pf_pad, int nbuf) {
-    constexpr int W = Rec<Real>::W;
+  size_t rec, val, gg, pfl, sxo, rec_stride, val_stride, gg_stride, pf_stride, sx_stride, sig, kacc, sacc, ring,
+      total;
+  __host__ __device__ SmemLayout(int nf, int mcp, int rows, int unit_wo, int pf_pad, int unit_sx, int nbuf) {
+    const int W = rec_words(sizeof(Real), nf);
     size_t o = 128;
     rec_stride = (size_t)kUnit * W * 4;
     val_stride = (size_t)(kUnit + 2) * 2 * sizeof(Real);
     val_stride = (val_stride + 15) & ~(size_t)15;
     gg_stride = (size_t)unit_wo * 4 * sizeof(Real);        // 4 Reals per wall entry (16-B multiple)
     pf_stride = (size_t)pf_pad * 4;                        // pf_pad is a multiple of 4
+    sx_stride = (size_t)unit_sx * 16;                      // output entries, int4 each
     rec = o; o += nbuf * rec_stride;
     val = o; o += nbuf * val_stride;
     gg = o; o += nbuf * gg_stride;
     pfl = o; o += nbuf * pf_stride;
+    sxo = o; o += nbuf * sx_stride;
     sig = o; o += (size_t)mcp * 3 * sizeof(Real);
     kacc = o; o += (size_t)mcp * sizeof(Real);
     sacc = o; o += (size_t)mcp * sizeof(Real);
@@ -427,14 +452,14 @@ __device__ __forceinline__ T group_sum(T v, unsigned mask) {
 // 16-byte shared load per lane and a group of 8 reads one full 128-byte row.
 template <typename Real, int NF, int G, bool FINAL>
 __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<Real> p) {
-  constexpr int RW = Rec<Real>::W;               // record words
+  constexpr int RW = Rec<Real, NF>::W;           // record words
   constexpr int KV = V16<Real>::K;               // MFPs per lane
   constexpr int MC = G * KV;                     // MFPs per CTA
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
   extern __shared__ __align__(128) unsigned char smem[];
   const int rows = p.rows;
   const int nbuf = p.nbuf;
-  const SmemLayout<Real> L(MC, rows, p.unit_wo, p.pf_pad, nbuf);
+  const SmemLayout<Real> L(NF, MC, rows, p.unit_wo, p.pf_pad, p.unit_sx, nbuf);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   int* s_abort = reinterpret_cast<int*>(smem + 64);
   Real* s_k = reinterpret_cast<Real*>(smem + L.kacc);
@@ -453,6 +478,7 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
   const int32_t* __restrict__ lev = p.lev_ptr + p.lev_off[q];
   const int32_t* __restrict__ kwo = p.kwo + p.lev_off[q];
   const int32_t* __restrict__ kpf = p.kpf + p.lev_off[q];
+  const int32_t* __restrict__ ksx = p.ksx + p.lev_off[q];
   const int nlev = p.nlev[q];
   const int32_t* __restrict__ rec_q = p.rec + (int64_t)q * p.n * RW;
   // values: absolute byte offsets from the (256-B aligned) array base keep every TMA window 16-B aligned
@@ -514,13 +540,16 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
     const unsigned gbytes = (unsigned)(w1 - w0) * 4u * (unsigned)sizeof(Real);
     const int f0 = u + 1 < nlev ? kpf[u + 1] : 0, f1 = u + 1 < nlev ? kpf[u + 2] : 0;
     const unsigned pbytes = (unsigned)(f1 - f0) * 4u;
+    const int x0 = ksx[u], x1 = ksx[u + 1];
+    const unsigned sbytes = (unsigned)(x1 - x0) * 16u;
     uint64_t* bar = &bars[bi];
     fence_proxy_async();
-    mbar_expect_tx(bar, rbytes + vbytes + gbytes + pbytes);
+    mbar_expect_tx(bar, rbytes + vbytes + gbytes + pbytes + sbytes);
     tma_load_1d(smem + L.rec + bi * L.rec_stride, rec_q + (int64_t)a * RW, rbytes, bar);
     tma_load_1d(smem + L.val + bi * L.val_stride, val_base + vb0, vbytes, bar);
     if (gbytes) tma_load_1d(smem + L.gg + bi * L.gg_stride, gg_q + (int64_t)w0 * 4, gbytes, bar);
     if (pbytes) tma_load_1d(smem + L.pfl + bi * L.pf_stride, p.pf + f0, pbytes, bar);
+    if (sbytes) tma_load_1d(smem + L.sxo + bi * L.sx_stride, p.sx + (int64_t)x0 * 4, sbytes, bar);
   };
   if (tid == 0)
     for (int u = 0; u < nbuf - 1 && u < nlev; ++u) issue(u, u);
@@ -564,13 +593,18 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
         const int c = r[0];
         const int so = r[1] & 0xFFFF, s0 = (int)((unsigned)r[1] >> 16);
         const int s1 = r[2] & 0xFFFF, s2 = (int)((unsigned)r[2] >> 16);
-        const int s3 = r[3] & 0xFFFF, xk = (int)((unsigned)r[3] >> 16) - 1;
-        const int wo = r[4], ce = r[5] - 1;
-        const Real c0 = word_real<Real>(r, Rec<Real>::COEF);
-        const Real c1 = word_real<Real>(r, Rec<Real>::COEF + Rec<Real>::CSTEP);
-        const Real c2 = word_real<Real>(r, Rec<Real>::COEF + 2 * Rec<Real>::CSTEP);
-        const Real c3 = word_real<Real>(r, Rec<Real>::COEF + 3 * Rec<Real>::CSTEP);
-        const Real D = word_real<Real>(r, Rec<Real>::D);
+        const int s3 = r[3] & 0xFFFF, sp = (int)((unsigned)r[3] >> 16);
+        int xk = -1, wo = 0, ce = -1;
+        if (sp) {
+          const int4 ent = reinterpret_cast<const int4*>(smem + L.sxo + bi * L.sx_stride)[sp - 1];
+          xk = ent.x; wo = ent.y; ce = ent.z;
+        }
+        using RR = Rec<Real, NF>;
+        const Real c0 = word_real<Real>(r, RR::COEF);
+        const Real c1 = word_real<Real>(r, RR::COEF + RR::CSTEP);
+        const Real c2 = word_real<Real>(r, RR::COEF + 2 * RR::CSTEP);
+        const Real c3 = NF > 3 ? word_real<Real>(r, RR::COEF + 3 * RR::CSTEP) : Real(0);
+        const Real D = word_real<Real>(r, RR::D);
         Real v0[KV], v1[KV], v2[KV], v3[KV];
         vload(ring + (size_t)s0 * MC + mo, v0);
         vload(ring + (size_t)s1 * MC + mo, v1);
@@ -686,7 +720,7 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
 // ---- table upload ---------------------------------------------------------------
 
 size_t DevSchedule::bytes() const {
-  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &kwo, &kpf, &pf, &mfp, &tco, &sig, &wo_wall, &wo_geo,
+  const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &kwo, &kpf, &pf, &sx, &ksx, &mfp, &tco, &sig, &wo_wall, &wo_geo,
                          &kcoef, &scoef, &hs, &vals, &cellmap, &Pq, &si, &sr, &wo_off, &spec};
   size_t b = 0;
   for (auto* x : all) b += x->bytes;
@@ -709,15 +743,16 @@ static constexpr int kGroups[] = {1, 2, 4, 8};
 // barriers and more, smaller CTAs per SM keep more chains in flight.  Larger groups stay available
 // through OBTE_SWEEP_G (tuning); a size whose shared memory does not fit is skipped.
 template <typename Real>
-static int choose_group(const Schedule& s, int rows, int unit_wo, int pf_pad, int nbuf, int num_sms, size_t optin) {
-  (void)s; (void)num_sms;
+static int choose_group(const Schedule& s, int rows, int unit_wo, int pf_pad, int unit_sx, int nbuf, int num_sms,
+                        size_t optin) {
+  (void)num_sms;
   const char* env = std::getenv("OBTE_SWEEP_G");
   const int forced = env ? std::atoi(env) : 1;
   for (int G : kGroups) {
     if (G != forced) continue;
-    if (SmemLayout<Real>(G * V16<Real>::K, rows, unit_wo, pf_pad, nbuf).total <= optin) return G;
+    if (SmemLayout<Real>(s.nf, G * V16<Real>::K, rows, unit_wo, pf_pad, unit_sx, nbuf).total <= optin) return G;
   }
-  return SmemLayout<Real>(V16<Real>::K, rows, unit_wo, pf_pad, nbuf).total <= optin ? 1 : 0;
+  return SmemLayout<Real>(s.nf, V16<Real>::K, rows, unit_wo, pf_pad, unit_sx, nbuf).total <= optin ? 1 : 0;
 }
 
 template <typename Real>
@@ -736,7 +771,8 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   const int rows = pk.rows;
   const char* nb_env = std::getenv("OBTE_SWEEP_NBUF");
   const int nbuf = nb_env ? std::max(2, std::min(kMaxBuf, std::atoi(nb_env))) : kDefaultBuf;
-  const int G = choose_group<Real>(s, rows, pk.unit_wo, pk.pf_pad, nbuf, plan->ctx->num_sms, plan->ctx->smem_optin);
+  const int G = choose_group<Real>(s, rows, pk.unit_wo, pk.pf_pad, pk.unit_sx, nbuf, plan->ctx->num_sms,
+                                   plan->ctx->smem_optin);
   if (!G) {
     set_error("sweep front needs more shared memory than one CTA can have (" + std::to_string(rows) + " rows)");
     return OBTE_ERR_UNSUPPORTED;
@@ -752,7 +788,8 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   d.unit_wo = pk.unit_wo;
   d.pf_pad = pk.pf_pad;
   d.nbuf = nbuf;
-  d.smem = SmemLayout<Real>(mcp, rows, pk.unit_wo, pk.pf_pad, nbuf).total;
+  d.unit_sx = pk.unit_sx;
+  d.smem = SmemLayout<Real>(s.nf, mcp, rows, pk.unit_wo, pk.pf_pad, pk.unit_sx, nbuf).total;
   OBTE_TRY(upload(d.rec, pk.rec, st));
   OBTE_TRY(upload(d.cellmap, pk.cellmap, st));
   OBTE_TRY(upload(d.Pq, pk.P, st));
@@ -765,6 +802,8 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   OBTE_TRY(upload(d.kwo, pk.kwo, st));
   OBTE_TRY(upload(d.kpf, pk.kpf, st));
   OBTE_TRY(upload(d.pf, pk.pf, st));
+  OBTE_TRY(upload(d.sx, pk.sx, st));
+  OBTE_TRY(upload(d.ksx, pk.ksx, st));
   std::vector<int32_t> wo = s.wo_wall;
   if (wo.empty()) wo.push_back(0);
   OBTE_TRY(upload(d.wo_wall, wo, st));
@@ -831,6 +870,7 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.rec = d.rec.as<int32_t>(); p.vals = d.vals.as<Real>();
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
   p.kwo = d.kwo.as<int32_t>(); p.kpf = d.kpf.as<int32_t>(); p.pf = d.pf.as<int32_t>();
+  p.ksx = d.ksx.as<int32_t>(); p.sx = d.sx.as<int32_t>(); p.unit_sx = d.unit_sx;
   p.x_base = plan->x_base_dev.as<int64_t>();
   p.wo_off = d.wo_off.as<int32_t>();
   p.wo_wall = d.wo_wall.as<int32_t>();
@@ -959,6 +999,7 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.rec = d.rec.as<int32_t>(); p.vals = vals;
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
   p.kwo = d.kwo.as<int32_t>(); p.kpf = d.kpf.as<int32_t>(); p.pf = d.pf.as<int32_t>();
+  p.ksx = d.ksx.as<int32_t>(); p.sx = d.sx.as<int32_t>(); p.unit_sx = d.unit_sx;
   p.x_base = plan->x_base_dev.as<int64_t>();
   p.wo_off = d.wo_off.as<int32_t>();
   p.wo_wall = d.wo_wall.as<int32_t>();
