@@ -16,6 +16,8 @@
 // residual every few iterations.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -367,6 +369,14 @@ struct obte_fourier_plan_s {
       k_e1, k_e2, k_coef, kap;
   // work
   obte::DevBuf C, rhs, r, z, p, Ap, part, part2, part3, sc, grad, tmp, kout, pmx, pmn;
+  // CG iterations between two convergence checks as one CUDA graph (captured per solution pointer)
+  cudaStream_t capture_stream = nullptr;
+  cudaGraphExec_t cg_exec = nullptr;
+  const double* cg_exec_T = nullptr;
+  ~obte_fourier_plan_s() {
+    if (cg_exec) cudaGraphExecDestroy(cg_exec);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+  }
 };
 
 using namespace obte;
@@ -567,6 +577,7 @@ extern "C" obte_status obte_fourier_plan_create(obte_context ctx, const obte_fou
 }
 
 extern "C" obte_status obte_fourier_plan_destroy(obte_fourier_plan plan) {
+  if (plan && plan->ctx) cudaStreamSynchronize(plan->ctx->stream);
   delete plan;
   return OBTE_OK;
 }
@@ -596,21 +607,39 @@ static obte_status cg_solve(obte_fourier_plan P, double* T, double rtol, int max
     const double tol = rtol * std::max(std::sqrt(std::max(hs[5], 0.0)), 1e-300);
     iters = 0;
     if (std::sqrt(std::max(hs[3], 0.0)) <= tol) return OBTE_OK;
-    // three launches per iteration; rz alternates between sc[0] and sc[1]
+    // three launches per iteration; rz alternates between sc[0] and sc[1].  At a few microseconds of work
+    // per launch the loop is launch-bound, so the `check` iterations between two convergence tests are
+    // captured once as a CUDA graph (on a private stream: capture is not allowed on the legacy default
+    // stream) and replayed on the plan's stream.  `check` is even, so every block starts with cur = 0.
     const int check = 8;
-    int cur = 0;
     double* pp = P->part.as<double>();
     double* prz = P->part2.as<double>();
     double* prr = P->part3.as<double>();
-    while (iters < max_iter) {
+    auto enqueue = [&](cudaStream_t s2) {
       for (int k = 0; k < check; ++k) {
-        spmv_kernel<<<nb, FT, 0, st>>>(n, rp, ci, val, p, Ap, pp);
-        cg_step_kernel<<<nb, FT, 0, st>>>(n, pp, nb, sc, cur, T, r, z, p, Ap, P->dinv.as<double>(), prz, prr);
-        cg_dir_kernel<<<nb, FT, 0, st>>>(n, prz, prr, nb, sc, cur, p, z);
-        count_launch(3);
-        cur ^= 1;
-        ++iters;
+        const int cur = k & 1;
+        spmv_kernel<<<nb, FT, 0, s2>>>(n, rp, ci, val, p, Ap, pp);
+        cg_step_kernel<<<nb, FT, 0, s2>>>(n, pp, nb, sc, cur, T, r, z, p, Ap, P->dinv.as<double>(), prz, prr);
+        cg_dir_kernel<<<nb, FT, 0, s2>>>(n, prz, prr, nb, sc, cur, p, z);
       }
+    };
+    if (P->cg_exec_T != T && !std::getenv("OBTE_NO_GRAPHS")) {
+      if (P->cg_exec) { cudaGraphExecDestroy(P->cg_exec); P->cg_exec = nullptr; }
+      if (!P->capture_stream) OBTE_CUDA(cudaStreamCreateWithFlags(&P->capture_stream, cudaStreamNonBlocking));
+      cudaGraph_t g = nullptr;
+      OBTE_CUDA(cudaStreamBeginCapture(P->capture_stream, cudaStreamCaptureModeThreadLocal));
+      enqueue(P->capture_stream);
+      OBTE_CUDA(cudaStreamEndCapture(P->capture_stream, &g));
+      const cudaError_t e = cudaGraphInstantiate(&P->cg_exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+      P->cg_exec_T = T;
+    }
+    while (iters < max_iter) {
+      if (P->cg_exec && P->cg_exec_T == T) OBTE_CUDA(cudaGraphLaunch(P->cg_exec, st));
+      else enqueue(st);
+      count_launch(3 * check);
+      iters += check;
       OBTE_CUDA(cudaGetLastError());
       OBTE_CUDA(cudaMemcpyAsync(hs, sc, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
       OBTE_CUDA(cudaStreamSynchronize(st));
