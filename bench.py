@@ -308,6 +308,33 @@ def run_inverse(args, dev):
         "gpu_launches": int(round(launches)),
         "clocks": clk.summary(),
     }
+    if args.fd_pixels > 0:
+        # adjoint gradient against central differences on seeded random pixels.  The solves are refined to
+        # 1e-12 (a step of h = 1e-3 moves kappa by ~1e-4 relative, so kappa must be far more accurate than the
+        # 1e-4 bar); pixels are drawn where rho - h > 0 and rho + h <= 1 keep the transmission in (0, 1].
+        fd_solver = PixelSolver(n, mat, size=100.0, precision="fp32_refine", rtol=1e-12, restart=100)
+        k0, g0 = fd_solver.kappa_and_gradient(rho)
+        g0 = g0.cpu().numpy()
+        h = 1e-3
+        ok = np.nonzero((rho >= 2 * h) & (rho <= 1 - h))[0]
+        pix = np.random.default_rng(123).choice(ok, args.fd_pixels, replace=False)
+        fds = []
+        for pi in pix:
+            r1, r2 = rho.copy(), rho.copy()
+            r1[pi] += h
+            r2[pi] -= h
+            fds.append((fd_solver.kappa_and_gradient(r1)[0] - fd_solver.kappa_and_gradient(r2)[0]) / (2 * h))
+        fds = np.array(fds)
+        ga = g0[pix]
+        big = np.abs(fds) >= 1e-2 * np.abs(g0).max()
+        rel = np.abs(ga - fds) / np.abs(fds)
+        line["finite_difference_check"] = {
+            "pixels": int(args.fd_pixels), "h": h, "rtol": 1e-12,
+            "vector_rel_err": float(np.linalg.norm(ga - fds) / np.linalg.norm(fds)),
+            "max_rel_err_large": float(rel[big].max()) if big.any() else None,
+            "median_rel_err_large": float(np.median(rel[big])) if big.any() else None,
+            "large_pixels": int(big.sum()),
+            "max_abs_err_over_max_grad": float(np.abs(ga - fds).max() / np.abs(g0).max())}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_inverse(n, n_mfp, n_dir)
     print(json.dumps(line))
@@ -367,6 +394,8 @@ def main():
     ap.add_argument("--serve", type=int, default=0,
                     help="also replay a seeded serving stream of this many requests (Poisson arrivals)")
     ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--fd-pixels", type=int, default=0,
+                    help="config 4: also check dkappa/drho against central differences on this many pixels")
     ap.add_argument("--profile-sweeps", type=int, default=0,
                     help="only build the plan and run this many FP32 and FP64 sweeps (for ncu captures)")
     args = ap.parse_args()

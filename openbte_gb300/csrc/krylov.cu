@@ -163,11 +163,13 @@ __global__ void __launch_bounds__(VT) multidot32_kernel(const float* __restrict_
 #pragma unroll
       for (int t = 0; t < DOT_TILE; ++t) acc[t] = fmaf(vp[t][i], wi, acc[t]);
     }
+    // warp sums in FP32 (32 partial sums of a few elements each), FP64 from the warp level up: FP64
+    // shuffles here kept the kernel on the FP64 pipe at 20 % of DRAM bandwidth
 #pragma unroll
     for (int t = 0; t < DOT_TILE; ++t) {
-      double v = (double)acc[t];
+      float v = acc[t];
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[warp][t] = v;
+      if (lane == 0) red[warp][t] = (double)v;
     }
     __syncthreads();
     if (threadIdx.x < DOT_TILE && jt + (int)threadIdx.x < kk) {
