@@ -178,7 +178,7 @@ obte_status build_schedule(const obte_problem* prob, const obte_material* mat, S
 //   si/sr    side table of special elements (periodic inflow, wall/periodic/contact outputs)
 struct DevSchedule {
   bool ready = false;
-  int G = 1, mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;   // G lanes per element, mcp MFPs per CTA
+  int G = 1, KV = 4, mc = 0, mcp = 0, n_chunks = 0, zero_slot = 0, rows = 0;   // G lanes x KV MFPs per element, mcp per CTA
   int emax = 0, unit_wo = 0, pf_pad = 0, unit_sx = 0;   // periodic bank rows, per-unit staging sizes
   int nbuf = 2;                            // TMA pipeline depth
   size_t smem = 0;

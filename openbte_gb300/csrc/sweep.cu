@@ -423,19 +423,31 @@ template <typename Real> struct V16;
 template <> struct V16<float> { static constexpr int K = 4; };
 template <> struct V16<double> { static constexpr int K = 2; };
 
-__device__ __forceinline__ void vload(const float* p, float (&x)[4]) {
-  const float4 v = *reinterpret_cast<const float4*>(p);
-  x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+template <int K>
+__device__ __forceinline__ void vload(const float* p, float (&x)[K]) {
+#pragma unroll
+  for (int i = 0; i < K; i += 4) {
+    const float4 v = *reinterpret_cast<const float4*>(p + i);
+    x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
+  }
 }
-__device__ __forceinline__ void vload(const double* p, double (&x)[2]) {
-  const double2 v = *reinterpret_cast<const double2*>(p);
-  x[0] = v.x; x[1] = v.y;
+template <int K>
+__device__ __forceinline__ void vload(const double* p, double (&x)[K]) {
+#pragma unroll
+  for (int i = 0; i < K; i += 2) {
+    const double2 v = *reinterpret_cast<const double2*>(p + i);
+    x[i] = v.x; x[i + 1] = v.y;
+  }
 }
-__device__ __forceinline__ void vstore(float* p, const float (&x)[4]) {
-  *reinterpret_cast<float4*>(p) = make_float4(x[0], x[1], x[2], x[3]);
+template <int K>
+__device__ __forceinline__ void vstore(float* p, const float (&x)[K]) {
+#pragma unroll
+  for (int i = 0; i < K; i += 4) *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
 }
-__device__ __forceinline__ void vstore(double* p, const double (&x)[2]) {
-  *reinterpret_cast<double2*>(p) = make_double2(x[0], x[1]);
+template <int K>
+__device__ __forceinline__ void vstore(double* p, const double (&x)[K]) {
+#pragma unroll
+  for (int i = 0; i < K; i += 2) *reinterpret_cast<double2*>(p + i) = make_double2(x[i], x[i + 1]);
 }
 
 // Sum over the G lanes of an element group (aligned groups of G lanes inside a warp).
@@ -446,14 +458,14 @@ __device__ __forceinline__ T group_sum(T v, unsigned mask) {
   return v;
 }
 
-// One CTA = direction q x a chunk of MC = G * KV mean free paths, 128 G threads.  Every element of
+// One CTA = direction q x a chunk of MC = G * KV mean free paths, 128 G threads (KV a multiple of the
+// 16-byte vector: 4 or 8 FP32, 2 or 4 FP64).  Every element of
 // a unit is owned by a group of G consecutive threads; lane l of the group computes the KV MFPs
 // [l KV, (l+1) KV) of the chunk.  The ring is [row][MC] (MFP fastest), so an upstream read is one
 // 16-byte shared load per lane and a group of 8 reads one full 128-byte row.
-template <typename Real, int NF, int G, bool FINAL>
+template <typename Real, int NF, int G, int KV, bool FINAL>
 __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<Real> p) {
   constexpr int RW = Rec<Real, NF>::W;           // record words
-  constexpr int KV = V16<Real>::K;               // MFPs per lane
   constexpr int MC = G * KV;                     // MFPs per CTA
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
   extern __shared__ __align__(128) unsigned char smem[];
@@ -734,25 +746,42 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
   return upload(b, h, st);
 }
 
-// Lane-group sizes compiled for each precision (chunk width = G x V16<Real>::K MFPs).
-static constexpr int kGroups[] = {1, 2, 4, 8};
+// Compiled thread shapes (lanes per element G, MFPs per lane KV) for each precision.
+struct Shape { int G, KV; };
+template <typename Real> struct Shapes;
+template <> struct Shapes<float> { static constexpr Shape v[] = {{1, 4}, {1, 8}, {2, 4}}; };
+template <> struct Shapes<double> { static constexpr Shape v[] = {{1, 2}, {1, 4}, {2, 2}}; };
+constexpr Shape Shapes<float>::v[];
+constexpr Shape Shapes<double>::v[];
 
-// Choose the lane-group size G.  Measured on the 60k-triangle (100 MFP x 96 directions) and the
-// 110k-tetrahedron (30 x 512) benchmark meshes: G = 1 is fastest (2.32 ms / 10.5 ms per FP32 sweep
-// against 2.40 / 16.7 ms at G = 2 and 2.90 ms at G = 8), because each CTA is a chain of level
-// barriers and more, smaller CTAs per SM keep more chains in flight.  Larger groups stay available
-// through OBTE_SWEEP_G (tuning); a size whose shared memory does not fit is skipped.
+// Choose the thread shape.  Measured on the 60k-triangle (100 MFP x 96 directions) and 110k-tetrahedron
+// (30 x 512) benchmark meshes: one thread per element (G = 1) is fastest (2.32 / 10.5 ms per FP32 sweep
+// against 2.40 / 16.7 ms at G = 2 and 2.90 ms at G = 8), because each CTA is a chain of level barriers
+// and more, smaller CTAs per SM keep more chains in flight.
+// OBTE_SWEEP_G / OBTE_SWEEP_KV force a shape (tuning); a shape whose shared memory does not fit is
+// skipped.
 template <typename Real>
-static int choose_group(const Schedule& s, int rows, int unit_wo, int pf_pad, int unit_sx, int nbuf, int num_sms,
-                        size_t optin) {
-  (void)num_sms;
-  const char* env = std::getenv("OBTE_SWEEP_G");
-  const int forced = env ? std::atoi(env) : 1;
-  for (int G : kGroups) {
-    if (G != forced) continue;
-    if (SmemLayout<Real>(s.nf, G * V16<Real>::K, rows, unit_wo, pf_pad, unit_sx, nbuf).total <= optin) return G;
+static Shape choose_shape(const Schedule& s, int rows, int unit_wo, int pf_pad, int unit_sx, int nbuf,
+                          size_t optin) {
+  const char* eg = std::getenv("OBTE_SWEEP_G");
+  const char* ek = std::getenv("OBTE_SWEEP_KV");
+  const int want_g = eg ? std::atoi(eg) : 1;
+  const int want_k = ek ? std::atoi(ek) : V16<Real>::K;
+  auto fits = [&](Shape sh) {
+    return SmemLayout<Real>(s.nf, sh.G * sh.KV, rows, unit_wo, pf_pad, unit_sx, nbuf).total <= optin;
+  };
+  if (eg || ek) {
+    for (Shape sh : Shapes<Real>::v)
+      if (sh.G == want_g && sh.KV == want_k && fits(sh)) return sh;
+  } else {
+    // two vectors per lane halve the per-element overhead per MFP; worth it while at least 4 CTAs still
+    // share an SM (60k triangles: 2.14 against 2.23 ms; 110k tetrahedra, 2 CTAs per SM: 20.8 against 11.6 ms)
+    const Shape wide{1, 2 * V16<Real>::K};
+    const size_t sm = SmemLayout<Real>(s.nf, wide.KV, rows, unit_wo, pf_pad, unit_sx, nbuf).total;
+    if (sizeof(Real) == 4 && sm + 1024 <= (228 * 1024) / 4 && fits(wide)) return wide;
   }
-  return SmemLayout<Real>(s.nf, V16<Real>::K, rows, unit_wo, pf_pad, unit_sx, nbuf).total <= optin ? 1 : 0;
+  const Shape base{1, V16<Real>::K};
+  return fits(base) ? base : Shape{0, 0};
 }
 
 template <typename Real>
@@ -771,14 +800,15 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   const int rows = pk.rows;
   const char* nb_env = std::getenv("OBTE_SWEEP_NBUF");
   const int nbuf = nb_env ? std::max(2, std::min(kMaxBuf, std::atoi(nb_env))) : kDefaultBuf;
-  const int G = choose_group<Real>(s, rows, pk.unit_wo, pk.pf_pad, pk.unit_sx, nbuf, plan->ctx->num_sms,
-                                   plan->ctx->smem_optin);
+  const Shape sh = choose_shape<Real>(s, rows, pk.unit_wo, pk.pf_pad, pk.unit_sx, nbuf, plan->ctx->smem_optin);
+  const int G = sh.G;
   if (!G) {
     set_error("sweep front needs more shared memory than one CTA can have (" + std::to_string(rows) + " rows)");
     return OBTE_ERR_UNSUPPORTED;
   }
-  const int mcp = G * V16<Real>::K;
+  const int mcp = G * sh.KV;
   d.G = G;
+  d.KV = sh.KV;
   d.mc = mcp;
   d.mcp = mcp;
   d.n_chunks = (s.n_mfp + mcp - 1) / mcp;
@@ -848,7 +878,7 @@ obte_status ensure_tables(obte_plan plan, bool fp32) {
 
 // ---- launch -----------------------------------------------------------------------
 
-template <typename Real, int NF, int G, bool FINAL>
+template <typename Real, int NF, int G, int KV, bool FINAL>
 static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                bool with_src, double* Jraw, double* K, double* S) {
   const Schedule& s = plan->sched;
@@ -861,7 +891,7 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
       d.vals.as<Real>());
   count_launch();
   OBTE_CUDA(cudaGetLastError());
-  auto kern = bte_sweep_kernel<Real, NF, G, FINAL>;
+  auto kern = bte_sweep_kernel<Real, NF, G, KV, FINAL>;
   OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
@@ -886,15 +916,15 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   return OBTE_OK;
 }
 
-template <typename Real, int G>
+template <typename Real, int G, int KV>
 static obte_status launch_w(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out, bool with_src,
                             bool final_pass, double* Jraw, double* K, double* S) {
   if (plan->sched.nf == 3) {
-    if (final_pass) return launch_impl<Real, 3, G, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
-    return launch_impl<Real, 3, G, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+    if (final_pass) return launch_impl<Real, 3, G, KV, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+    return launch_impl<Real, 3, G, KV, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
   }
-  if (final_pass) return launch_impl<Real, 4, G, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
-  return launch_impl<Real, 4, G, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  if (final_pass) return launch_impl<Real, 4, G, KV, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  return launch_impl<Real, 4, G, KV, false>(plan, d, u_in, u_out, with_src, Jraw, K, S);
 }
 
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
@@ -907,15 +937,15 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
   OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
   if (final_pass) OBTE_CUDA(cudaMemsetAsync(Jraw, 0, (size_t)s.n * s.ds * sizeof(double), st));
   const DevSchedule& d = fp32 ? plan->d32 : plan->d64;
-#define OBTE_W(R, G) \
-  case G: return launch_w<R, G>(plan, d, u_in, u_out, with_src, final_pass, Jraw, K, S)
+#define OBTE_W(R, GG, KK) \
+  if (d.G == GG && d.KV == KK) return launch_w<R, GG, KK>(plan, d, u_in, u_out, with_src, final_pass, Jraw, K, S)
   if (fp32) {
-    switch (d.G) { OBTE_W(float, 1); OBTE_W(float, 2); OBTE_W(float, 4); OBTE_W(float, 8); }
+    OBTE_W(float, 1, 4); OBTE_W(float, 1, 8); OBTE_W(float, 2, 4);
   } else {
-    switch (d.G) { OBTE_W(double, 1); OBTE_W(double, 2); OBTE_W(double, 4); OBTE_W(double, 8); }
+    OBTE_W(double, 1, 2); OBTE_W(double, 1, 4); OBTE_W(double, 2, 2);
   }
 #undef OBTE_W
-  set_error("no compiled sweep kernel for this lane-group size");
+  set_error("no compiled sweep kernel for this thread shape");
   return OBTE_ERR_UNSUPPORTED;
 }
 
@@ -978,7 +1008,7 @@ static obte_status static_scratch_address(int device, void** out) {
   return OBTE_OK;
 }
 
-template <typename Real, int NF, int G>
+template <typename Real, int NF, int G, int KV>
 static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                       bool with_src, Real* vals, int* err) {
   const Schedule& s = plan->sched;
@@ -990,7 +1020,7 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
       s.n, s.hs.empty() ? nullptr : d.hs.as<double>(), with_src ? 1 : 0, total, vals);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
-  auto kern = bte_sweep_kernel<Real, NF, G, false>;
+  auto kern = bte_sweep_kernel<Real, NF, G, KV, false>;
   OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
@@ -1014,11 +1044,11 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   return OBTE_OK;
 }
 
-template <typename Real, int G>
+template <typename Real, int G, int KV>
 static obte_status launch_static_w(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                    bool with_src, Real* vals, int* err) {
-  if (plan->sched.nf == 3) return launch_static_impl<Real, 3, G>(plan, d, u_in, u_out, with_src, vals, err);
-  return launch_static_impl<Real, 4, G>(plan, d, u_in, u_out, with_src, vals, err);
+  if (plan->sched.nf == 3) return launch_static_impl<Real, 3, G, KV>(plan, d, u_in, u_out, with_src, vals, err);
+  return launch_static_impl<Real, 4, G, KV>(plan, d, u_in, u_out, with_src, vals, err);
 }
 
 // Runs with the plan's device current; the caller restores its own.
@@ -1034,15 +1064,15 @@ static obte_status sweep_static_on_device(obte_plan plan, bool fp32, const doubl
   OBTE_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
   OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
   obte_status rc = OBTE_ERR_UNSUPPORTED;
-#define OBTE_SW(R, G) \
-  case G: rc = launch_static_w<R, G>(plan, d, u_in, u_out, with_src, static_cast<R*>(vals), err); break
+#define OBTE_SW(R, GG, KK) \
+  if (d.G == GG && d.KV == KK) rc = launch_static_w<R, GG, KK>(plan, d, u_in, u_out, with_src, static_cast<R*>(vals), err)
   if (fp32) {
-    switch (d.G) { OBTE_SW(float, 1); OBTE_SW(float, 2); OBTE_SW(float, 4); OBTE_SW(float, 8); }
+    OBTE_SW(float, 1, 4); else OBTE_SW(float, 1, 8); else OBTE_SW(float, 2, 4);
   } else {
-    switch (d.G) { OBTE_SW(double, 1); OBTE_SW(double, 2); OBTE_SW(double, 4); OBTE_SW(double, 8); }
+    OBTE_SW(double, 1, 2); else OBTE_SW(double, 1, 4); else OBTE_SW(double, 2, 2);
   }
 #undef OBTE_SW
-  if (rc == OBTE_ERR_UNSUPPORTED) set_error("no compiled sweep kernel for this lane-group size");
+  if (rc == OBTE_ERR_UNSUPPORTED) set_error("no compiled sweep kernel for this thread shape");
   if (rc != OBTE_OK) return rc;
   int h = 0;
   OBTE_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
