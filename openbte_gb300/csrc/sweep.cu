@@ -892,7 +892,9 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   count_launch();
   OBTE_CUDA(cudaGetLastError());
   auto kern = bte_sweep_kernel<Real, NF, G, KV, FINAL>;
-  OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
+  // the limit is per kernel, shared by every plan and thread: always the device maximum, so concurrent
+  // plans with different footprints cannot lower it under each other's launches
+  OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan->ctx->smem_optin));
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
   p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;
@@ -1021,7 +1023,7 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   count_launch();
   OBTE_CUDA(cudaGetLastError());
   auto kern = bte_sweep_kernel<Real, NF, G, KV, false>;
-  OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem));
+  OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan->ctx->smem_optin));
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
   p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;

@@ -279,8 +279,9 @@ def summarize(results, wall_s: Optional[float] = None) -> dict:
     lat = np.array([r.latency for r in ok]) if ok else np.zeros(1)
     if wall_s is None and ok:
         wall_s = max(r.t_done for r in ok) - min(r.t_submit for r in results)
+    errs = sorted({r.error for r in results if r.status == "error" and r.error})
     return {"completed": len(ok), "rejected": sum(r.status == "rejected" for r in results),
-            "errors": sum(r.status == "error" for r in results),
+            "errors": sum(r.status == "error" for r in results), "error_messages": errs[:3],
             "solves_per_s": len(ok) / wall_s if wall_s else 0.0,
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "mean_queue_ms": float(np.mean([r.queue_time for r in ok]) * 1e3) if ok else 0.0,

@@ -76,3 +76,50 @@ def test_request_over_budget_is_rejected():
     res = replay(srv, [r])[0]
     srv.close()
     assert res.status == "rejected"
+
+
+def test_concurrent_sweeps_with_different_footprints():
+    """Two plans whose sweep kernels need different shared memory, swept from two threads on their own
+    streams at the same time: every call succeeds and matches the same sweep run alone."""
+    import ctypes as C
+    import threading
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.runtime import HostProblem, Plan
+    from openbte_gb300 import objects as O
+    from openbte_gb300.geometry import porous_cell_2d
+    from openbte_gb300.material import synthetic_isotropic_2d
+    from openbte_gb300.mesh import mesh_from_cell
+    bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
+    ek = O.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
+    cases = [(400, 0.10, "circle", 8, 16), (3000, 0.30, "square", 24, 48)]
+    plans, states, refs = [], [], []
+    for i, (n, phi, pore, nm, nq) in enumerate(cases):
+        stream = torch.cuda.Stream()
+        geo = mesh_from_cell(porous_cell_2d(n, phi, pore, seed=200 + i))
+        plan = Plan(HostProblem(geo, synthetic_isotropic_2d(nm, nq), bcs, ek), stream=stream.cuda_stream)
+        u = torch.tensor(np.random.default_rng(i).standard_normal(plan.nu), dtype=torch.float64, device="cuda")
+        out = torch.zeros_like(u)
+        _lib.check(plan.lib.obte_bte_sweep(plan.handle, 2, C.c_void_p(u.data_ptr()), C.c_void_p(out.data_ptr()), 1))
+        plans.append(plan); states.append(u); refs.append(out.cpu().numpy())
+    errors = []
+
+    def run(i):
+        out = torch.zeros_like(states[i])
+        for _ in range(40):
+            st = plans[i].lib.obte_bte_sweep(plans[i].handle, 2, C.c_void_p(states[i].data_ptr()),
+                                             C.c_void_p(out.data_ptr()), 1)
+            if st != 0:
+                errors.append(plans[i].lib.obte_last_error())
+                return
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        if not np.allclose(got, refs[i], rtol=0, atol=1e-5 * np.abs(refs[i]).max()):
+            errors.append(b"mismatch")
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
