@@ -408,6 +408,8 @@ def main():
                     help="config 4: also check dkappa/drho against central differences on this many pixels")
     ap.add_argument("--profile-sweeps", type=int, default=0,
                     help="only build the plan and run this many FP32 and FP64 sweeps (for ncu captures)")
+    ap.add_argument("--profile-fourier", type=int, default=0,
+                    help="only build the Fourier plan and run this many Fourier first-guess solves")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -437,6 +439,23 @@ def main():
     lib = _lib.load()
 
     geo, mat, bcs, ek = problem(args.workload)
+    if args.profile_fourier:
+        t0 = time.time()
+        fplan = get_fourier_plan(geo, mat.thermal_conductivity, bcs, ek, [], local)
+        fplan_s = time.time() - t0
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        half = args.profile_fourier // 2
+        for i in range(args.profile_fourier):
+            if i == half:
+                ev[0].record()
+            finfo, _, _ = fplan.solve(device=local)
+        ev[1].record()
+        ev[1].synchronize()
+        print(json.dumps({"profile_fourier": args.profile_fourier, "workload": args.workload,
+                          "plan_s": fplan_s, "ms_per_solve": ev[0].elapsed_time(ev[1]) / max(1, args.profile_fourier - half),
+                          "outer_iterations": finfo.n_iter, "cg_iterations": finfo.n_cg, "kappa": finfo.kappa,
+                          "preconditioner": "jacobi" if os.environ.get("OBTE_FOURIER_JACOBI", "0") != "0" else "amg"}))
+        return
     hp = HostProblem(geo, mat, bcs, ek)
     t0 = time.time()
     plan = get_plan(hp, local)

@@ -131,7 +131,8 @@ __device__ __forceinline__ double sum_partials(const double* __restrict__ part, 
 }
 
 // one CG step after the SpMV: alpha = rz / sum(pAp partials); x += a p; r -= a Ap; z = r dinv;
-// partials of r.z (next rz) and r.r.  rz is read from sc[cur].
+// partials of r.z (next rz) and r.r.  rz is read from sc[cur].  z == nullptr: another preconditioner
+// writes z and the r.z partials.
 __global__ void cg_step_kernel(int64_t n, const double* __restrict__ part_pap, int nb, const double* __restrict__ sc,
                                int cur, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
                                const double* __restrict__ p, const double* __restrict__ Ap,
@@ -146,7 +147,7 @@ __global__ void cg_step_kernel(int64_t n, const double* __restrict__ part_pap, i
     const double ri = r[i] - a * Ap[i];
     r[i] = ri;
     const double zi = ri * dinv[i];
-    z[i] = zi;
+    if (z) z[i] = zi;
     rz += ri * zi;
     rr += ri * ri;
   }
@@ -162,7 +163,7 @@ __global__ void cg_step_kernel(int64_t n, const double* __restrict__ part_pap, i
   if (threadIdx.x == 0) {
     double t0 = 0, t1 = 0;
     for (int w = 0; w < FT / 32; ++w) { t0 += red[0][w]; t1 += red[1][w]; }
-    part_rz[blockIdx.x] = t0;
+    if (z) part_rz[blockIdx.x] = t0;
     part_rr[blockIdx.x] = t1;
   }
 }
@@ -182,6 +183,26 @@ __global__ void cg_dir_kernel(int64_t n, const double* __restrict__ part_rz, con
       sc[cur ^ 1] = rzn;
       sc[3] = rr;
     }
+  }
+}
+
+// partials of r.z (the preconditioned residual product); p = z as well when p is given
+__global__ void rz_kernel(int64_t n, const double* __restrict__ r, const double* __restrict__ z, double* __restrict__ p,
+                          double* __restrict__ part) {
+  __shared__ double red[FT / 32];
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * FT + threadIdx.x; i < n; i += (int64_t)gridDim.x * FT) {
+    const double zi = z[i];
+    acc += r[i] * zi;
+    if (p) p[i] = zi;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < FT / 32; ++w) t += red[w];
+    part[blockIdx.x] = t;
   }
 }
 
@@ -373,6 +394,8 @@ struct obte_fourier_plan_s {
   cudaStream_t capture_stream = nullptr;
   cudaGraphExec_t cg_exec = nullptr;
   const double* cg_exec_T = nullptr;
+  // smoothed-aggregation AMG V-cycle as the CG preconditioner (null: Jacobi)
+  obte::AmgPtr amg;
   ~obte_fourier_plan_s() {
     if (cg_exec) cudaGraphExecDestroy(cg_exec);
     if (capture_stream) cudaStreamDestroy(capture_stream);
@@ -567,6 +590,10 @@ extern "C" obte_status obte_fourier_plan_create(obte_context ctx, const obte_fou
   up(P->sc.alloc(8 * sizeof(double))); up(P->grad.alloc(vb * dim)); up(P->tmp.alloc((size_t)std::max<int64_t>(ni, 1) * 8));
   up(P->kout.alloc((size_t)std::max<int64_t>(P->nc, 1) * 8));
   up(P->pmx.alloc((size_t)P->nb * 8)); up(P->pmn.alloc((size_t)P->nb * 8));
+  // OBTE_FOURIER_JACOBI=1 keeps the diagonal preconditioner (same solution, ~40x more CG iterations)
+  const char* jac = std::getenv("OBTE_FOURIER_JACOBI");
+  if (s0 == OBTE_OK && !(jac && std::atoi(jac) != 0))
+    up(amg_build(n, rp, ci, val, pin, ctx->num_sms, st, P->amg));
   if (s0 == OBTE_OK) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) s0 = cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
@@ -582,7 +609,7 @@ extern "C" obte_status obte_fourier_plan_destroy(obte_fourier_plan plan) {
   return OBTE_OK;
 }
 
-// Jacobi-preconditioned CG on the masked system, warm-started from T (device). Returns iterations.
+// Preconditioned CG (AMG V-cycle, or Jacobi) on the masked system, warm-started from T (device). Returns iterations.
 static obte_status cg_solve(obte_fourier_plan P, double* T, double rtol, int max_iter, int& iters) {
   cudaStream_t st = P->ctx->stream;
   const int64_t n = P->n;
@@ -592,9 +619,15 @@ static obte_status cg_solve(obte_fourier_plan P, double* T, double rtol, int max
   const int32_t *rp = P->rp.as<int32_t>(), *ci = P->ci.as<int32_t>();
   const double* val = P->val.as<double>();
   // r = rhs - L T, z = r dinv, p = z; rz -> sc[0], rr -> sc[3], ‖rhs‖^2 -> sc[5]
+  const AmgHierarchy* amg = P->amg.get();
   spmv_kernel<<<nb, FT, 0, st>>>(n, rp, ci, val, T, Ap, P->part.as<double>());
   cg_init_kernel<<<nb, FT, 0, st>>>(n, P->rhs.as<double>(), Ap, P->dinv.as<double>(), r, z, p, P->part.as<double>(),
                                     P->part2.as<double>(), P->part3.as<double>());
+  if (amg) {                         // z = M^-1 r, p = z, r.z
+    count_launch(amg_apply(*amg, r, z, nullptr, 0, st));
+    rz_kernel<<<nb, FT, 0, st>>>(n, r, z, p, P->part.as<double>());
+    count_launch();
+  }
   reduce_kernel<<<1, FT, 0, st>>>(P->part.as<double>(), nb, sc + 0);
   reduce_kernel<<<1, FT, 0, st>>>(P->part2.as<double>(), nb, sc + 3);
   reduce_kernel<<<1, FT, 0, st>>>(P->part3.as<double>(), nb, sc + 5);
@@ -611,15 +644,20 @@ static obte_status cg_solve(obte_fourier_plan P, double* T, double rtol, int max
     // per launch the loop is launch-bound, so the `check` iterations between two convergence tests are
     // captured once as a CUDA graph (on a private stream: capture is not allowed on the legacy default
     // stream) and replayed on the plan's stream.  `check` is even, so every block starts with cur = 0.
-    const int check = 8;
+    // With the AMG preconditioner a solve takes a few tens of iterations, so the check comes every 4.
+    // The V-cycle writes z and the partials of r.z (cg_step_kernel then skips its Jacobi z).
+    const int check = amg ? 4 : 8;
     double* pp = P->part.as<double>();
     double* prz = P->part2.as<double>();
     double* prr = P->part3.as<double>();
+    const int per_iter = amg ? 3 + amg_launches(*amg, true) : 3;
     auto enqueue = [&](cudaStream_t s2) {
       for (int k = 0; k < check; ++k) {
         const int cur = k & 1;
         spmv_kernel<<<nb, FT, 0, s2>>>(n, rp, ci, val, p, Ap, pp);
-        cg_step_kernel<<<nb, FT, 0, s2>>>(n, pp, nb, sc, cur, T, r, z, p, Ap, P->dinv.as<double>(), prz, prr);
+        cg_step_kernel<<<nb, FT, 0, s2>>>(n, pp, nb, sc, cur, T, r, amg ? nullptr : z, p, Ap, P->dinv.as<double>(),
+                                          prz, prr);
+        if (amg) amg_apply(*amg, r, z, prz, nb, s2);
         cg_dir_kernel<<<nb, FT, 0, s2>>>(n, prz, prr, nb, sc, cur, p, z);
       }
     };
@@ -638,7 +676,7 @@ static obte_status cg_solve(obte_fourier_plan P, double* T, double rtol, int max
     while (iters < max_iter) {
       if (P->cg_exec && P->cg_exec_T == T) OBTE_CUDA(cudaGraphLaunch(P->cg_exec, st));
       else enqueue(st);
-      count_launch(3 * check);
+      count_launch(per_iter * check);
       iters += check;
       OBTE_CUDA(cudaGetLastError());
       OBTE_CUDA(cudaMemcpyAsync(hs, sc, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));

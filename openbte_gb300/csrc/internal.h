@@ -95,6 +95,21 @@ struct DevBuf {
 template <typename T>
 obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream);
 
+// ---- smoothed-aggregation AMG (preconditioner of the Fourier CG, amg.cu) ---------------------------
+struct AmgHierarchy;
+struct AmgDeleter {
+  void operator()(AmgHierarchy* h) const;
+};
+using AmgPtr = std::unique_ptr<AmgHierarchy, AmgDeleter>;
+// Hierarchy of the SPD CSR matrix (rp, ci, val); row `pin` (>= 0) is replaced by the identity.
+obte_status amg_build(int64_t n, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
+                      const std::vector<double>& val, int pin, int num_sms, cudaStream_t st, AmgPtr& out);
+// Enqueue z = M^-1 r (one symmetric V-cycle) on `st`; with `part`, also the nb_part block partials of
+// r . z (launched on exactly nb_part blocks).  Returns the number of kernel launches.
+int amg_apply(const AmgHierarchy& H, const double* r, double* z, double* part, int nb_part, cudaStream_t st);
+int amg_levels(const AmgHierarchy& H);
+int amg_launches(const AmgHierarchy& H, bool with_part);   // kernel launches of one amg_apply
+
 }  // namespace obte
 
 struct obte_context_s {
