@@ -587,6 +587,8 @@ def main():
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_sweep / t_sweep / 1e9
 
+    pb, ps, pms = C.c_int32(), C.c_int32(), C.c_double()
+    _lib.check(lib.obte_bte_precond_info(plan.handle, C.byref(pb), C.byref(ps), C.byref(pms)), "precond_info")
     line = {
         "metric": "kappa_eff solves/s (served FP32+refine, <=1e-4 kappa error)",
         "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -614,6 +616,8 @@ def main():
                      "algorithmic_bytes": int(bytes_sweep), "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "clocks": clk.summary(),
         "plan_build_s": plan_s,
+        # periodic-inflow preconditioner, built once per plan on its first (warm-up) solve
+        "preconditioner": {"blocks": pb.value, "setup_sweeps": ps.value, "setup_ms": pms.value},
         "wall_timed_s": t_total,
     }
     if args.serve:

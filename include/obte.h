@@ -111,6 +111,10 @@ typedef struct {
   double inner_rtol;              /* inner FP32 tolerance (FP32_REFINE)           */
   int32_t warm_start;             /* 1: start from this plan's previous converged state (dT0 still
                                      fixes the conserved temperature level); 0: start from dT0 */
+  int32_t precond;                /* periodic-inflow preconditioner (see obte_bte_precond_info):
+                                     0 built on the plan's second solve (plans solved once do not pay
+                                     its setup), 1 built on the first solve, -1 off; other values: 0.
+                                     The environment variable OBTE_XPREC=0 / 1 overrides it. */
 } obte_solve_opts;
 
 typedef struct {
@@ -213,6 +217,14 @@ obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_opts* opts,
                                     double* grad_t, obte_solve_info* info);
 /* Sizes of the state vector pieces: n_elems, n_diffuse, n_x. */
 obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x);
+/*
+ * Periodic-inflow preconditioner of the plan (no counterpart in the reference, whose per-ordinate
+ * sparse LU solves the periodic coupling directly): built on the plan's first solve unless the
+ * environment sets OBTE_XPREC=0.  n_blocks: ordinates it covers (0: none, or not built yet);
+ * setup_sweeps: FP32 sweeps its setup ran (detection and probing); setup_ms: host wall time of the
+ * setup.  Any pointer may be null.
+ */
+obte_status obte_bte_precond_info(obte_plan plan, int32_t* n_blocks, int32_t* setup_sweeps, double* setup_ms);
 /*
  * Sweep schedule of direction q, as built on the host (for bit-exact checks):
  *   order  host [n_elems]      element processed at each position

@@ -51,7 +51,7 @@ class MaterialC(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_sweeps", C.c_int32),
                 ("restart", C.c_int32), ("refine_steps", C.c_int32), ("inner_rtol", C.c_double),
-                ("warm_start", C.c_int32)]
+                ("warm_start", C.c_int32), ("precond", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -101,6 +101,8 @@ SIGNATURES = [
     ("obte_bte_kappa_gradient", C.c_int, [C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p,
                                           C.POINTER(SolveInfo)]),
     ("obte_bte_state_layout", C.c_int, [C.c_void_p, p_i64, p_i64, p_i64]),
+    ("obte_bte_precond_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_double)]),
     ("obte_bte_schedule", C.c_int, [C.c_void_p, C.c_int32, p_i64, p_i64, p_i64, p_i64]),
     ("obte_fourier_plan_create", C.c_int, [C.c_void_p, C.POINTER(FourierProblem), C.POINTER(C.c_void_p)]),
     ("obte_fourier_plan_destroy", C.c_int, [C.c_void_p]),

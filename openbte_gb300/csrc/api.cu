@@ -179,6 +179,16 @@ extern "C" obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, i
   return OBTE_OK;
 }
 
+extern "C" obte_status obte_bte_precond_info(obte_plan plan, int32_t* n_blocks, int32_t* setup_sweeps,
+                                             double* setup_ms) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  const XPrec* P = plan->xprec.get();
+  if (n_blocks) *n_blocks = P ? P->nblk : 0;
+  if (setup_sweeps) *setup_sweeps = P ? P->detect_sweeps + P->probe_sweeps : 0;
+  if (setup_ms) *setup_ms = P ? P->setup_ms : 0.0;
+  return OBTE_OK;
+}
+
 extern "C" obte_status obte_bte_schedule(obte_plan plan, int32_t q, int64_t* order, int64_t* level_ptr,
                                          int64_t* n_levels, int64_t* n_slots) {
   if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }

@@ -211,7 +211,20 @@ struct SolveWork {
   int restart = 0;
   int nb = 1;
   DevBuf u, Fu, r, V, w, tmp, partial, hdev, sdev, Jraw, Kraw, Sraw, delta;
+  DevBuf pz;         // preconditioned vector (allocated when the plan has a preconditioner)
   DevBuf V32, w32;   // FP32 basis and working vector (stages with FP32 sweeps), allocated on first use
+};
+
+// Right preconditioner of the GMRES on the periodic-inflow unknowns: for the ordinates whose inflow
+// circulates through the periodic cell for many periods, the exact inverse of their one-period
+// inflow -> outflow transfer, (I - T_b)^-1 - I, as a dense FP32 block over the direction's source slots.
+struct XPrec {
+  bool tried = false;            // setup ran (blocks may still be empty)
+  int nblk = 0, smax = 0;
+  int probe_sweeps = 0, detect_sweeps = 0;
+  double setup_ms = 0;
+  DevBuf bm, bs, bbase, bwoff;   // per block: MFP, size (slots), first slot, offset of its W block
+  DevBuf W;                      // FP32 row-major blocks
 };
 
 // Transmission-interface gradient: per internal side tables, ordinate tables and the final-pass
@@ -239,6 +252,11 @@ struct obte_plan_s {
   bool has_solution = false;        // work->u holds the last converged state
   float* xstore = nullptr;          // set during a gradient solve: final-pass per-ordinate temperatures
   std::unique_ptr<obte::TimDevice> tim;   // transmission-interface gradient tables and scratch
+  // non-final sweeps run only these CTAs (direction * n_chunks + chunk) while set (preconditioner setup)
+  const int32_t* sweep_cta_map = nullptr;
+  int sweep_n_cta = 0;
+  std::unique_ptr<obte::XPrec> xprec;     // periodic-inflow block preconditioner
+  int n_solves = 0;                       // obte_bte_solve calls on this plan
 };
 
 namespace obte {
@@ -246,6 +264,10 @@ namespace obte {
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
                          bool final_pass, double* Jraw, double* K, double* S);
 obte_status ensure_tables(obte_plan plan, bool fp32);
+// Periodic-inflow preconditioner (xprec.cu): built once per plan.
+obte_status ensure_xprec(obte_plan plan, SolveWork& wk);
+// out[X blocks] += W in[X blocks] (fp32: FP32 accumulation, for stages with an FP32 Krylov basis)
+void xprec_add(obte_plan plan, const double* in, double* out, bool fp32);
 obte_status check_device_error(obte_plan plan);
 int64_t solve_scratch_bytes(obte_plan plan, int restart);
 }  // namespace obte

@@ -326,6 +326,16 @@ struct Solver {
   double t_wall = 0;
   int t_iters = 0;
 
+  // right preconditioner (periodic-inflow blocks), or off
+  bool xp = false;
+  // out = M^-1 in = in + W in (W on the slow inflow blocks)
+  obte_status prec(const double* in, double* out, bool fp32) {
+    OBTE_CUDA(cudaMemcpyAsync(out, in, (size_t)wk.nu * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    xprec_add(plan, in, out, fp32);
+    OBTE_CUDA(cudaGetLastError());
+    return OBTE_OK;
+  }
+
   obte_status sweep(bool fp32, const double* in, double* out, bool src, bool fin = false) {
     ++sweeps;
     if (!fp32) ++sweeps64;
@@ -449,9 +459,14 @@ struct Solver {
         if (trace) cudaEventRecord(ev[0], st);
         widen_kernel<<<nb, VT, 0, st>>>(V + (int64_t)j * n, vj64, n);
         count_launch();
-        OBTE_TRY(sweep(true, vj64, wk.tmp.as<double>(), false));
+        const double* zj = vj64;              // z_j = M^-1 v_j
+        if (xp) {
+          OBTE_TRY(prec(vj64, wk.pz.as<double>(), true));
+          zj = wk.pz.as<double>();
+        }
+        OBTE_TRY(sweep(true, zj, wk.tmp.as<double>(), false));
         if (trace) cudaEventRecord(ev[1], st);
-        diff_to_f32_kernel<<<nb, VT, 0, st>>>(vj64, wk.tmp.as<double>(), w, n);
+        diff_to_f32_kernel<<<nb, VT, 0, st>>>(zj, wk.tmp.as<double>(), w, n);
         count_launch();
         OBTE_CUDA(cudaGetLastError());
         // classical Gram-Schmidt with one conditional re-orthogonalisation (as in gmres())
@@ -506,8 +521,17 @@ struct Solver {
       }
       if (j > 0) {
         OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, st));
-        xupdate32_kernel<<<nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n);
-        count_launch();
+        if (xp) {                             // x += M^-1 (V y)
+          double* z = wk.pz.as<double>();
+          OBTE_CUDA(cudaMemsetAsync(z, 0, (size_t)n * sizeof(double), st));
+          xupdate32_kernel<<<nb, VT, 0, st>>>(z, V, n, j, wk.hdev.as<double>(), n);
+          count_launch();
+          OBTE_TRY(axpby(1.0, z, 1.0, x));
+          xprec_add(plan, z, x, true);
+        } else {
+          xupdate32_kernel<<<nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n);
+          count_launch();
+        }
         OBTE_CUDA(cudaGetLastError());
       }
       OBTE_TRY(residual(true, rhs, x, r));
@@ -552,9 +576,14 @@ struct Solver {
         double* vj = V + (int64_t)j * n;
         const auto w0 = std::chrono::steady_clock::now();
         if (trace) cudaEventRecord(ev[0], st);
-        OBTE_TRY(sweep(fp32, vj, wk.tmp.as<double>(), false));
+        const double* zj = vj;                // z_j = M^-1 v_j
+        if (xp) {
+          OBTE_TRY(prec(vj, wk.pz.as<double>(), false));
+          zj = wk.pz.as<double>();
+        }
+        OBTE_TRY(sweep(fp32, zj, wk.tmp.as<double>(), false));
         if (trace) cudaEventRecord(ev[1], st);
-        OBTE_TRY(lincomb(1.0, vj, -1.0, wk.tmp.as<double>(), w));
+        OBTE_TRY(lincomb(1.0, zj, -1.0, wk.tmp.as<double>(), w));
         // classical Gram-Schmidt; a second pass only when the first one cancelled most of w
         // (Daniel-Gragg-Kaufman-Stewart criterion, ‖w‖ after < 0.7 ‖w‖ before)
         OBTE_TRY(multidot(V, j + 1, w, h, true));   // h[0..j] and w.w in one pass
@@ -610,8 +639,17 @@ struct Solver {
       for (double& v : y) v = -v;   // update_kernel subtracts
       if (j > 0) {
         OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, st));
-        update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n, nullptr);
-        count_launch();
+        if (xp) {                             // x += M^-1 (V y)
+          double* z = wk.pz.as<double>();
+          OBTE_CUDA(cudaMemsetAsync(z, 0, (size_t)n * sizeof(double), st));
+          update_kernel<<<wk.nb, VT, 0, st>>>(z, V, n, j, wk.hdev.as<double>(), n, nullptr);
+          count_launch();
+          OBTE_TRY(axpby(1.0, z, 1.0, x));
+          xprec_add(plan, z, x, false);
+        } else {
+          update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n, nullptr);
+          count_launch();
+        }
         OBTE_CUDA(cudaGetLastError());
       }
       // true residual for the restart
@@ -692,8 +730,18 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   }
   Work& wk = *plan->work;
   const bool warm = opts->warm_start && plan->has_solution;
+  // the preconditioner's setup sweeps use the work vectors, so it runs before the state is set up
+  // (a warm start keeps its previous state in wk.u, which the setup does not touch)
+  int pmode = (opts->precond >= -1 && opts->precond <= 1) ? opts->precond : 0;
+  if (const char* e = std::getenv("OBTE_XPREC")) pmode = std::atoi(e) == 0 ? -1 : 1;
+  const bool build_xp = pmode == 1 || (pmode == 0 && plan->n_solves >= 1);
+  ++plan->n_solves;
+  if (build_xp) OBTE_TRY(ensure_xprec(plan, wk));
+  const bool use_xp = pmode >= 0 && plan->xprec && plan->xprec->nblk > 0;
+  if (use_xp && !wk.pz.p) OBTE_TRY(wk.pz.alloc((size_t)wk.nu * sizeof(double)));
   plan->has_solution = false;
   Solver sv(plan, wk, max_sweeps);
+  sv.xp = use_xp;
   double* u = wk.u.as<double>();
   const int64_t nsrc = s.x_base[s.n_dir];
   // the state implied by dT0 fixes the conserved temperature level; a warm start keeps the

@@ -359,6 +359,7 @@ struct SweepParams {
   double* __restrict__ S_out;
   int* __restrict__ err;
   float* __restrict__ Xs;   // final pass only: per-ordinate temperatures [n_dir][n][n_mfp], or null
+  const int32_t* __restrict__ cta_map;   // CTA -> direction * n_chunks + chunk (a subset), or null: all
 };
 
 template <typename Real>
@@ -478,8 +479,9 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
   Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
   Real* ring = reinterpret_cast<Real*>(smem + L.ring);    // [rows][MC]
 
-  const int q = blockIdx.x / p.n_chunks;
-  const int chunk = blockIdx.x - q * p.n_chunks;
+  const int cta = p.cta_map ? p.cta_map[blockIdx.x] : (int)blockIdx.x;
+  const int q = cta / p.n_chunks;
+  const int chunk = cta - q * p.n_chunks;
   const int m0 = chunk * MC;
   const int mc = min(MC, p.n_mfp - m0);
   const int tid = threadIdx.x;
@@ -911,7 +913,8 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S_out = S;
   p.err = plan->err.as<int>();
   p.Xs = FINAL ? plan->xstore : nullptr;
-  const int grid = s.n_dir * d.n_chunks;
+  p.cta_map = FINAL ? nullptr : plan->sweep_cta_map;
+  const int grid = p.cta_map ? plan->sweep_n_cta : s.n_dir * d.n_chunks;
   kern<<<grid, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
@@ -1040,6 +1043,7 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.u_in = u_in; p.u_out = u_out; p.Jraw = nullptr; p.K = nullptr; p.S_out = nullptr;
   p.err = err;
   p.Xs = nullptr;
+  p.cta_map = nullptr;
   kern<<<s.n_dir * d.n_chunks, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());

@@ -1,0 +1,302 @@
+// Periodic-inflow block preconditioner of the GMRES on the sweep fixed point.
+//
+// The state carries, per ordinate, the temperatures entering the cell across the cut periodic faces
+// (openbte/bte.py:99-110 couples the two sides of each periodic pair inside one sparse solve; here
+// that coupling is an unknown of the fixed point, see krylov.cu).  One sweep carries an inflow one
+// period further.  An ordinate whose rays run through the cell without meeting a wall — a direction
+// along a lattice axis of the periodic cell, beside the pore — at a mean free path much longer than
+// the cell keeps most of its inflow after a period: its one-period transfer T (source slots ->
+// source slots) has a spectral radius near exp(-L / mfp) ~ 0.99, and GMRES spends an iteration on
+// almost every such ordinate.  The right preconditioner M^-1 = I + sum_b E_b ((I - T_b)^-1 - I) E_b^T
+// applies the exact inverse of those blocks, so (I - K) M^-1 is close to the identity on them.
+//
+// Setup, once per plan (by default on its second solve: a plan solved once does not pay for it), with
+// FP32 sweeps of zero temperature and wall inputs, which isolate the inflow -> outflow map:
+//   1. detection: ten applications of the map to an all-ones inflow; an ordinate is slow when the
+//      last application kept more than 60 % of its inflow norm;
+//   2. probing: for slot j of every slow ordinate's direction, a sweep of the unit inflow e_j gives
+//      column j of every slow block at once (the ordinates do not interact); only the CTAs of the
+//      slow (direction, MFP chunk) pairs run;
+//   3. one CTA per block inverts I - T in place by Gauss-Jordan in FP32: T >= 0 with row sums below
+//      one makes I - T strictly diagonally dominant, so no pivoting is needed; a block whose pivot
+//      falls below 1e-5 is dropped.
+// The preconditioner only changes the Krylov space, not the fixed point: the convergence test stays
+// on the true residual ‖F(u) - u‖.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <vector>
+
+#include "internal.h"
+
+namespace obte {
+
+namespace {
+
+constexpr int XT = 256;
+constexpr int kDetect = 10;        // applications of the inflow map in the detection (OBTE_XPREC_DETECT)
+constexpr double kSlow = 0.6;      // norm kept by the last application above which an ordinate is slow
+                                   // (OBTE_XPREC_SLOW)
+constexpr int kMaxSlots = 1024;    // largest block
+constexpr double kMaxBytes = 1.0e9;
+
+// per-ordinate sum of squares of the inflow part: out[q * n_mfp + m]
+__global__ void xnorm_kernel(const double* __restrict__ x, int64_t xoff, const int64_t* __restrict__ x_base,
+                             int n_mfp, double* __restrict__ out) {
+  const int q = blockIdx.x;
+  const int64_t b0 = x_base[q], b1 = x_base[q + 1];
+  for (int m = threadIdx.x; m < n_mfp; m += blockDim.x) {
+    double s = 0;
+    for (int64_t slot = b0; slot < b1; ++slot) {
+      const double v = x[xoff + slot * n_mfp + m];
+      s += v * v;
+    }
+    out[(int64_t)q * n_mfp + m] = s;
+  }
+}
+
+__global__ void fill_kernel(double* __restrict__ x, int64_t n, double v) {
+  for (int64_t i = (int64_t)blockIdx.x * XT + threadIdx.x; i < n; i += (int64_t)gridDim.x * XT) x[i] = v;
+}
+
+// x[X(b, j)] = v for every block with j < s_b   (X(b, i) = xoff + (base_b + i) n_mfp + m_b)
+__global__ void xprobe_set_kernel(int nblk, const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
+                                  const int64_t* __restrict__ bbase, int n_mfp, int64_t xoff, int j, double v,
+                                  double* __restrict__ x) {
+  for (int b = blockIdx.x * XT + threadIdx.x; b < nblk; b += gridDim.x * XT)
+    if (j < bs[b]) x[xoff + (bbase[b] + j) * n_mfp + bm[b]] = v;
+}
+
+// column j of every block: W_b[i][j] = y[X(b, i)]
+__global__ void xprobe_get_kernel(const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
+                                  const int64_t* __restrict__ bbase, const int64_t* __restrict__ bwoff, int n_mfp,
+                                  int64_t xoff, int j, const double* __restrict__ y, float* __restrict__ W) {
+  const int b = blockIdx.x;
+  const int s = bs[b];
+  if (j >= s) return;
+  float* Wb = W + bwoff[b];
+  const int64_t base = xoff + bbase[b] * n_mfp + bm[b];
+  for (int i = threadIdx.x; i < s; i += blockDim.x) Wb[(int64_t)i * s + j] = (float)y[base + (int64_t)i * n_mfp];
+}
+
+// In place: W_b holds T_b on entry and (I - T_b)^-1 - I on exit (Gauss-Jordan without pivoting, FP32).
+// A block whose pivot falls below 1e-5 is zeroed (no preconditioning on it) and flagged in bad[b].
+__global__ void __launch_bounds__(1024) xprec_invert_kernel(const int32_t* __restrict__ bs,
+                                                            const int64_t* __restrict__ bwoff, float* __restrict__ W,
+                                                            int* __restrict__ bad) {
+  __shared__ float colk[kMaxSlots];
+  const int b = blockIdx.x;
+  const int s = bs[b];
+  float* A = W + bwoff[b];
+  const int64_t ss = (int64_t)s * s;
+  for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) {
+    const int i = (int)(e / s), j = (int)(e - (int64_t)i * s);
+    A[e] = (i == j ? 1.0f : 0.0f) - A[e];
+  }
+  __syncthreads();
+  for (int k = 0; k < s; ++k) {
+    for (int i = threadIdx.x; i < s; i += blockDim.x) colk[i] = A[(int64_t)i * s + k];
+    __syncthreads();
+    const float piv = colk[k];
+    if (!(piv > 1e-5f)) {                       // same value in every thread: a uniform exit
+      for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) A[e] = 0.0f;
+      if (threadIdx.x == 0) bad[b] = 1;
+      return;
+    }
+    const float p = 1.0f / piv;
+    for (int j = threadIdx.x; j < s; j += blockDim.x) A[(int64_t)k * s + j] = (j == k) ? p : A[(int64_t)k * s + j] * p;
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) {
+      const int i = (int)(e / s);
+      if (i == k) continue;
+      const int j = (int)(e - (int64_t)i * s);
+      A[e] = (j == k) ? -colk[i] * p : A[e] - colk[i] * A[(int64_t)k * s + j];
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < s; i += blockDim.x) A[(int64_t)i * s + i] -= 1.0f;
+}
+
+// out[X(b, i)] += sum_j W_b[i][j] in[X(b, j)]: one CTA per block, the block's inflow staged in shared
+// memory, one warp per row (lane-strided products, fixed summation order).  Acc = float for stages
+// whose Krylov basis is FP32 (GB300's FP64 pipe would bound the FP64 form), double otherwise.
+template <typename Acc>
+__global__ void xprec_apply_kernel(const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
+                                   const int64_t* __restrict__ bbase, const int64_t* __restrict__ bwoff,
+                                   const float* __restrict__ W, int n_mfp, int64_t xoff, const double* __restrict__ in,
+                                   double* __restrict__ out) {
+  extern __shared__ double xin_raw[];
+  Acc* xin = reinterpret_cast<Acc*>(xin_raw);
+  const int b = blockIdx.x;
+  const int s = bs[b];
+  const int64_t base = xoff + bbase[b] * n_mfp + bm[b];
+  for (int i = threadIdx.x; i < s; i += blockDim.x) xin[i] = (Acc)in[base + (int64_t)i * n_mfp];
+  __syncthreads();
+  const float* Wb = W + bwoff[b];
+  const int lane = threadIdx.x & 31;
+  for (int row = threadIdx.x >> 5; row < s; row += blockDim.x >> 5) {
+    const float* wr = Wb + (int64_t)row * s;
+    Acc acc = 0;
+    for (int j = lane; j < s; j += 32) acc += (Acc)wr[j] * xin[j];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[base + (int64_t)row * n_mfp] += (double)acc;
+  }
+}
+
+int blocks_for(int64_t n, int num_sms) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + XT - 1) / XT, (int64_t)num_sms * 8));
+}
+
+}  // namespace
+
+void xprec_add(obte_plan plan, const double* in, double* out, bool fp32) {
+  const XPrec& P = *plan->xprec;
+  if (P.nblk == 0) return;
+  const Schedule& s = plan->sched;
+  auto kern = fp32 ? xprec_apply_kernel<float> : xprec_apply_kernel<double>;
+  kern<<<P.nblk, XT, (size_t)P.smax * sizeof(double), plan->stream>>>(
+      P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(), P.bwoff.as<int64_t>(), P.W.as<float>(), s.n_mfp,
+      s.n + s.nd, in, out);
+  count_launch();
+}
+
+obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
+  if (plan->xprec && plan->xprec->tried) return OBTE_OK;
+  plan->xprec.reset(new XPrec());
+  XPrec& P = *plan->xprec;
+  P.tried = true;
+  const Schedule& s = plan->sched;
+  const int64_t nsrc = s.x_base[s.n_dir];
+  if (nsrc == 0 || s.n_mfp == 0) return OBTE_OK;
+  PhaseTimer timer("xprec setup");
+  const auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t st = plan->stream;
+  const int num_sms = plan->ctx->num_sms;
+  const int64_t xoff = s.n + s.nd;
+  const int64_t nu = plan->nu;
+  OBTE_TRY(ensure_tables(plan, true));
+  double* x = wk.tmp.as<double>();
+  double* y = wk.w.as<double>();
+  // 1. detection: inflow map applied to an all-ones inflow
+  OBTE_CUDA(cudaMemsetAsync(x, 0, (size_t)xoff * sizeof(double), st));
+  fill_kernel<<<blocks_for(nu - xoff, num_sms), XT, 0, st>>>(x + xoff, nu - xoff, 1.0);
+  count_launch();
+  int n_detect = kDetect;
+  double slow = kSlow;
+  if (const char* e = std::getenv("OBTE_XPREC_DETECT")) n_detect = std::max(2, std::atoi(e));
+  if (const char* e = std::getenv("OBTE_XPREC_SLOW")) slow = std::atof(e);
+  const int64_t nord = (int64_t)s.n_dir * s.n_mfp;
+  DevBuf nrm;
+  OBTE_TRY(nrm.alloc((size_t)nord * 2 * sizeof(double)));
+  for (int it = 0; it < n_detect; ++it) {
+    if (it == n_detect - 1) {
+      xnorm_kernel<<<s.n_dir, XT, 0, st>>>(x, xoff, plan->x_base_dev.as<int64_t>(), s.n_mfp, nrm.as<double>());
+      count_launch();
+    }
+    OBTE_TRY(launch_sweep(plan, true, x, y, false, false, nullptr, nullptr, nullptr));
+    OBTE_CUDA(cudaMemsetAsync(y, 0, (size_t)xoff * sizeof(double), st));
+    std::swap(x, y);
+  }
+  xnorm_kernel<<<s.n_dir, XT, 0, st>>>(x, xoff, plan->x_base_dev.as<int64_t>(), s.n_mfp, nrm.as<double>() + nord);
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  std::vector<double> hn((size_t)nord * 2);
+  OBTE_CUDA(cudaMemcpyAsync(hn.data(), nrm.p, hn.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  OBTE_CUDA(cudaStreamSynchronize(st));
+  P.detect_sweeps = n_detect;
+  struct Cand { int q, m; double ratio; int64_t slots; };
+  std::vector<Cand> cand;
+  for (int q = 0; q < s.n_dir; ++q) {
+    const int64_t slots = s.x_base[q + 1] - s.x_base[q];
+    if (slots == 0 || slots > kMaxSlots) continue;
+    for (int m = 0; m < s.n_mfp; ++m) {
+      const double a = hn[(size_t)q * s.n_mfp + m], b = hn[(size_t)nord + (size_t)q * s.n_mfp + m];
+      const double ratio = a > 0 ? std::sqrt(b / a) : 0.0;
+      if (ratio > slow) cand.push_back({q, m, ratio, slots});
+    }
+  }
+  // memory cap: keep the slowest blocks
+  std::stable_sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.ratio > b.ratio; });
+  double bytes = 0;
+  size_t keep = 0;
+  for (; keep < cand.size(); ++keep) {
+    const double bb = (double)cand[keep].slots * cand[keep].slots * sizeof(float);
+    if (bytes + bb > kMaxBytes) break;
+    bytes += bb;
+  }
+  cand.resize(keep);
+  std::stable_sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.q != b.q ? a.q < b.q : a.m < b.m; });
+  if (cand.empty()) {
+    P.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return OBTE_OK;
+  }
+  const int nblk = (int)cand.size();
+  std::vector<int32_t> bm(nblk), bsz(nblk);
+  std::vector<int64_t> bbase(nblk), bwoff(nblk);
+  int64_t woff = 0;
+  int smax = 0;
+  for (int b = 0; b < nblk; ++b) {
+    bm[b] = cand[b].m;
+    bsz[b] = (int32_t)cand[b].slots;
+    bbase[b] = s.x_base[cand[b].q];
+    bwoff[b] = woff;
+    woff += cand[b].slots * cand[b].slots;
+    smax = std::max(smax, (int)cand[b].slots);
+  }
+  OBTE_TRY(upload(P.bm, bm, st));
+  OBTE_TRY(upload(P.bs, bsz, st));
+  OBTE_TRY(upload(P.bbase, bbase, st));
+  OBTE_TRY(upload(P.bwoff, bwoff, st));
+  OBTE_TRY(P.W.alloc((size_t)woff * sizeof(float)));
+  // 2. probing on the CTAs of the slow (direction, MFP chunk) pairs
+  const DevSchedule& d = plan->d32;
+  std::vector<int32_t> ctas;
+  for (const Cand& c : cand) {
+    const int id = c.q * d.n_chunks + c.m / d.mc;
+    if (ctas.empty() || ctas.back() != id) ctas.push_back(id);
+  }
+  ctas.erase(std::unique(ctas.begin(), ctas.end()), ctas.end());
+  DevBuf cmap;
+  OBTE_TRY(upload(cmap, ctas, st));
+  OBTE_CUDA(cudaMemsetAsync(x, 0, (size_t)nu * sizeof(double), st));
+  plan->sweep_cta_map = cmap.as<int32_t>();
+  plan->sweep_n_cta = (int)ctas.size();
+  obte_status ps = OBTE_OK;
+  const int sb = blocks_for(nblk, num_sms);
+  for (int j = 0; j < smax && ps == OBTE_OK; ++j) {
+    xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(), s.n_mfp,
+                                         xoff, j, 1.0, x);
+    ps = launch_sweep(plan, true, x, y, false, false, nullptr, nullptr, nullptr);
+    if (ps != OBTE_OK) break;
+    xprobe_get_kernel<<<nblk, XT, 0, st>>>(P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(),
+                                           P.bwoff.as<int64_t>(), s.n_mfp, xoff, j, y, P.W.as<float>());
+    xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(), s.n_mfp,
+                                         xoff, j, 0.0, x);
+    count_launch(3);
+  }
+  plan->sweep_cta_map = nullptr;
+  plan->sweep_n_cta = 0;
+  OBTE_TRY(ps);
+  P.probe_sweeps = smax;
+  // 3. (I - T)^-1 - I per block
+  DevBuf bad;
+  OBTE_TRY(bad.alloc((size_t)nblk * sizeof(int)));
+  OBTE_CUDA(cudaMemsetAsync(bad.p, 0, (size_t)nblk * sizeof(int), st));
+  xprec_invert_kernel<<<nblk, 1024, 0, st>>>(P.bs.as<int32_t>(), P.bwoff.as<int64_t>(), P.W.as<float>(), bad.as<int>());
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  OBTE_CUDA(cudaStreamSynchronize(st));
+  OBTE_TRY(check_device_error(plan));
+  P.nblk = nblk;
+  P.smax = smax;
+  P.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (timer.on)
+    std::fprintf(stderr, "[obte trace] xprec: %d blocks (largest %d slots), %zu CTAs per probe, %d probe sweeps\n",
+                 nblk, smax, ctas.size(), smax);
+  return OBTE_OK;
+}
+
+}  // namespace obte
