@@ -212,6 +212,7 @@ struct SolveWork {
   int nb = 1;
   DevBuf u, Fu, r, V, w, tmp, partial, hdev, sdev, Jraw, Kraw, Sraw, delta;
   DevBuf pz;         // preconditioned vector (allocated when the plan has a preconditioner)
+  DevBuf rc, Jraw2, Kraw2, Sraw2;   // refinement: correction right-hand side, outputs of the correction
   DevBuf V32, w32;   // FP32 basis and working vector (stages with FP32 sweeps), allocated on first use
 };
 

@@ -82,3 +82,20 @@ def test_blocks_are_the_slow_axis_ordinates():
     nblk, _, _ = _info(plan)
     n_mfp, n_dir = np.asarray(mat.t_coeff).shape
     assert 0 < nblk < n_mfp * n_dir // 4
+
+
+@pytest.mark.parametrize("precision,inner", [("fp32", 1e-5), ("fp32_refine", 1e-8)])
+def test_fp32_stage_stops_at_its_floor(precision, inner):
+    """A tolerance below the FP32 sweeps' rounding floor ends the FP32 stage instead of spinning."""
+    import torch
+    from openbte_gb300.bte import solve_plan
+    geo, mat, bcs, ek = _problem()
+    plan = _plan(geo, mat, bcs, ek)
+    dT0 = torch.zeros(geo.n_elems, dtype=torch.float64, device="cuda:0")
+    info, *_ = solve_plan(plan, dT0, precision=precision, rtol=1e-9, max_sweeps=3000, restart=40,
+                          inner_rtol=inner, precond=1)
+    assert info.n_sweeps < 400, info.n_sweeps
+    if precision == "fp32_refine":
+        assert info.converged and info.residual <= 1e-9
+    else:
+        assert info.residual < 1e-5
