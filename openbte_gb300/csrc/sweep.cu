@@ -66,7 +66,13 @@ template <typename Real, int NF> struct Rec {
 //   sr: wc0 wc1 wc2 pad                          (4 reals)
 static constexpr int SI = 8, SR = 4;
 
-// Level units: each level of direction q split into runs of at most kUnit elements.
+// Level units: each level of direction q split into runs of at most kUnit elements, and cut so that no
+// unit holds more than kUnitPf cut periodic inflow faces or kUnitSx output entries.  The per-unit
+// staging areas and the two periodic banks of the ring are sized by the largest unit; without the caps
+// the few units on the periodic boundaries (up to ~110 cut faces and outputs each on the 60k-triangle
+// cell) set them, and the extra ~5 KB cost a CTA per SM (4 instead of 5 at 8 MFPs per lane).
+constexpr int kUnitPf = 48;
+constexpr int kUnitSx = 64;
 struct Units {
   std::vector<int32_t> ptr;   // per direction: n[q] + 1 positions (relative to the direction)
   std::vector<int64_t> off;   // [n_dir] first entry of direction q in ptr (and in kpf, kwo)
@@ -81,11 +87,28 @@ static void build_units(const Schedule& s, Units& un) {
     un.off[q] = (int64_t)un.ptr.size();
     const int32_t* lp = s.lev_ptr.data() + s.lev_off[q];
     un.ptr.push_back(0);
-    for (int Lv = 0; Lv < s.nlev[q]; ++Lv)
-      for (int32_t a = lp[Lv]; a < lp[Lv + 1]; a += kUnit) {
-        un.ptr.push_back(std::min(a + kUnit, lp[Lv + 1]));
+    for (int Lv = 0; Lv < s.nlev[q]; ++Lv) {
+      int cnt = 0, npf = 0, nsx = 0;
+      for (int32_t pos = lp[Lv]; pos < lp[Lv + 1]; ++pos) {
+        const size_t it = (size_t)q * s.n + pos;
+        int pf = 0;
+        for (int f = 0; f < s.nf; ++f)
+          if ((int)((uint32_t)s.in_idx[it * s.nf + f] >> ITEM_SHIFT) == ITEM_PERIODIC) ++pf;
+        const int sx = (s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0) ? 1 : 0;
+        if (cnt > 0 && (cnt == kUnit || npf + pf > kUnitPf || nsx + sx > kUnitSx)) {
+          un.ptr.push_back(pos);
+          un.n[q]++;
+          cnt = npf = nsx = 0;
+        }
+        ++cnt;
+        npf += pf;
+        nsx += sx;
+      }
+      if (cnt > 0) {
+        un.ptr.push_back(lp[Lv + 1]);
         un.n[q]++;
       }
+    }
   }
 }
 
@@ -464,8 +487,15 @@ __device__ __forceinline__ T group_sum(T v, unsigned mask) {
 // a unit is owned by a group of G consecutive threads; lane l of the group computes the KV MFPs
 // [l KV, (l+1) KV) of the chunk.  The ring is [row][MC] (MFP fastest), so an upstream read is one
 // 16-byte shared load per lane and a group of 8 reads one full 128-byte row.
+// Resident CTAs per SM the register allocation is bounded for: 8 FP32 MFPs per lane would otherwise take
+// ~125 registers and hold an SM to 4 CTAs (a third wave of 32 CTAs on the 60k-triangle cell, 1,248 CTAs
+// over 608 slots); at 5 the 1,248 CTAs fit in two waves.  (Capping 4 FP32 MFPs per lane at 64 registers
+// made the 110k-tetrahedron sweep, held to 3 CTAs per SM by shared memory, 5 % slower.)
+template <typename Real, int G, int KV>
+struct SweepMinBlocks { static constexpr int v = (sizeof(Real) == 4 && G == 1 && KV == 8) ? 5 : 1; };
+
 template <typename Real, int NF, int G, int KV, bool FINAL>
-__global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<Real> p) {
+__global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte_sweep_kernel(const SweepParams<Real> p) {
   constexpr int RW = Rec<Real, NF>::W;           // record words
   constexpr int MC = G * KV;                     // MFPs per CTA
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
@@ -509,16 +539,20 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
   double* __restrict__ TB_out = p.u_out + p.n;
   double* __restrict__ X_out = p.u_out + p.n + p.nd;
 
-  // this lane's ordinate data in registers; padded MFPs get L = t = sigma = 0 (harmless T = b)
-  Real lam[KV], tt[KV], sg[KV][3];
+  // this lane's ordinate data in registers; padded MFPs get L = t = sigma = 0 (harmless T = b).
+  // sigma (wall re-emission and the final pass only) is read from shared memory: [MC][3]
+  Real lam[KV], tt[KV];
 #pragma unroll
   for (int j = 0; j < KV; ++j) {
     const bool ok = mo + j < mc;
     const int64_t m = m0 + mo + j;
     lam[j] = ok ? p.mfp[m] : Real(0);
     tt[j] = ok ? p.tco[(int64_t)q * p.m_pad + m] : Real(0);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) sg[j][d] = (ok && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m) * p.ds + d] : Real(0);
+  }
+  Real* s_sig = reinterpret_cast<Real*>(smem + L.sig);
+  for (int i = tid; i < MC * 3; i += blockDim.x) {
+    const int jj = i / 3, d = i - 3 * jj;
+    s_sig[i] = (jj < mc && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m0 + jj) * p.ds + d] : Real(0);
   }
   if (FINAL)
     for (int j = tid; j < MC; j += blockDim.x) { s_k[j] = 0; s_s[j] = 0; }
@@ -633,9 +667,10 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
           T[j] = (b + lam[j] * (pw - sm)) * recip(Real(1) + lam[j] * D);
           dacc += tt[j] * T[j];
           if (FINAL) {
-            j0 += sg[j][0] * T[j];
-            j1 += sg[j][1] * T[j];
-            j2 += sg[j][2] * T[j];
+            const Real* sj = s_sig + (mo + j) * 3;
+            j0 += sj[0] * T[j];
+            j1 += sj[1] * T[j];
+            j2 += sj[2] * T[j];
           }
         }
         vstore(ring + (size_t)so * MC + mo, T);
@@ -672,9 +707,10 @@ __global__ void __launch_bounds__(kUnit * G) bte_sweep_kernel(const SweepParams<
           Real w0 = 0, w1 = 0, w2 = 0;
 #pragma unroll
           for (int j = 0; j < KV; ++j) {
-            const Real a0 = sg[j][0] * gw[0] + sg[j][1] * gw[1] + sg[j][2] * gw[2];
-            const Real a1 = sg[j][0] * gw1[0] + sg[j][1] * gw1[1] + sg[j][2] * gw1[2];
-            const Real a2 = sg[j][0] * gw2[0] + sg[j][1] * gw2[1] + sg[j][2] * gw2[2];
+            const Real* sj = s_sig + (mo + j) * 3;
+            const Real a0 = sj[0] * gw[0] + sj[1] * gw[1] + sj[2] * gw[2];
+            const Real a1 = sj[0] * gw1[0] + sj[1] * gw1[1] + sj[2] * gw1[2];
+            const Real a2 = sj[0] * gw2[0] + sj[1] * gw2[1] + sj[2] * gw2[2];
             w0 += (a0 > Real(0) ? a0 * gw[3] : Real(0)) * T[j];
             w1 += (a1 > Real(0) ? a1 * gw1[3] : Real(0)) * T[j];
             w2 += (a2 > Real(0) ? a2 * gw2[3] : Real(0)) * T[j];
@@ -822,6 +858,12 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   d.nbuf = nbuf;
   d.unit_sx = pk.unit_sx;
   d.smem = SmemLayout<Real>(s.nf, mcp, rows, pk.unit_wo, pk.pf_pad, pk.unit_sx, nbuf).total;
+  if (timer.on)
+    std::fprintf(stderr, "[obte trace] sweep shape %s: G %d KV %d, %d chunks x %d directions = %d CTAs, %zu B shared "
+                 "memory (%d rows = %d slots + 2 + 2 x %d bank rows; staging per unit: %d wall entries, %d prefetch ints, %d "
+                 "output entries), <= %zu CTAs per SM by shared memory\n", sizeof(Real) == 4 ? "fp32" : "fp64", G,
+                 sh.KV, d.n_chunks, s.n_dir, d.n_chunks * s.n_dir, d.smem, rows, s.max_slots, pk.emax, pk.unit_wo,
+                 pk.pf_pad, pk.unit_sx, (size_t)(233472 / (d.smem + 1024)));
   OBTE_TRY(upload(d.rec, pk.rec, st));
   OBTE_TRY(upload(d.cellmap, pk.cellmap, st));
   OBTE_TRY(upload(d.Pq, pk.P, st));
