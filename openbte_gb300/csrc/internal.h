@@ -199,6 +199,7 @@ struct DevSchedule {
   size_t smem = 0;
   DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, sx, ksx, mfp, tco, sig, wo_wall, wo_geo, kcoef, scoef, hs, vals, cellmap,
       Pq, si, sr, wo_off, spec;
+  DevBuf lpt;                              // launch order: CTAs of the directions with the most units first
   size_t bytes() const;
 };
 
