@@ -70,16 +70,20 @@ __global__ void xprobe_set_kernel(int nblk, const int32_t* __restrict__ bm, cons
     if (j < bs[b]) x[xoff + (bbase[b] + j) * n_mfp + bm[b]] = v;
 }
 
+// W blocks are row-major with rows padded to a multiple of 4 floats (16-byte rows for vector loads);
+// the padding stays zero
+__host__ __device__ __forceinline__ int row_stride(int s) { return (s + 3) & ~3; }
+
 // column j of every block: W_b[i][j] = y[X(b, i)]
 __global__ void xprobe_get_kernel(const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
                                   const int64_t* __restrict__ bbase, const int64_t* __restrict__ bwoff, int n_mfp,
                                   int64_t xoff, int j, const double* __restrict__ y, float* __restrict__ W) {
   const int b = blockIdx.x;
-  const int s = bs[b];
+  const int s = bs[b], sp = row_stride(s);
   if (j >= s) return;
   float* Wb = W + bwoff[b];
   const int64_t base = xoff + bbase[b] * n_mfp + bm[b];
-  for (int i = threadIdx.x; i < s; i += blockDim.x) Wb[(int64_t)i * s + j] = (float)y[base + (int64_t)i * n_mfp];
+  for (int i = threadIdx.x; i < s; i += blockDim.x) Wb[(int64_t)i * sp + j] = (float)y[base + (int64_t)i * n_mfp];
 }
 
 // In place: W_b holds T_b on entry and (I - T_b)^-1 - I on exit (Gauss-Jordan without pivoting, FP32).
@@ -89,40 +93,41 @@ __global__ void __launch_bounds__(1024) xprec_invert_kernel(const int32_t* __res
                                                             int* __restrict__ bad) {
   __shared__ float colk[kMaxSlots];
   const int b = blockIdx.x;
-  const int s = bs[b];
+  const int s = bs[b], sp = row_stride(s);
   float* A = W + bwoff[b];
   const int64_t ss = (int64_t)s * s;
   for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) {
     const int i = (int)(e / s), j = (int)(e - (int64_t)i * s);
-    A[e] = (i == j ? 1.0f : 0.0f) - A[e];
+    A[(int64_t)i * sp + j] = (i == j ? 1.0f : 0.0f) - A[(int64_t)i * sp + j];
   }
   __syncthreads();
   for (int k = 0; k < s; ++k) {
-    for (int i = threadIdx.x; i < s; i += blockDim.x) colk[i] = A[(int64_t)i * s + k];
+    for (int i = threadIdx.x; i < s; i += blockDim.x) colk[i] = A[(int64_t)i * sp + k];
     __syncthreads();
     const float piv = colk[k];
     if (!(piv > 1e-5f)) {                       // same value in every thread: a uniform exit
-      for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) A[e] = 0.0f;
+      for (int64_t e = threadIdx.x; e < (int64_t)s * sp; e += blockDim.x) A[e] = 0.0f;
       if (threadIdx.x == 0) bad[b] = 1;
       return;
     }
     const float p = 1.0f / piv;
-    for (int j = threadIdx.x; j < s; j += blockDim.x) A[(int64_t)k * s + j] = (j == k) ? p : A[(int64_t)k * s + j] * p;
+    for (int j = threadIdx.x; j < s; j += blockDim.x) A[(int64_t)k * sp + j] = (j == k) ? p : A[(int64_t)k * sp + j] * p;
     __syncthreads();
     for (int64_t e = threadIdx.x; e < ss; e += blockDim.x) {
       const int i = (int)(e / s);
       if (i == k) continue;
       const int j = (int)(e - (int64_t)i * s);
-      A[e] = (j == k) ? -colk[i] * p : A[e] - colk[i] * A[(int64_t)k * s + j];
+      A[(int64_t)i * sp + j] = (j == k) ? -colk[i] * p : A[(int64_t)i * sp + j] - colk[i] * A[(int64_t)k * sp + j];
     }
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < s; i += blockDim.x) A[(int64_t)i * s + i] -= 1.0f;
+  for (int i = threadIdx.x; i < s; i += blockDim.x) A[(int64_t)i * sp + i] -= 1.0f;
 }
 
 // out[X(b, i)] += sum_j W_b[i][j] in[X(b, j)]: one CTA per block, the block's inflow staged in shared
-// memory, one warp per row (lane-strided products, fixed summation order).  Acc = float for stages
-// whose Krylov basis is FP32 (GB300's FP64 pipe would bound the FP64 form), double otherwise.
+// memory (zero-padded to the row stride), one warp per pair of rows, 16-byte loads of W (fixed summation
+// order).  Acc = float for stages whose Krylov basis is FP32 (GB300's FP64 pipe would bound the FP64
+// form), double otherwise.
 template <typename Acc>
 __global__ void xprec_apply_kernel(const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
                                    const int64_t* __restrict__ bbase, const int64_t* __restrict__ bwoff,
@@ -131,18 +136,33 @@ __global__ void xprec_apply_kernel(const int32_t* __restrict__ bm, const int32_t
   extern __shared__ double xin_raw[];
   Acc* xin = reinterpret_cast<Acc*>(xin_raw);
   const int b = blockIdx.x;
-  const int s = bs[b];
+  const int s = bs[b], sp = row_stride(s);
   const int64_t base = xoff + bbase[b] * n_mfp + bm[b];
-  for (int i = threadIdx.x; i < s; i += blockDim.x) xin[i] = (Acc)in[base + (int64_t)i * n_mfp];
+  for (int i = threadIdx.x; i < sp; i += blockDim.x) xin[i] = i < s ? (Acc)in[base + (int64_t)i * n_mfp] : Acc(0);
   __syncthreads();
   const float* Wb = W + bwoff[b];
   const int lane = threadIdx.x & 31;
-  for (int row = threadIdx.x >> 5; row < s; row += blockDim.x >> 5) {
-    const float* wr = Wb + (int64_t)row * s;
-    Acc acc = 0;
-    for (int j = lane; j < s; j += 32) acc += (Acc)wr[j] * xin[j];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) out[base + (int64_t)row * n_mfp] += (double)acc;
+  const int nw = blockDim.x >> 5;
+  const int q4 = sp >> 2;                                  // float4 per row
+  for (int r0 = 2 * (threadIdx.x >> 5); r0 < s; r0 += 2 * nw) {
+    const bool two = r0 + 1 < s;
+    const float4* w0 = reinterpret_cast<const float4*>(Wb + (int64_t)r0 * sp);
+    const float4* w1 = reinterpret_cast<const float4*>(Wb + (int64_t)(two ? r0 + 1 : r0) * sp);
+    Acc a0 = 0, a1 = 0;
+    for (int c = lane; c < q4; c += 32) {
+      const float4 u = w0[c], v = w1[c];
+      const Acc x0 = xin[4 * c], x1 = xin[4 * c + 1], x2 = xin[4 * c + 2], x3 = xin[4 * c + 3];
+      a0 += (Acc)u.x * x0 + (Acc)u.y * x1 + (Acc)u.z * x2 + (Acc)u.w * x3;
+      a1 += (Acc)v.x * x0 + (Acc)v.y * x1 + (Acc)v.z * x2 + (Acc)v.w * x3;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    }
+    if (lane == 0) {
+      out[base + (int64_t)r0 * n_mfp] += (double)a0;
+      if (two) out[base + (int64_t)(r0 + 1) * n_mfp] += (double)a1;
+    }
   }
 }
 
@@ -157,7 +177,7 @@ void xprec_add(obte_plan plan, const double* in, double* out, bool fp32) {
   if (P.nblk == 0) return;
   const Schedule& s = plan->sched;
   auto kern = fp32 ? xprec_apply_kernel<float> : xprec_apply_kernel<double>;
-  kern<<<P.nblk, XT, (size_t)P.smax * sizeof(double), plan->stream>>>(
+  kern<<<P.nblk, XT, (size_t)row_stride(P.smax) * sizeof(double), plan->stream>>>(
       P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(), P.bwoff.as<int64_t>(), P.W.as<float>(), s.n_mfp,
       s.n + s.nd, in, out);
   count_launch();
@@ -223,7 +243,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   double bytes = 0;
   size_t keep = 0;
   for (; keep < cand.size(); ++keep) {
-    const double bb = (double)cand[keep].slots * cand[keep].slots * sizeof(float);
+    const double bb = (double)cand[keep].slots * row_stride((int)cand[keep].slots) * sizeof(float);
     if (bytes + bb > kMaxBytes) break;
     bytes += bb;
   }
@@ -243,7 +263,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
     bsz[b] = (int32_t)cand[b].slots;
     bbase[b] = s.x_base[cand[b].q];
     bwoff[b] = woff;
-    woff += cand[b].slots * cand[b].slots;
+    woff += cand[b].slots * row_stride((int)cand[b].slots);
     smax = std::max(smax, (int)cand[b].slots);
   }
   OBTE_TRY(upload(P.bm, bm, st));
@@ -251,6 +271,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   OBTE_TRY(upload(P.bbase, bbase, st));
   OBTE_TRY(upload(P.bwoff, bwoff, st));
   OBTE_TRY(P.W.alloc((size_t)woff * sizeof(float)));
+  OBTE_CUDA(cudaMemsetAsync(P.W.p, 0, (size_t)woff * sizeof(float), st));   // row padding stays zero
   // 2. probing on the CTAs of the slow (direction, MFP chunk) pairs
   const DevSchedule& d = plan->d32;
   std::vector<int32_t> ctas;
