@@ -225,7 +225,8 @@ struct XPrec {
   int nblk = 0, smax = 0;
   int probe_sweeps = 0, detect_sweeps = 0;
   double setup_ms = 0;
-  DevBuf bm, bs, bbase, bwoff;   // per block: MFP, size (slots), first slot, offset of its W block
+  DevBuf bm, bs, boff, bwoff;    // per block: MFP, size (slots), first entry in bslot, offset of its W block
+  DevBuf bslot;                  // source slots of every block, concatenated
   DevBuf W;                      // FP32 row-major blocks
 };
 

@@ -13,7 +13,8 @@
 // Setup, once per plan (by default on its second solve: a plan solved once does not pay for it), with
 // FP32 sweeps of zero temperature and wall inputs, which isolate the inflow -> outflow map:
 //   1. detection: ten applications of the map to an all-ones inflow; an ordinate is slow when the
-//      last application kept more than 60 % of its inflow norm;
+//      last application kept more than 35 % of its inflow norm (and had not underflowed); its block
+//      covers the source slots that iterate reached;
 //   2. probing: for slot j of every slow ordinate's direction, a sweep of the unit inflow e_j gives
 //      column j of every slow block at once (the ordinates do not interact); only the CTAs of the
 //      slow (direction, MFP chunk) pairs run;
@@ -38,9 +39,12 @@ namespace {
 
 constexpr int XT = 256;
 constexpr int kDetect = 10;        // applications of the inflow map in the detection (OBTE_XPREC_DETECT)
-constexpr double kSlow = 0.6;      // norm kept by the last application above which an ordinate is slow
+constexpr double kSlow = 0.35;     // norm kept by the last application above which an ordinate is slow
                                    // (OBTE_XPREC_SLOW)
 constexpr int kMaxSlots = 1024;    // largest block
+constexpr double kActive = 0.0;    // slots of a block: detection iterate above this fraction of its largest
+                                   // (OBTE_XPREC_ACTIVE; 1e-3 took the largest block 348 -> 298 slots and
+                                   // the setup 400 -> 294 ms but cost a sweep per solve on the 60k cell)
 constexpr double kMaxBytes = 1.0e9;
 
 // per-ordinate sum of squares of the inflow part: out[q * n_mfp + m]
@@ -62,12 +66,14 @@ __global__ void fill_kernel(double* __restrict__ x, int64_t n, double v) {
   for (int64_t i = (int64_t)blockIdx.x * XT + threadIdx.x; i < n; i += (int64_t)gridDim.x * XT) x[i] = v;
 }
 
-// x[X(b, j)] = v for every block with j < s_b   (X(b, i) = xoff + (base_b + i) n_mfp + m_b)
+// Block b covers MFP m_b and the s_b source slots slot[off_b .. off_b + s_b) of its direction:
+// X(b, i) = xoff + slot[off_b + i] n_mfp + m_b.
+// x[X(b, j)] = v for every block with j < s_b
 __global__ void xprobe_set_kernel(int nblk, const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
-                                  const int64_t* __restrict__ bbase, int n_mfp, int64_t xoff, int j, double v,
-                                  double* __restrict__ x) {
+                                  const int64_t* __restrict__ boff, const int32_t* __restrict__ bslot, int n_mfp,
+                                  int64_t xoff, int j, double v, double* __restrict__ x) {
   for (int b = blockIdx.x * XT + threadIdx.x; b < nblk; b += gridDim.x * XT)
-    if (j < bs[b]) x[xoff + (bbase[b] + j) * n_mfp + bm[b]] = v;
+    if (j < bs[b]) x[xoff + (int64_t)bslot[boff[b] + j] * n_mfp + bm[b]] = v;
 }
 
 // W blocks are row-major with rows padded to a multiple of 4 floats (16-byte rows for vector loads);
@@ -76,14 +82,16 @@ __host__ __device__ __forceinline__ int row_stride(int s) { return (s + 3) & ~3;
 
 // column j of every block: W_b[i][j] = y[X(b, i)]
 __global__ void xprobe_get_kernel(const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
-                                  const int64_t* __restrict__ bbase, const int64_t* __restrict__ bwoff, int n_mfp,
-                                  int64_t xoff, int j, const double* __restrict__ y, float* __restrict__ W) {
+                                  const int64_t* __restrict__ boff, const int32_t* __restrict__ bslot,
+                                  const int64_t* __restrict__ bwoff, int n_mfp, int64_t xoff, int j,
+                                  const double* __restrict__ y, float* __restrict__ W) {
   const int b = blockIdx.x;
   const int s = bs[b], sp = row_stride(s);
   if (j >= s) return;
   float* Wb = W + bwoff[b];
-  const int64_t base = xoff + bbase[b] * n_mfp + bm[b];
-  for (int i = threadIdx.x; i < s; i += blockDim.x) Wb[(int64_t)i * sp + j] = (float)y[base + (int64_t)i * n_mfp];
+  const int32_t* sl = bslot + boff[b];
+  const int64_t mb = xoff + bm[b];
+  for (int i = threadIdx.x; i < s; i += blockDim.x) Wb[(int64_t)i * sp + j] = (float)y[mb + (int64_t)sl[i] * n_mfp];
 }
 
 // In place: W_b holds T_b on entry and (I - T_b)^-1 - I on exit (Gauss-Jordan without pivoting, FP32).
@@ -130,15 +138,16 @@ __global__ void __launch_bounds__(1024) xprec_invert_kernel(const int32_t* __res
 // form), double otherwise.
 template <typename Acc>
 __global__ void xprec_apply_kernel(const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
-                                   const int64_t* __restrict__ bbase, const int64_t* __restrict__ bwoff,
-                                   const float* __restrict__ W, int n_mfp, int64_t xoff, const double* __restrict__ in,
-                                   double* __restrict__ out) {
+                                   const int64_t* __restrict__ boff, const int32_t* __restrict__ bslot,
+                                   const int64_t* __restrict__ bwoff, const float* __restrict__ W, int n_mfp,
+                                   int64_t xoff, const double* __restrict__ in, double* __restrict__ out) {
   extern __shared__ double xin_raw[];
   Acc* xin = reinterpret_cast<Acc*>(xin_raw);
   const int b = blockIdx.x;
   const int s = bs[b], sp = row_stride(s);
-  const int64_t base = xoff + bbase[b] * n_mfp + bm[b];
-  for (int i = threadIdx.x; i < sp; i += blockDim.x) xin[i] = i < s ? (Acc)in[base + (int64_t)i * n_mfp] : Acc(0);
+  const int32_t* sl = bslot + boff[b];
+  const int64_t mb = xoff + bm[b];
+  for (int i = threadIdx.x; i < sp; i += blockDim.x) xin[i] = i < s ? (Acc)in[mb + (int64_t)sl[i] * n_mfp] : Acc(0);
   __syncthreads();
   const float* Wb = W + bwoff[b];
   const int lane = threadIdx.x & 31;
@@ -160,8 +169,8 @@ __global__ void xprec_apply_kernel(const int32_t* __restrict__ bm, const int32_t
       a1 += __shfl_xor_sync(0xffffffffu, a1, o);
     }
     if (lane == 0) {
-      out[base + (int64_t)r0 * n_mfp] += (double)a0;
-      if (two) out[base + (int64_t)(r0 + 1) * n_mfp] += (double)a1;
+      out[mb + (int64_t)sl[r0] * n_mfp] += (double)a0;
+      if (two) out[mb + (int64_t)sl[r0 + 1] * n_mfp] += (double)a1;
     }
   }
 }
@@ -178,8 +187,8 @@ void xprec_add(obte_plan plan, const double* in, double* out, bool fp32) {
   const Schedule& s = plan->sched;
   auto kern = fp32 ? xprec_apply_kernel<float> : xprec_apply_kernel<double>;
   kern<<<P.nblk, XT, (size_t)row_stride(P.smax) * sizeof(double), plan->stream>>>(
-      P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(), P.bwoff.as<int64_t>(), P.W.as<float>(), s.n_mfp,
-      s.n + s.nd, in, out);
+      P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(), P.bslot.as<int32_t>(), P.bwoff.as<int64_t>(),
+      P.W.as<float>(), s.n_mfp, s.n + s.nd, in, out);
   count_launch();
 }
 
@@ -208,6 +217,8 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   double slow = kSlow;
   if (const char* e = std::getenv("OBTE_XPREC_DETECT")) n_detect = std::max(2, std::atoi(e));
   if (const char* e = std::getenv("OBTE_XPREC_SLOW")) slow = std::atof(e);
+  double active = kActive;
+  if (const char* e = std::getenv("OBTE_XPREC_ACTIVE")) active = std::atof(e);
   const int64_t nord = (int64_t)s.n_dir * s.n_mfp;
   DevBuf nrm;
   OBTE_TRY(nrm.alloc((size_t)nord * 2 * sizeof(double)));
@@ -227,15 +238,36 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   OBTE_CUDA(cudaMemcpyAsync(hn.data(), nrm.p, hn.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
   OBTE_CUDA(cudaStreamSynchronize(st));
   P.detect_sweeps = n_detect;
-  struct Cand { int q, m; double ratio; int64_t slots; };
+  struct Cand { int q, m; double ratio; std::vector<int32_t> slots; };
   std::vector<Cand> cand;
+  std::vector<double> hx;
   for (int q = 0; q < s.n_dir; ++q) {
-    const int64_t slots = s.x_base[q + 1] - s.x_base[q];
-    if (slots == 0 || slots > kMaxSlots) continue;
+    const int64_t nsl = s.x_base[q + 1] - s.x_base[q];
+    if (nsl == 0) continue;
+    std::vector<int> ms;
     for (int m = 0; m < s.n_mfp; ++m) {
       const double a = hn[(size_t)q * s.n_mfp + m], b = hn[(size_t)nord + (size_t)q * s.n_mfp + m];
       const double ratio = a > 0 ? std::sqrt(b / a) : 0.0;
-      if (ratio > slow) cand.push_back({q, m, ratio, slots});
+      // fast ordinates' FP32 iterates underflow into denormals, where they stop shrinking (ratio ~1):
+      // only an inflow that kept more than 1e-12 of its initial norm (sum of squares = slots) counts
+      if (ratio > slow && b > 1e-24 * (double)nsl) ms.push_back(m);
+    }
+    if (ms.empty()) continue;
+    // the block covers the slots where the detection iterate (>= 0, near the slowest mode) is above
+    // `active` of its largest value (by default every slot it reached)
+    hx.resize((size_t)nsl * s.n_mfp);
+    OBTE_CUDA(cudaMemcpyAsync(hx.data(), x + xoff + s.x_base[q] * s.n_mfp, hx.size() * sizeof(double),
+                              cudaMemcpyDeviceToHost, st));
+    OBTE_CUDA(cudaStreamSynchronize(st));
+    for (int m : ms) {
+      double vmax = 0;
+      for (int64_t i = 0; i < nsl; ++i) vmax = std::max(vmax, hx[(size_t)i * s.n_mfp + m]);
+      Cand c{q, m, 0.0, {}};
+      const double a = hn[(size_t)q * s.n_mfp + m], b = hn[(size_t)nord + (size_t)q * s.n_mfp + m];
+      c.ratio = std::sqrt(b / a);
+      for (int64_t i = 0; i < nsl; ++i)
+        if (hx[(size_t)i * s.n_mfp + m] > active * vmax) c.slots.push_back((int32_t)(s.x_base[q] + i));
+      if (!c.slots.empty() && (int)c.slots.size() <= kMaxSlots) cand.push_back(std::move(c));
     }
   }
   // memory cap: keep the slowest blocks
@@ -243,7 +275,8 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   double bytes = 0;
   size_t keep = 0;
   for (; keep < cand.size(); ++keep) {
-    const double bb = (double)cand[keep].slots * row_stride((int)cand[keep].slots) * sizeof(float);
+    const int sz = (int)cand[keep].slots.size();
+    const double bb = (double)sz * row_stride(sz) * sizeof(float);
     if (bytes + bb > kMaxBytes) break;
     bytes += bb;
   }
@@ -254,21 +287,24 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
     return OBTE_OK;
   }
   const int nblk = (int)cand.size();
-  std::vector<int32_t> bm(nblk), bsz(nblk);
-  std::vector<int64_t> bbase(nblk), bwoff(nblk);
+  std::vector<int32_t> bm(nblk), bsz(nblk), bslot;
+  std::vector<int64_t> boff(nblk), bwoff(nblk);
   int64_t woff = 0;
   int smax = 0;
   for (int b = 0; b < nblk; ++b) {
+    const int sz = (int)cand[b].slots.size();
     bm[b] = cand[b].m;
-    bsz[b] = (int32_t)cand[b].slots;
-    bbase[b] = s.x_base[cand[b].q];
+    bsz[b] = sz;
+    boff[b] = (int64_t)bslot.size();
+    bslot.insert(bslot.end(), cand[b].slots.begin(), cand[b].slots.end());
     bwoff[b] = woff;
-    woff += cand[b].slots * row_stride((int)cand[b].slots);
-    smax = std::max(smax, (int)cand[b].slots);
+    woff += (int64_t)sz * row_stride(sz);
+    smax = std::max(smax, sz);
   }
   OBTE_TRY(upload(P.bm, bm, st));
   OBTE_TRY(upload(P.bs, bsz, st));
-  OBTE_TRY(upload(P.bbase, bbase, st));
+  OBTE_TRY(upload(P.boff, boff, st));
+  OBTE_TRY(upload(P.bslot, bslot, st));
   OBTE_TRY(upload(P.bwoff, bwoff, st));
   OBTE_TRY(P.W.alloc((size_t)woff * sizeof(float)));
   OBTE_CUDA(cudaMemsetAsync(P.W.p, 0, (size_t)woff * sizeof(float), st));   // row padding stays zero
@@ -288,14 +324,15 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   obte_status ps = OBTE_OK;
   const int sb = blocks_for(nblk, num_sms);
   for (int j = 0; j < smax && ps == OBTE_OK; ++j) {
-    xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(), s.n_mfp,
-                                         xoff, j, 1.0, x);
+    xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(),
+                                         P.bslot.as<int32_t>(), s.n_mfp, xoff, j, 1.0, x);
     ps = launch_sweep(plan, true, x, y, false, false, nullptr, nullptr, nullptr);
     if (ps != OBTE_OK) break;
-    xprobe_get_kernel<<<nblk, XT, 0, st>>>(P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(),
-                                           P.bwoff.as<int64_t>(), s.n_mfp, xoff, j, y, P.W.as<float>());
-    xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.bbase.as<int64_t>(), s.n_mfp,
-                                         xoff, j, 0.0, x);
+    xprobe_get_kernel<<<nblk, XT, 0, st>>>(P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(),
+                                           P.bslot.as<int32_t>(), P.bwoff.as<int64_t>(), s.n_mfp, xoff, j, y,
+                                           P.W.as<float>());
+    xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(),
+                                         P.bslot.as<int32_t>(), s.n_mfp, xoff, j, 0.0, x);
     count_launch(3);
   }
   plan->sweep_cta_map = nullptr;
