@@ -258,6 +258,8 @@ struct obte_plan_s {
   // non-final sweeps run only these CTAs (direction * n_chunks + chunk) while set (preconditioner setup)
   const int32_t* sweep_cta_map = nullptr;
   int sweep_n_cta = 0;
+  int sweep_batch = 1;                    // with the map: that many state vectors, sweep_batch_stride apart
+  int64_t sweep_batch_stride = 0;
   std::unique_ptr<obte::XPrec> xprec;     // periodic-inflow block preconditioner
   int n_solves = 0;                       // obte_bte_solve calls on this plan
 };

@@ -383,6 +383,11 @@ struct SweepParams {
   int* __restrict__ err;
   float* __restrict__ Xs;   // final pass only: per-ordinate temperatures [n_dir][n][n_mfp], or null
   const int32_t* __restrict__ cta_map;   // CTA -> direction * n_chunks + chunk (a subset), or null: all
+  // batched subset sweeps (batch_stride > 0): CTA b runs entry b % n_cta_batch of cta_map on the state
+  // vectors u_in / u_out + (b / n_cta_batch) batch_stride.  The batch shares one set of staged values
+  // (computed from the first state), so its states must agree on DeltaT and T_B.
+  int n_cta_batch;
+  int64_t batch_stride;
 };
 
 template <typename Real>
@@ -510,7 +515,14 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
   Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
   Real* ring = reinterpret_cast<Real*>(smem + L.ring);    // [rows][MC]
 
-  const int cta = p.cta_map ? p.cta_map[blockIdx.x] : (int)blockIdx.x;
+  int bid = (int)blockIdx.x;
+  int64_t boff = 0;
+  if (p.batch_stride > 0) {
+    const int bt = bid / p.n_cta_batch;
+    bid -= bt * p.n_cta_batch;
+    boff = (int64_t)bt * p.batch_stride;
+  }
+  const int cta = p.cta_map ? p.cta_map[bid] : bid;
   const int q = cta / p.n_chunks;
   const int chunk = cta - q * p.n_chunks;
   const int m0 = chunk * MC;
@@ -535,10 +547,10 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
   // wall weights of this (direction, chunk): [entry][MC], entries in sweep order
   const Real* __restrict__ gg_q = p.wo_geo + (int64_t)wo0 * 4;
   const int prow0 = p.S + 2;
-  const double* __restrict__ X = p.u_in + p.n + p.nd;
-  double* __restrict__ dT_out = p.u_out;
-  double* __restrict__ TB_out = p.u_out + p.n;
-  double* __restrict__ X_out = p.u_out + p.n + p.nd;
+  const double* __restrict__ X = p.u_in + boff + p.n + p.nd;
+  double* __restrict__ dT_out = p.u_out + boff;
+  double* __restrict__ TB_out = p.u_out + boff + p.n;
+  double* __restrict__ X_out = p.u_out + boff + p.n + p.nd;
 
   // this lane's ordinate data in registers; padded MFPs get L = t = sigma = 0 (harmless T = b).
   // sigma (wall re-emission and the final pass only) is read from shared memory: [MC][3]
@@ -976,7 +988,10 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   const bool subset = !FINAL && plan->sweep_cta_map != nullptr;
   static const bool index_order = std::getenv("OBTE_SWEEP_NO_LPT") != nullptr;   // plain index order
   p.cta_map = subset ? plan->sweep_cta_map : (index_order ? nullptr : d.lpt.as<int32_t>());
-  const int grid = subset ? plan->sweep_n_cta : s.n_dir * d.n_chunks;
+  const int batch = subset && plan->sweep_batch > 1 ? plan->sweep_batch : 1;
+  p.n_cta_batch = subset ? plan->sweep_n_cta : 0;
+  p.batch_stride = batch > 1 ? plan->sweep_batch_stride : 0;
+  const int grid = subset ? plan->sweep_n_cta * batch : s.n_dir * d.n_chunks;
   kern<<<grid, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
@@ -1106,6 +1121,8 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.err = err;
   p.Xs = nullptr;
   p.cta_map = nullptr;
+  p.n_cta_batch = 0;
+  p.batch_stride = 0;
   kern<<<s.n_dir * d.n_chunks, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());

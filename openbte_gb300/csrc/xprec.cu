@@ -68,25 +68,31 @@ __global__ void fill_kernel(double* __restrict__ x, int64_t n, double v) {
 
 // Block b covers MFP m_b and the s_b source slots slot[off_b .. off_b + s_b) of its direction:
 // X(b, i) = xoff + slot[off_b + i] n_mfp + m_b.
-// x[X(b, j)] = v for every block with j < s_b
+// probes j0 .. j0 + nj - 1 on the state vectors x + t stride (t = j - j0): x_t[X(b, j)] = v for every block
+// with j < s_b
 __global__ void xprobe_set_kernel(int nblk, const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
                                   const int64_t* __restrict__ boff, const int32_t* __restrict__ bslot, int n_mfp,
-                                  int64_t xoff, int j, double v, double* __restrict__ x) {
-  for (int b = blockIdx.x * XT + threadIdx.x; b < nblk; b += gridDim.x * XT)
-    if (j < bs[b]) x[xoff + (int64_t)bslot[boff[b] + j] * n_mfp + bm[b]] = v;
+                                  int64_t xoff, int j0, int nj, int64_t stride, double v, double* __restrict__ x) {
+  for (int e = blockIdx.x * XT + threadIdx.x; e < nblk * nj; e += gridDim.x * XT) {
+    const int b = e / nj, t = e - b * nj;
+    if (j0 + t < bs[b]) x[(int64_t)t * stride + xoff + (int64_t)bslot[boff[b] + j0 + t] * n_mfp + bm[b]] = v;
+  }
 }
 
 // W blocks are row-major with rows padded to a multiple of 4 floats (16-byte rows for vector loads);
 // the padding stays zero
 __host__ __device__ __forceinline__ int row_stride(int s) { return (s + 3) & ~3; }
 
-// column j of every block: W_b[i][j] = y[X(b, i)]
+// column j = j0 + blockIdx.y of every block (blockIdx.x) from the state y + blockIdx.y stride:
+// W_b[i][j] = y[X(b, i)]
 __global__ void xprobe_get_kernel(const int32_t* __restrict__ bm, const int32_t* __restrict__ bs,
                                   const int64_t* __restrict__ boff, const int32_t* __restrict__ bslot,
-                                  const int64_t* __restrict__ bwoff, int n_mfp, int64_t xoff, int j,
-                                  const double* __restrict__ y, float* __restrict__ W) {
+                                  const int64_t* __restrict__ bwoff, int n_mfp, int64_t xoff, int j0, int64_t stride,
+                                  const double* __restrict__ ybase, float* __restrict__ W) {
   const int b = blockIdx.x;
   const int s = bs[b], sp = row_stride(s);
+  const int j = j0 + (int)blockIdx.y;
+  const double* __restrict__ y = ybase + (int64_t)blockIdx.y * stride;
   if (j >= s) return;
   float* Wb = W + bwoff[b];
   const int32_t* sl = bslot + boff[b];
@@ -318,27 +324,41 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   ctas.erase(std::unique(ctas.begin(), ctas.end()), ctas.end());
   DevBuf cmap;
   OBTE_TRY(upload(cmap, ctas, st));
-  OBTE_CUDA(cudaMemsetAsync(x, 0, (size_t)nu * sizeof(double), st));
+  // a probe sweep runs only these CTAs (one chain each, a small part of the GPU): `nbat` probes share a
+  // launch, each on its own pair of state vectors (all with zero DeltaT and T_B, as batching requires)
+  const int nbat = (int)std::max<int64_t>(
+      1, std::min<int64_t>({16, (int64_t)num_sms * 4 / (int64_t)ctas.size(), (int64_t)(2e9 / (16.0 * (double)nu))}));
+  DevBuf xb, yb;
+  OBTE_TRY(xb.alloc((size_t)nbat * nu * sizeof(double)));
+  OBTE_TRY(yb.alloc((size_t)nbat * nu * sizeof(double)));
+  OBTE_CUDA(cudaMemsetAsync(xb.p, 0, (size_t)nbat * nu * sizeof(double), st));
   plan->sweep_cta_map = cmap.as<int32_t>();
   plan->sweep_n_cta = (int)ctas.size();
+  plan->sweep_batch_stride = nu;
   obte_status ps = OBTE_OK;
-  const int sb = blocks_for(nblk, num_sms);
-  for (int j = 0; j < smax && ps == OBTE_OK; ++j) {
+  int launches = 0;
+  for (int j0 = 0; j0 < smax && ps == OBTE_OK; j0 += nbat) {
+    const int nj = std::min(nbat, smax - j0);
+    const int sb = blocks_for((int64_t)nblk * nj, num_sms);
+    plan->sweep_batch = nj;
     xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(),
-                                         P.bslot.as<int32_t>(), s.n_mfp, xoff, j, 1.0, x);
-    ps = launch_sweep(plan, true, x, y, false, false, nullptr, nullptr, nullptr);
+                                         P.bslot.as<int32_t>(), s.n_mfp, xoff, j0, nj, nu, 1.0, xb.as<double>());
+    ps = launch_sweep(plan, true, xb.as<double>(), yb.as<double>(), false, false, nullptr, nullptr, nullptr);
     if (ps != OBTE_OK) break;
-    xprobe_get_kernel<<<nblk, XT, 0, st>>>(P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(),
-                                           P.bslot.as<int32_t>(), P.bwoff.as<int64_t>(), s.n_mfp, xoff, j, y,
-                                           P.W.as<float>());
+    ++launches;
+    xprobe_get_kernel<<<dim3(nblk, nj), XT, 0, st>>>(P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(),
+                                                     P.bslot.as<int32_t>(), P.bwoff.as<int64_t>(), s.n_mfp, xoff, j0,
+                                                     nu, yb.as<double>(), P.W.as<float>());
     xprobe_set_kernel<<<sb, XT, 0, st>>>(nblk, P.bm.as<int32_t>(), P.bs.as<int32_t>(), P.boff.as<int64_t>(),
-                                         P.bslot.as<int32_t>(), s.n_mfp, xoff, j, 0.0, x);
+                                         P.bslot.as<int32_t>(), s.n_mfp, xoff, j0, nj, nu, 0.0, xb.as<double>());
     count_launch(3);
   }
   plan->sweep_cta_map = nullptr;
   plan->sweep_n_cta = 0;
+  plan->sweep_batch = 1;
+  plan->sweep_batch_stride = 0;
   OBTE_TRY(ps);
-  P.probe_sweeps = smax;
+  P.probe_sweeps = launches;
   // 3. (I - T)^-1 - I per block
   DevBuf bad;
   OBTE_TRY(bad.alloc((size_t)nblk * sizeof(int)));
@@ -352,8 +372,8 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   P.smax = smax;
   P.setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (timer.on)
-    std::fprintf(stderr, "[obte trace] xprec: %d blocks (largest %d slots), %zu CTAs per probe, %d probe sweeps\n",
-                 nblk, smax, ctas.size(), smax);
+    std::fprintf(stderr, "[obte trace] xprec: %d blocks (largest %d slots), %zu CTAs per probe, %d probes in %d "
+                 "batched sweeps of %d\n", nblk, smax, ctas.size(), smax, P.probe_sweeps, nbat);
   return OBTE_OK;
 }
 
