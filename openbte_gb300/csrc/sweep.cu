@@ -673,17 +673,50 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
         if (NF > 3) vload(ring + (size_t)s3 * MC + mo, v3);
         Real T[KV];
         Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
+        if constexpr (sizeof(Real) == 4 && KV % 2 == 0) {
+          // FP32: the MFPs in pairs with Blackwell's packed FP32x2 arithmetic (one instruction per two MFPs;
+          // each lane of a packed operation rounds like the scalar one)
+          const float2 C0 = make_float2(c0, c0), C1 = make_float2(c1, c1), C2 = make_float2(c2, c2);
+          const float2 C3 = make_float2(c3, c3), DD = make_float2(D, D), BB = make_float2(b, b);
+          const float2 PW = make_float2(pw, pw), ONE = make_float2(1.0f, 1.0f), NEG = make_float2(-1.0f, -1.0f);
+          float2 da = make_float2(0.0f, 0.0f), ja = da, jb = da, jc = da;
 #pragma unroll
-        for (int j = 0; j < KV; ++j) {
-          Real sm = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
-          if (NF > 3) sm += c3 * v3[j];
-          T[j] = quot(b + lam[j] * (pw - sm), Real(1) + lam[j] * D);
-          dacc += tt[j] * T[j];
-          if (FINAL) {
-            const Real* sj = s_sig + (mo + j) * 3;
-            j0 += sj[0] * T[j];
-            j1 += sj[1] * T[j];
-            if (p.ds > 2) j2 += sj[2] * T[j];
+          for (int j = 0; j < KV; j += 2) {
+            float2 sm = __fmul2_rn(C0, make_float2(v0[j], v0[j + 1]));
+            sm = __ffma2_rn(C1, make_float2(v1[j], v1[j + 1]), sm);
+            sm = __ffma2_rn(C2, make_float2(v2[j], v2[j + 1]), sm);
+            if (NF > 3) sm = __ffma2_rn(C3, make_float2(v3[j], v3[j + 1]), sm);
+            const float2 lm = make_float2(lam[j], lam[j + 1]);
+            const float2 num = __ffma2_rn(lm, __ffma2_rn(NEG, sm, PW), BB);    // b + L (pw - sm)
+            const float2 den = __ffma2_rn(lm, DD, ONE);                        // 1 + L D
+            const float2 t2 = __fmul2_rn(num, make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y)));
+            T[j] = t2.x;
+            T[j + 1] = t2.y;
+            da = __ffma2_rn(make_float2(tt[j], tt[j + 1]), t2, da);
+            if (FINAL) {
+              const Real* sj = s_sig + (mo + j) * 3;
+              ja = __ffma2_rn(make_float2(sj[0], sj[3]), t2, ja);
+              jb = __ffma2_rn(make_float2(sj[1], sj[4]), t2, jb);
+              if (p.ds > 2) jc = __ffma2_rn(make_float2(sj[2], sj[5]), t2, jc);
+            }
+          }
+          dacc = da.x + da.y;
+          j0 = ja.x + ja.y;
+          j1 = jb.x + jb.y;
+          j2 = jc.x + jc.y;
+        } else {
+#pragma unroll
+          for (int j = 0; j < KV; ++j) {
+            Real sm = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
+            if (NF > 3) sm += c3 * v3[j];
+            T[j] = quot(b + lam[j] * (pw - sm), Real(1) + lam[j] * D);
+            dacc += tt[j] * T[j];
+            if (FINAL) {
+              const Real* sj = s_sig + (mo + j) * 3;
+              j0 += sj[0] * T[j];
+              j1 += sj[1] * T[j];
+              if (p.ds > 2) j2 += sj[2] * T[j];
+            }
           }
         }
         vstore(ring + (size_t)so * MC + mo, T);
