@@ -125,8 +125,10 @@ class GPUBackend:
         pl.set_stream(st.cuda_stream)
         with torch.cuda.stream(st):
             dT0 = torch.zeros(pl.n, dtype=torch.float64, device=f"cuda:{self.device}")
+            # the periodic-inflow preconditioner stays off: its blocks and set-up buffers are not part of the
+            # footprint a request is admitted by (and a request's plan is usually solved once)
             info, *_ = solve_plan(pl, dT0, precision=req.precision, rtol=req.rtol, max_sweeps=self.max_sweeps,
-                                  restart=self.restart, warm_start=req.warm_start)
+                                  restart=self.restart, warm_start=req.warm_start, precond=-1)
         st.synchronize()
         return {"kappa": info.kappa_eff, "converged": bool(info.converged), "n_sweeps": info.n_sweeps,
                 "n_sweeps_fp64": info.n_sweeps_fp64}
