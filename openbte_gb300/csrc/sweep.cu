@@ -70,7 +70,10 @@ static constexpr int SI = 8, SR = 4;
 // unit holds more than kUnitPf cut periodic inflow faces or kUnitSx output entries.  The per-unit
 // staging areas and the two periodic banks of the ring are sized by the largest unit; without the caps
 // the few units on the periodic boundaries (up to ~110 cut faces and outputs each on the 60k-triangle
-// cell) set them, and the extra ~5 KB cost a CTA per SM (4 instead of 5 at 8 MFPs per lane).
+// cell) set them, and the extra ~5 KB cost a CTA per SM (4 instead of 5 at 8 MFPs per lane).  A cap only
+// applies when at most 1 % of the uncapped units exceed it: where most units are over it (the pixel
+// model, where every element has reflecting-wall outputs) it would split every unit and lengthen every
+// chain instead.
 constexpr int kUnitPf = 48;
 constexpr int kUnitSx = 64;
 struct Units {
@@ -79,37 +82,50 @@ struct Units {
   std::vector<int32_t> n;     // [n_dir] units of direction q
 };
 
-static void build_units(const Schedule& s, Units& un) {
+static void build_units_capped(const Schedule& s, int cap_pf, int cap_sx, Units& un, int64_t* over_pf,
+                               int64_t* over_sx) {
   un.ptr.clear();
   un.off.assign(s.n_dir, 0);
   un.n.assign(s.n_dir, 0);
+  if (over_pf) *over_pf = 0;
+  if (over_sx) *over_sx = 0;
   for (int q = 0; q < s.n_dir; ++q) {
     un.off[q] = (int64_t)un.ptr.size();
     const int32_t* lp = s.lev_ptr.data() + s.lev_off[q];
     un.ptr.push_back(0);
     for (int Lv = 0; Lv < s.nlev[q]; ++Lv) {
       int cnt = 0, npf = 0, nsx = 0;
+      auto close = [&](int32_t end) {
+        un.ptr.push_back(end);
+        un.n[q]++;
+        if (over_pf && npf > kUnitPf) ++*over_pf;
+        if (over_sx && nsx > kUnitSx) ++*over_sx;
+        cnt = npf = nsx = 0;
+      };
       for (int32_t pos = lp[Lv]; pos < lp[Lv + 1]; ++pos) {
         const size_t it = (size_t)q * s.n + pos;
         int pf = 0;
         for (int f = 0; f < s.nf; ++f)
           if ((int)((uint32_t)s.in_idx[it * s.nf + f] >> ITEM_SHIFT) == ITEM_PERIODIC) ++pf;
         const int sx = (s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0) ? 1 : 0;
-        if (cnt > 0 && (cnt == kUnit || npf + pf > kUnitPf || nsx + sx > kUnitSx)) {
-          un.ptr.push_back(pos);
-          un.n[q]++;
-          cnt = npf = nsx = 0;
-        }
+        if (cnt > 0 && (cnt == kUnit || npf + pf > cap_pf || nsx + sx > cap_sx)) close(pos);
         ++cnt;
         npf += pf;
         nsx += sx;
       }
-      if (cnt > 0) {
-        un.ptr.push_back(lp[Lv + 1]);
-        un.n[q]++;
-      }
+      if (cnt > 0) close(lp[Lv + 1]);
     }
   }
+}
+
+static void build_units(const Schedule& s, Units& un) {
+  constexpr int kNone = 1 << 30;
+  int64_t over_pf = 0, over_sx = 0;
+  build_units_capped(s, kNone, kNone, un, &over_pf, &over_sx);
+  const int64_t units = (int64_t)un.ptr.size() - s.n_dir;
+  const int cap_pf = over_pf * 100 <= units ? kUnitPf : kNone;
+  const int cap_sx = over_sx * 100 <= units ? kUnitSx : kNone;
+  if (cap_pf != kNone || cap_sx != kNone) build_units_capped(s, cap_pf, cap_sx, un, nullptr, nullptr);
 }
 
 struct Packed {
