@@ -761,7 +761,20 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   if (const char* e = std::getenv("OBTE_XPREC")) pmode = std::atoi(e) == 0 ? -1 : 1;
   const bool build_xp = pmode == 1 || (pmode == 0 && plan->n_solves >= 1);
   ++plan->n_solves;
-  if (build_xp) OBTE_TRY(ensure_xprec(plan, wk));
+  if (build_xp) {
+    // a preconditioner that does not fit in device memory is left out: the solve runs without it
+    const obte_status xs = ensure_xprec(plan, wk);
+    if (xs == OBTE_ERR_OOM) {
+      plan->xprec->nblk = 0;
+      plan->xprec->W.release();
+      plan->sweep_cta_map = nullptr;
+      plan->sweep_n_cta = 0;
+      plan->sweep_batch = 1;
+      plan->sweep_batch_stride = 0;
+    } else {
+      OBTE_TRY(xs);
+    }
+  }
   const bool use_xp = pmode >= 0 && plan->xprec && plan->xprec->nblk > 0;
   if (use_xp && !wk.pz.p) OBTE_TRY(wk.pz.alloc((size_t)wk.nu * sizeof(double)));
   plan->has_solution = false;
