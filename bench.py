@@ -410,6 +410,8 @@ def main():
                     help="only build the plan and run this many FP32 and FP64 sweeps (for ncu captures)")
     ap.add_argument("--profile-fourier", type=int, default=0,
                     help="only build the Fourier plan and run this many Fourier first-guess solves")
+    ap.add_argument("--profile-solves", type=int, default=0,
+                    help="only build the plan and run this many kappa_eff solves (for launch lists)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -461,6 +463,21 @@ def main():
     plan = get_plan(hp, local)
     plan_s = time.time() - t0
     n_mfp, n_dir = np.asarray(mat.t_coeff).shape
+    if args.profile_solves:
+        dT0 = torch.zeros(geo.n_elems, dtype=torch.float64, device=dev)
+        out = []
+        for i in range(args.profile_solves):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            info, *_ = solve_plan(plan, dT0, precision=args.precision, rtol=args.rtol, max_sweeps=2000, restart=40)
+            ev[1].record()
+            ev[1].synchronize()
+            out.append({"ms": ev[0].elapsed_time(ev[1]), "sweeps": info.n_sweeps, "kappa": info.kappa_eff})
+        pb, ps, pms = C.c_int32(), C.c_int32(), C.c_double()
+        _lib.check(lib.obte_bte_precond_info(plan.handle, C.byref(pb), C.byref(ps), C.byref(pms)), "precond_info")
+        print(json.dumps({"profile_solves": out, "workload": args.workload, "precision": args.precision,
+                          "preconditioner": {"blocks": pb.value, "setup_sweeps": ps.value, "setup_ms": pms.value}}))
+        return
     if args.profile_sweeps:
         u = torch.zeros(plan.nu, dtype=torch.float64, device=dev)
         uo = torch.zeros_like(u)
