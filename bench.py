@@ -39,6 +39,10 @@ WORKLOADS = {
     "c4_inverse_128x50x64": (128, 50, 64, None, "pixels", 0),
 }
 L2_BYTES = 129 * 1024 * 1024
+# DRAM bytes (read + write) of one FP32 sweep launch, from one ncu capture of `bench.py --profile-sweeps 2`
+# (dram__bytes.sum.per_second x gpu__time_duration): 154.7 GB/s x 1.852 ms.  The iterate stays in shared
+# memory, so this is about an eighth of the algorithmic bytes.
+SWEEP_DRAM_BYTES = {"c1_60k_100x96": 2.866e8}
 
 
 def problem(workload):
@@ -629,7 +633,10 @@ def main():
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(round(launches)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "bte_sweep_kernel", "ms_per_launch": t_sweep * 1e3,
+                     "traffic": SWEEP_DRAM_BYTES.get(args.workload) if fp32 else None,
+                     "traffic_source": "ncu dram__bytes of one FP32 sweep launch (profiles/bte_sweep_fp32_c1_60k_100x96.md)"
+                     if fp32 and args.workload in SWEEP_DRAM_BYTES else None,
+                     "kernel": "bte_sweep_kernel", "ms_per_launch": t_sweep * 1e3,
                      "algorithmic_bytes": int(bytes_sweep), "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "clocks": clk.summary(),
         "plan_build_s": plan_s,
