@@ -206,13 +206,21 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   const Schedule& s = plan->sched;
   const int64_t nsrc = s.x_base[s.n_dir];
   if (nsrc == 0 || s.n_mfp == 0) return OBTE_OK;
+  // a block spans at most all source slots of its direction: nothing to build where every direction has
+  // more than kMaxSlots (the 3D meshes' periodic faces)
+  bool any_fits = false;
+  for (int q = 0; q < s.n_dir && !any_fits; ++q) {
+    const int64_t nsl = s.x_base[q + 1] - s.x_base[q];
+    any_fits = nsl > 0 && nsl <= kMaxSlots;
+  }
+  if (!any_fits) return OBTE_OK;
+  OBTE_TRY(ensure_tables(plan, true));
   PhaseTimer timer("xprec setup");
   const auto t0 = std::chrono::steady_clock::now();
   cudaStream_t st = plan->stream;
   const int num_sms = plan->ctx->num_sms;
   const int64_t xoff = s.n + s.nd;
   const int64_t nu = plan->nu;
-  OBTE_TRY(ensure_tables(plan, true));
   double* x = wk.tmp.as<double>();
   double* y = wk.w.as<double>();
   // 1. detection: inflow map applied to an all-ones inflow
