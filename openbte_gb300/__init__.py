@@ -6,7 +6,7 @@ transport path: ``BTE_RTA``, ``Fourier``, ``get_mesh`` and the data types.
 from .objects import (BoundaryConditions, EffectiveThermalConductivity, Material, Mesh,  # noqa: F401
                       SolverResults)
 from .mesh import get_mesh  # noqa: F401
-from .material import Gray2D, synthetic_isotropic_2d, synthetic_isotropic_3d  # noqa: F401
+from .material import Gray2D, RTA2DSym, RTA3D, load_rta, synthetic_isotropic_2d, synthetic_isotropic_3d  # noqa: F401
 
 
 def __getattr__(name):

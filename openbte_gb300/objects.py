@@ -121,6 +121,21 @@ class SolverResults(NamedTuple):
     variables: dict = {}
 
 
+class MaterialRTA(NamedTuple):
+    """Mode-resolved bulk data of a material in the relaxation-time approximation (openbte/objects.py:114-120).
+
+    heat_capacity [n_modes] J/m^3/K, scattering_time [n_modes] s, group_velocity [n_modes, 3] m/s,
+    frequency [n_modes], thermal_conductivity [3, 3] W/m/K (the last two are carried, not used by the
+    binning).
+    """
+
+    heat_capacity: np.ndarray
+    scattering_time: np.ndarray
+    group_velocity: np.ndarray
+    frequency: np.ndarray = np.zeros(0)
+    thermal_conductivity: np.ndarray = np.zeros(0)
+
+
 class Material(NamedTuple):
     """Ordinate data (openbte/objects.py:500-509).
 

@@ -218,3 +218,100 @@ def solve_ordinate(geo, mat, bcs, q, m, B):
     ops = setup_operators(geo, mat, bcs)
     s = OrdinateSolver(geo, np.asarray(mat.mfps, dtype=np.float64), ops)
     return s.solve(q, m, B)
+
+
+def _one_pass(ops, solver, mat, ct, dT, TB, with_source, hs=None):
+    """The reference's per-ordinate solves and reductions at the state (DeltaT, T_B) (openbte/bte.py:199-249);
+    with_source=False leaves out the periodic-jump and heat sources (the linear part of the map)."""
+    n = len(dT)
+    mfps = np.asarray(mat.mfps, dtype=np.float64)
+    t_coeff = np.asarray(mat.t_coeff)
+    n_mfp = len(mfps)
+    idf = ops["i_diffuse"]
+    nd = len(idf)
+    boundary = -TB[None, :] * ops["Gbm2"] if nd > 0 else None
+    pT, pTB = np.zeros(n), np.zeros(nd)
+    pJ = np.zeros((n, np.asarray(mat.vmfp).shape[1]))
+    pK = np.zeros((n_mfp, ops["n_angles"]))
+    pS = np.zeros_like(pK)
+    for q in range(ops["n_angles"]):
+        for m, mfp in enumerate(mfps):
+            B = dT.copy()
+            if with_source:
+                B += mfp * ops["perturbation"][q]
+                if hs is not None:
+                    B += hs * mat.heat_source_coeff
+            if nd > 0:
+                np.add.at(B, idf, mfp * boundary[q])
+            T = solver.solve(q, m, B)
+            pT += t_coeff[m, q] * T
+            if nd > 0:
+                pTB -= T[idf] * ops["GG"][m, q]
+            pJ += np.outer(T - dT, mat.sigma[m, q])
+            if ct is not None and with_source:
+                sn = ct["sigma_normal"][m, q]
+                nrm = ct["normalization"]
+                if ct["is_nanowire"]:
+                    pK[m, q] = np.dot(T[ct["e1"]], sn) * nrm
+                else:
+                    pK[m, q] = np.dot(T[ct["e1"]], sn.clip(min=0)) * nrm
+                    pS[m, q] = np.dot(T[ct["e1"]], ct["side_areas"]) * nrm
+                if len(ct["e2"]) > 0:
+                    pK[m, q] += np.dot(T[ct["e2"]], sn.clip(max=0)) * nrm
+                pK[m, q] += ct["alpha"] * np.sum(sn.clip(max=0)) * nrm
+    return pT, pTB, pJ, pK, pS
+
+
+def bte_rta_krylov(geo, mat, bcs, effective_thermal_conductivity=None, rtol=1e-12, restart=80, max_matvec=800):
+    """The fixed point of the reference's source iteration (openbte/bte.py:193-256), found by restarted GMRES on
+    (I - K) u = f, u = (DeltaT, T_B), with the same exact per-ordinate solves and reductions.
+
+    For materials whose plain iteration is too slow to converge (long or very short MFPs).  The fixed point is
+    defined up to a uniform shift of every temperature (which the reference's iteration fixes by its starting
+    point): compare kappa, J and the volume-mean-free DeltaT.  Returns (kappa_eff, DeltaT, J, K, S, n_matvec).
+    """
+    ops = setup_operators(geo, mat, bcs)
+    n = geo.n_elems
+    nd = len(ops["i_diffuse"])
+    ek = effective_thermal_conductivity
+    ct = contact_terms(geo, mat, bcs, ek) if ek is not None else None
+    solver = OrdinateSolver(geo, np.asarray(mat.mfps, dtype=np.float64), ops)
+
+    def F(u, src):
+        pT, pTB, *_ = _one_pass(ops, solver, mat, None, u[:n], u[n:], src)
+        return np.concatenate([pT, pTB])
+
+    f = F(np.zeros(n + nd), True)
+    fn = np.linalg.norm(f)
+    x = np.zeros(n + nd)
+    mv = 0
+    while mv < max_matvec:
+        r = f - (x - F(x, False)) if mv else f.copy()
+        mv += 1 if mv else 0
+        beta = np.linalg.norm(r)
+        if beta <= rtol * fn:
+            break
+        V = [r / beta]
+        H = np.zeros((restart + 1, restart))
+        g = np.zeros(restart + 1)
+        g[0] = beta
+        y = np.zeros(0)
+        for j in range(restart):
+            w = V[j] - F(V[j], False)
+            mv += 1
+            for _ in range(2):                       # Gram-Schmidt twice
+                for i in range(j + 1):
+                    h = V[i] @ w
+                    H[i, j] += h
+                    w = w - h * V[i]
+            H[j + 1, j] = np.linalg.norm(w)
+            V.append(w / H[j + 1, j] if H[j + 1, j] > 0 else w)
+            y, *_ = np.linalg.lstsq(H[:j + 2, :j + 1], g[:j + 2], rcond=None)
+            res = np.linalg.norm(g[:j + 2] - H[:j + 2, :j + 1] @ y)
+            if res <= rtol * fn or H[j + 1, j] == 0 or mv >= max_matvec:
+                break
+        x = x + sum(y[k] * V[k] for k in range(len(y)))
+        if res <= rtol * fn:
+            break
+    pT, pTB, pJ, pK, pS = _one_pass(ops, solver, mat, ct, x[:n], x[n:], True)
+    return float(np.sum(pK)), pT, pJ, pK, pS, mv
