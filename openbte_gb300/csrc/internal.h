@@ -182,6 +182,8 @@ struct Schedule {
   std::vector<char> tim_contact;             // [ni] 1 = contact side
   double contact_alpha = 0, normalization = 0;
   bool extra_sources = false;                // isothermal walls, heat source or nanowire terms
+  bool isothermal = false;                   // isothermal (mixed) walls: they fix the temperature level, so
+                                             // I - K has no constant null mode and no offset is applied
 };
 
 obte_status build_schedule(const obte_problem* prob, const obte_material* mat, Schedule& s);

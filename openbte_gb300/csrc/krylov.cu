@@ -13,6 +13,8 @@
 // A_w sum_mq t_mq L_m |min(s_q.n_w, 0)|), the left null vector of I - K; the
 // converged state is therefore shifted by a constant so that ell.u equals its
 // value at the initial guess, reproducing the reference's temperature level.
+// Isothermal (mixed) walls emit at a fixed temperature: the constant mode is
+// then not a fixed point, the solution is unique and no shift is applied.
 //
 // Precision modes: FP64 sweeps; FP32 sweeps; FP32 sweeps inside an iterative
 // refinement whose residual F(u) - u is evaluated with FP64 sweeps.  The
@@ -866,10 +868,12 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
       OBTE_CUDA(cudaGetLastError());
     }
   }
-  // offset: ell.(Fu + c) = ell0
-  OBTE_TRY(sv.multidot(Fu, 1, plan->ell.as<double>(), h));
-  const double ellF = h[0];
-  const double c = (ell0 - ellF) / plan->ell_sum;
+  // offset: ell.(Fu + c) = ell0 (none with isothermal walls, whose fixed point is unique)
+  double c = 0;
+  if (!s.isothermal) {
+    OBTE_TRY(sv.multidot(Fu, 1, plan->ell.as<double>(), h));
+    c = (ell0 - h[0]) / plan->ell_sum;
+  }
   const double s0 = s.ds > 0 ? s.sig_sum[0] : 0, s1 = s.ds > 1 ? s.sig_sum[1] : 0, s2 = s.ds > 2 ? s.sig_sum[2] : 0;
   finalize_kernel<<<wk.nb, VT, 0, st>>>(Fu, u, s.n, c, wk.Jraw.as<double>(), s.ds, s0, s1, s2,
                                         wk.Kraw.as<double>(), wk.Sraw.as<double>(), plan->kconst.as<double>(),

@@ -224,6 +224,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.tim = pb->side_transmission != nullptr;
   s.contact_alpha = pb->contact_alpha;
   s.extra_sources = pb->n_mixed > 0 || pb->is_nanowire || pb->heat_source != nullptr;
+  s.isothermal = pb->n_mixed > 0;
   s.normalization = nrm;
   if (s.tim) {
     std::vector<double> jump_of(ns, 0.0);
