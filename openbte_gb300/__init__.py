@@ -7,6 +7,8 @@ from .objects import (BoundaryConditions, EffectiveThermalConductivity, Material
                       SolverResults)
 from .mesh import get_mesh  # noqa: F401
 from .material import Gray2D, RTA2DSym, RTA3D, load_rta, synthetic_isotropic_2d, synthetic_isotropic_3d  # noqa: F401
+from .objects import MaterialRTA  # noqa: F401
+from .results import OpenBTEResults  # noqa: F401
 
 
 def __getattr__(name):
