@@ -210,8 +210,27 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
   pk.P.assign(total, 0.0);
   pk.si.clear();
   pk.sr.clear();
-  // pass 2: records
-  for (int q = 0; q < s.n_dir; ++q) {
+  // pass 2: records, in parallel over directions.  Elements with outputs or wall inflow get a "special"
+  // entry (si/sr); a first sweep counts them per direction so every direction writes its own range.
+  auto is_special = [&](size_t it) {
+    if (s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0) return true;
+    for (int f = 0; f < s.nf; ++f)
+      if ((int)((uint32_t)s.in_idx[it * s.nf + f] >> ITEM_SHIFT) == ITEM_WALL) return true;
+    return false;
+  };
+  std::vector<int64_t> spec_base(s.n_dir + 1, 0);
+  parallel_for(s.n_dir, [&](int64_t q) {
+    int64_t c = 0;
+    for (int64_t pos = 0; pos < s.n; ++pos) c += is_special((size_t)q * s.n + pos) ? 1 : 0;
+    spec_base[q + 1] = c;
+  });
+  for (int q = 0; q < s.n_dir; ++q) spec_base[q + 1] += spec_base[q];
+  pk.si.assign((size_t)spec_base[s.n_dir] * SI, 0);
+  pk.sr.assign((size_t)spec_base[s.n_dir] * SR, 0.0);
+  std::vector<int> dir_err(s.n_dir, 0);   // 1: outputs without a ring slot, 2: more than three wall inflows
+  parallel_for(s.n_dir, [&](int64_t qq) {
+    const int q = (int)qq;
+    int64_t nsp = spec_base[q];
     const int32_t* up = un.ptr.data() + un.off[q];
     for (int u = 0; u < un.n[q]; ++u) {
       int ent = 0, sent = 0;
@@ -228,10 +247,7 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
         int32_t si[SI] = {s.xk[it], s.wout[it], s.contact[it], 0, 0, 0, 0, 0};
         double sr[SR] = {0, 0, 0, 0};
         const bool outputs = s.xk[it] >= 0 || s.wout[it] != 0 || s.contact[it] >= 0;
-        if (outputs && s.slot[it] < 0) {
-          set_error("element with per-MFP outputs has no ring slot");
-          return OBTE_ERR_BAD_ARG;
-        }
+        if (outputs && s.slot[it] < 0) { dir_err[q] = 1; return; }
         bool special = outputs;
         double coef[4] = {0, 0, 0, 0};
         int32_t row_in[4] = {zero_row, zero_row, zero_row, zero_row};
@@ -252,7 +268,7 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
             coef[k] = g;
             ++k;
           } else if (kind == ITEM_WALL) {
-            if (si[3] >= 3) { set_error("more than three wall inflow faces on one element"); return OBTE_ERR_UNSUPPORTED; }
+            if (si[3] >= 3) { dir_err[q] = 2; return; }
             si[4 + si[3]] = idx;
             sr[si[3]] = g;
             si[3]++;
@@ -273,9 +289,10 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
         r[2] = (row_in[1] & 0xFFFF) | (row_in[2] << 16);
         r[3] = (row_in[3] & 0xFFFF) | (sp << 16);
         if (special) {
-          pk.spec[it] = (int32_t)(pk.si.size() / SI);
-          pk.si.insert(pk.si.end(), si, si + SI);
-          pk.sr.insert(pk.sr.end(), sr, sr + SR);
+          pk.spec[it] = (int32_t)nsp;
+          std::copy(si, si + SI, pk.si.begin() + (size_t)nsp * SI);
+          std::copy(sr, sr + SR, pk.sr.begin() + (size_t)nsp * SR);
+          ++nsp;
         }
         for (int f = 0; f < s.nf; ++f) {
           const Real v = (Real)coef[f];
@@ -284,6 +301,13 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
         const Real dv = (Real)s.D[it];
         std::memcpy(&r[COEF + s.nf * CSTEP], &dv, sizeof(Real));
       }
+    }
+  });
+  for (int q = 0; q < s.n_dir; ++q) {
+    if (dir_err[q] == 1) { set_error("element with per-MFP outputs has no ring slot"); return OBTE_ERR_BAD_ARG; }
+    if (dir_err[q] == 2) {
+      set_error("more than three wall inflow faces on one element");
+      return OBTE_ERR_UNSUPPORTED;
     }
   }
   if (pk.si.empty()) {
