@@ -35,6 +35,18 @@ obte_status DevBuf::alloc(size_t n) {
   return OBTE_OK;
 }
 
+obte_status HostBuf::alloc(size_t n) {
+  release();
+  if (n == 0) n = 16;
+  cudaError_t e = cudaMallocHost(&p, n);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    return cuda_fail(e, "cudaMallocHost", __FILE__, __LINE__);
+  }
+  bytes = n;
+  return OBTE_OK;
+}
+
 template <typename T>
 obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
   OBTE_TRY(b.alloc(std::max<size_t>(v.size(), 1) * sizeof(T)));

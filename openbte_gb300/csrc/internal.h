@@ -91,6 +91,24 @@ struct DevBuf {
   T* as() const { return static_cast<T*>(p); }
 };
 
+// Page-locked host buffer (the solver's small per-iteration device -> host reads).
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf&) = delete;
+  HostBuf& operator=(const HostBuf&) = delete;
+  ~HostBuf() { release(); }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  obte_status alloc(size_t n);
+  template <typename T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
 // Upload a host vector into a fresh device buffer (synchronous on `stream`).
 template <typename T>
 obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream);
@@ -217,6 +235,8 @@ struct SolveWork {
   DevBuf pz;         // preconditioned vector (allocated when the plan has a preconditioner)
   DevBuf rc, Jraw2, Kraw2, Sraw2;   // refinement: correction right-hand side, outputs of the correction
   DevBuf V32, w32;   // FP32 basis and working vector (stages with FP32 sweeps), allocated on first use
+  DevBuf gs;         // device Arnoldi step: second-pass coefficients, Hessenberg column, flags
+  HostBuf hcol;      // pinned copy of the Hessenberg column
 };
 
 // Right preconditioner of the GMRES on the periodic-inflow unknowns: for the ordinates whose inflow

@@ -50,7 +50,8 @@ int vec_blocks(const obte_plan plan, int64_t n) {
 // j == k when self != 0 (kk = k + self)
 __global__ void __launch_bounds__(VT) multidot_kernel(const double* __restrict__ V, int64_t ld, int k, int self,
                                                       const double* __restrict__ w, int64_t n,
-                                                      double* __restrict__ partial) {
+                                                      double* __restrict__ partial, const int* __restrict__ skip) {
+  if (skip && *skip) return;
   __shared__ double red[VT / 32][DOT_TILE];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int kk = k + self;
@@ -106,7 +107,8 @@ __global__ void __launch_bounds__(VT) reduce_partials_kernel(const double* __res
 constexpr int MAX_BASIS = 256;
 __global__ void __launch_bounds__(VT) update_kernel(double* __restrict__ w, const double* __restrict__ V, int64_t ld,
                                                     int k, const double* __restrict__ h, int64_t n,
-                                                    double* __restrict__ partial) {
+                                                    double* __restrict__ partial, const int* __restrict__ skip) {
+  if (skip && *skip) return;
   __shared__ double red[VT / 32];
   __shared__ double hs[MAX_BASIS];
   for (int j = threadIdx.x; j < k; j += VT) hs[j] = h[j];
@@ -146,35 +148,53 @@ __global__ void __launch_bounds__(VT) update_kernel(double* __restrict__ w, cons
 // per-thread sums, FP64 across threads and blocks.  The sweep still takes FP64 input (one widening
 // pass per Krylov vector) and the solution x stays FP64.
 
+// The two Gram-Schmidt products read 16 bytes per load: V's rows (stride ld) and w must be 16-byte
+// aligned (the FP32 basis rows are padded to a multiple of 4 floats); the n % 4 tail goes through
+// block 0.  They run on fewer blocks than the elementwise kernels so that each thread streams several
+// float4 per tile: with small states (0.9M entries) one scalar per thread and 8-vector tile left the
+// per-tile reductions and barriers dominant.  Warp sums are FP32 (32 partial sums of a few elements
+// each), FP64 from the warp level up: FP64 shuffles kept these kernels on the FP64 pipe.
+
 // partial[b * kk + j] = block b's part of V[j] . w (j < k) and of w . w (j == k when self)
-__global__ void __launch_bounds__(VT) multidot32_kernel(const float* __restrict__ V, int64_t ld, int k, int self,
-                                                        const float* __restrict__ w, int64_t n,
-                                                        double* __restrict__ partial) {
-  __shared__ double red[VT / 32][DOT_TILE];
+constexpr int DOT_TILE4 = 16;
+__global__ void __launch_bounds__(VT) multidot32v_kernel(const float* __restrict__ V, int64_t ld, int k, int self,
+                                                         const float* __restrict__ w, int64_t n,
+                                                         double* __restrict__ partial, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ double red[VT / 32][DOT_TILE4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int kk = k + self;
-  for (int jt = 0; jt < kk; jt += DOT_TILE) {
-    const float* vp[DOT_TILE];
+  const int64_t n4 = n >> 2;
+  const float4* w4 = reinterpret_cast<const float4*>(w);
+  for (int jt = 0; jt < kk; jt += DOT_TILE4) {
+    const float* vp[DOT_TILE4];
 #pragma unroll
-    for (int t = 0; t < DOT_TILE; ++t) vp[t] = jt + t < k ? V + (int64_t)(jt + t) * ld : w;   // self / padding read w
-    float acc[DOT_TILE];
+    for (int t = 0; t < DOT_TILE4; ++t) vp[t] = jt + t < k ? V + (int64_t)(jt + t) * ld : w;   // self / padding read w
+    float acc[DOT_TILE4];
 #pragma unroll
-    for (int t = 0; t < DOT_TILE; ++t) acc[t] = 0.f;
-    for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
-      const float wi = w[i];
+    for (int t = 0; t < DOT_TILE4; ++t) acc[t] = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n4; i += (int64_t)gridDim.x * VT) {
+      const float4 b = w4[i];
 #pragma unroll
-      for (int t = 0; t < DOT_TILE; ++t) acc[t] = fmaf(vp[t][i], wi, acc[t]);
+      for (int t = 0; t < DOT_TILE4; ++t) {
+        const float4 a = reinterpret_cast<const float4*>(vp[t])[i];
+        acc[t] = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, acc[t]))));
+      }
     }
-    // warp sums in FP32 (32 partial sums of a few elements each), FP64 from the warp level up: FP64
-    // shuffles here kept the kernel on the FP64 pipe at 20 % of DRAM bandwidth
+    if (blockIdx.x == 0)
+      for (int64_t i = 4 * n4 + threadIdx.x; i < n; i += VT) {
+        const float b = w[i];
 #pragma unroll
-    for (int t = 0; t < DOT_TILE; ++t) {
+        for (int t = 0; t < DOT_TILE4; ++t) acc[t] = fmaf(vp[t][i], b, acc[t]);
+      }
+#pragma unroll
+    for (int t = 0; t < DOT_TILE4; ++t) {
       float v = acc[t];
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       if (lane == 0) red[warp][t] = (double)v;
     }
     __syncthreads();
-    if (threadIdx.x < DOT_TILE && jt + (int)threadIdx.x < kk) {
+    if (threadIdx.x < DOT_TILE4 && jt + (int)threadIdx.x < kk) {
       double v = 0;
       for (int w2 = 0; w2 < VT / 32; ++w2) v += red[w2][threadIdx.x];
       partial[(int64_t)blockIdx.x * kk + jt + threadIdx.x] = v;
@@ -184,28 +204,38 @@ __global__ void __launch_bounds__(VT) multidot32_kernel(const float* __restrict_
 }
 
 // w -= sum_j h[j] V[j] (FP32); partial[b] = block b's part of the new w . w
-__global__ void __launch_bounds__(VT) update32_kernel(float* __restrict__ w, const float* __restrict__ V, int64_t ld,
-                                                      int k, const double* __restrict__ h, int64_t n,
-                                                      double* __restrict__ partial) {
+__global__ void __launch_bounds__(VT) update32v_kernel(float* __restrict__ w, const float* __restrict__ V, int64_t ld,
+                                                       int k, const double* __restrict__ h, int64_t n,
+                                                       double* __restrict__ partial, const int* __restrict__ skip) {
+  if (skip && *skip) return;
   __shared__ double red[VT / 32];
   __shared__ float hs[MAX_BASIS];
   for (int j = threadIdx.x; j < k; j += VT) hs[j] = (float)h[j];
   __syncthreads();
+  const int64_t n4 = n >> 2;
+  float4* w4 = reinterpret_cast<float4*>(w);
   float ss = 0.f;
-  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n; i += (int64_t)gridDim.x * VT) {
-    float acc = w[i];
-    int j = 0;
-    for (; j + 8 <= k; j += 8) {
-      float v[8];
-#pragma unroll
-      for (int t = 0; t < 8; ++t) v[t] = V[(int64_t)(j + t) * ld + i];
-#pragma unroll
-      for (int t = 0; t < 8; ++t) acc = fmaf(-hs[j + t], v[t], acc);
+  for (int64_t i = (int64_t)blockIdx.x * VT + threadIdx.x; i < n4; i += (int64_t)gridDim.x * VT) {
+    float4 acc = w4[i];
+#pragma unroll 4
+    for (int j = 0; j < k; ++j) {
+      const float4 v = reinterpret_cast<const float4*>(V + (int64_t)j * ld)[i];
+      const float c = -hs[j];
+      acc.x = fmaf(c, v.x, acc.x);
+      acc.y = fmaf(c, v.y, acc.y);
+      acc.z = fmaf(c, v.z, acc.z);
+      acc.w = fmaf(c, v.w, acc.w);
     }
-    for (; j < k; ++j) acc = fmaf(-hs[j], V[(int64_t)j * ld + i], acc);
-    w[i] = acc;
-    ss = fmaf(acc, acc, ss);
+    w4[i] = acc;
+    ss = fmaf(acc.x, acc.x, fmaf(acc.y, acc.y, fmaf(acc.z, acc.z, fmaf(acc.w, acc.w, ss))));
   }
+  if (blockIdx.x == 0)
+    for (int64_t i = 4 * n4 + threadIdx.x; i < n; i += VT) {
+      float acc = w[i];
+      for (int j = 0; j < k; ++j) acc = fmaf(-hs[j], V[(int64_t)j * ld + i], acc);
+      w[i] = acc;
+      ss = fmaf(acc, acc, ss);
+    }
   double sd = (double)ss;
   for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sd;
@@ -215,6 +245,45 @@ __global__ void __launch_bounds__(VT) update32_kernel(float* __restrict__ w, con
     for (int w2 = 0; w2 < VT / 32; ++w2) t += red[w2];
     partial[blockIdx.x] = t;
   }
+}
+
+// Device side of the Arnoldi step (no host round trip between the Gram-Schmidt passes).
+// DGKS test after the first pass: skip[0] = 1 (no second pass) unless the projection left less than
+// 0.7 of the norm w had before it (h[k] = w . w before, s[0] = w . w after).
+__global__ void gs_check_kernel(const double* __restrict__ h, int k, const double* __restrict__ s,
+                                int* __restrict__ skip) {
+  if (threadIdx.x == 0) skip[0] = sqrt(fmax(s[0], 0.0)) < 0.7 * sqrt(fmax(h[k], 0.0)) ? 0 : 1;
+}
+
+// Hessenberg column of the step: col[i] = h[i] (+ h2[i] after a second pass) for i < k, col[k] = ‖w‖,
+// col[k + 1] = 1 when the second pass ran; inv[0] = 1 / ‖w‖ in FP32 and inv64[0] in FP64 (0 for a zero
+// vector).
+__global__ void gs_finish_kernel(const double* __restrict__ h, const double* __restrict__ h2, int k,
+                                 const double* __restrict__ s, const int* __restrict__ skip,
+                                 double* __restrict__ col, float* __restrict__ inv, double* __restrict__ inv64) {
+  const bool two = skip[0] == 0;
+  for (int i = threadIdx.x; i < k; i += blockDim.x) col[i] = two ? h[i] + h2[i] : h[i];
+  if (threadIdx.x == 0) {
+    const double hn = sqrt(fmax(two ? s[1] : s[0], 0.0));
+    col[k] = hn;
+    col[k + 1] = two ? 1.0 : 0.0;
+    inv[0] = hn > 0 ? (float)(1.0 / hn) : 0.f;
+    inv64[0] = hn > 0 ? 1.0 / hn : 0.0;
+  }
+}
+
+// y = a[0] x (scale read from the device)
+__global__ void scaled_kernel(const double* __restrict__ a, const double* __restrict__ x, double* __restrict__ y,
+                              int64_t n) {
+  const double s = *a;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = s * x[i];
+}
+__global__ void scale32d_kernel(const float* __restrict__ a, const float* __restrict__ x, float* __restrict__ y,
+                                int64_t n) {
+  const float s = *a;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = s * x[i];
 }
 
 // x += sum_j y[j] V[j] (FP32 combination, FP64 accumulate into x)
@@ -234,11 +303,6 @@ __global__ void __launch_bounds__(VT) xupdate32_kernel(double* __restrict__ x, c
 __global__ void scale_to_f32_kernel(double a, const double* __restrict__ x, float* __restrict__ y, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = (float)(a * x[i]);
-}
-// y = a * x (FP32)
-__global__ void scale32_kernel(float a, const float* __restrict__ x, float* __restrict__ y, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = a * x[i];
 }
 // y = (double)x
 __global__ void widen_kernel(const float* __restrict__ x, double* __restrict__ y, int64_t n) {
@@ -359,26 +423,13 @@ struct Solver {
   obte_status multidot(const double* V, int k, const double* w, std::vector<double>& h, bool self = false) {
     const int64_t n = wk.nu;
     const int kk = k + (self ? 1 : 0);
-    multidot_kernel<<<wk.nb, VT, 0, st>>>(V, n, k, self ? 1 : 0, w, n, wk.partial.as<double>());
+    multidot_kernel<<<wk.nb, VT, 0, st>>>(V, n, k, self ? 1 : 0, w, n, wk.partial.as<double>(), nullptr);
     reduce_partials_kernel<<<kk, VT, 0, st>>>(wk.partial.as<double>(), wk.nb, kk, wk.hdev.as<double>());
     count_launch(2);
     OBTE_CUDA(cudaGetLastError());
     h.resize(kk);
     OBTE_CUDA(cudaMemcpyAsync(h.data(), wk.hdev.p, kk * sizeof(double), cudaMemcpyDeviceToHost, st));
     OBTE_CUDA(cudaStreamSynchronize(st));
-    return OBTE_OK;
-  }
-  // w -= V[0..k) h (h already on the device in wk.hdev); returns ‖w‖ after the update
-  obte_status update_norm(double* w, const double* V, int k, double& nrm) {
-    const int64_t n = wk.nu;
-    update_kernel<<<wk.nb, VT, 0, st>>>(w, V, n, k, wk.hdev.as<double>(), n, wk.partial.as<double>());
-    reduce_partials_kernel<<<1, VT, 0, st>>>(wk.partial.as<double>(), wk.nb, 1, wk.sdev.as<double>());
-    count_launch(2);
-    OBTE_CUDA(cudaGetLastError());
-    double ss;
-    OBTE_CUDA(cudaMemcpyAsync(&ss, wk.sdev.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-    OBTE_CUDA(cudaStreamSynchronize(st));
-    nrm = std::sqrt(std::max(ss, 0.0));
     return OBTE_OK;
   }
   obte_status norm(const double* x, double& out) {
@@ -413,20 +464,53 @@ struct Solver {
     return OBTE_OK;
   }
 
-  // Restarted GMRES with the FP32 basis (see multidot32_kernel); same contract as gmres().
+  // Device Arnoldi scratch: second-pass coefficients [m+1], Hessenberg column [m+3], norms [2], DGKS flag,
+  // 1/‖w‖ in FP32 and FP64; and the pinned host copy of the column.
+  struct GsScratch {
+    double *h2, *col, *s, *inv64;
+    int* skip;
+    float* inv;
+  };
+  obte_status gs_scratch(GsScratch& g) {
+    const int m = wk.restart;
+    if (!wk.gs.p) OBTE_TRY(wk.gs.alloc((size_t)(2 * m + 9) * sizeof(double)));
+    if (!wk.hcol.p) OBTE_TRY(wk.hcol.alloc((size_t)(m + 3) * sizeof(double)));
+    g.h2 = wk.gs.as<double>();
+    g.col = g.h2 + (m + 1);
+    g.s = g.col + (m + 3);
+    g.skip = reinterpret_cast<int*>(g.s + 2);
+    g.inv = reinterpret_cast<float*>(g.s + 3);
+    g.inv64 = g.s + 4;
+    return OBTE_OK;
+  }
+
+  // Restarted GMRES with the FP32 basis (see multidot32v_kernel); same contract as gmres().
   obte_status gmres32(const double* rhs, double* x, double tol_rel, double tol_abs, double& res_out, bool& ok) {
     const int64_t n = wk.nu;
     const int m = wk.restart;
+    const int64_t ld = (n + 3) & ~(int64_t)3;   // basis rows padded to 16 bytes
     if (!wk.V32.p) {
-      OBTE_TRY(wk.V32.alloc((size_t)n * (m + 1) * sizeof(float)));
-      OBTE_TRY(wk.w32.alloc((size_t)n * sizeof(float)));
+      OBTE_TRY(wk.V32.alloc((size_t)ld * (m + 1) * sizeof(float)));
+      OBTE_TRY(wk.w32.alloc((size_t)ld * sizeof(float)));
     }
     float* V = wk.V32.as<float>();
     float* w = wk.w32.as<float>();
     double* vj64 = wk.w.as<double>();
     double* r = wk.r.as<double>();
     const int nb = wk.nb;
-    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), h, h2;
+    // Gram-Schmidt kernels: about 4 float4 per thread and tile, at most the elementwise grid
+    const int nbg = (int)std::max<int64_t>(1, std::min<int64_t>(nb, (n / 4 + 4 * VT - 1) / (4 * VT)));
+    GsScratch gsd;
+    OBTE_TRY(gs_scratch(gsd));
+    double* h2d = gsd.h2;
+    double* cold = gsd.col;
+    double* sd = gsd.s;
+    int* skipd = gsd.skip;
+    float* invd = gsd.inv;
+    const double* hc = wk.hcol.as<double>();
+    double* hdev = wk.hdev.as<double>();
+    double* part = wk.partial.as<double>();
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
     ok = false;
     if (x_zero && rhs) OBTE_TRY(lincomb(1.0, rhs, 0.0, rhs, r));
     else OBTE_TRY(residual(true, rhs, x, r));
@@ -434,29 +518,6 @@ struct Solver {
     double beta;
     OBTE_TRY(norm(r, beta));
     res_out = beta;
-    auto dots = [&](int k, bool self, std::vector<double>& out) -> obte_status {
-      const int kk = k + (self ? 1 : 0);
-      multidot32_kernel<<<nb, VT, 0, st>>>(V, n, k, self ? 1 : 0, w, n, wk.partial.as<double>());
-      reduce_partials_kernel<<<kk, VT, 0, st>>>(wk.partial.as<double>(), nb, kk, wk.hdev.as<double>());
-      count_launch(2);
-      OBTE_CUDA(cudaGetLastError());
-      out.resize(kk);
-      OBTE_CUDA(cudaMemcpyAsync(out.data(), wk.hdev.p, kk * sizeof(double), cudaMemcpyDeviceToHost, st));
-      OBTE_CUDA(cudaStreamSynchronize(st));
-      return OBTE_OK;
-    };
-    auto project = [&](int k, const std::vector<double>& coef, double& nrm) -> obte_status {
-      OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, coef.data(), k * sizeof(double), cudaMemcpyHostToDevice, st));
-      update32_kernel<<<nb, VT, 0, st>>>(w, V, n, k, wk.hdev.as<double>(), n, wk.partial.as<double>());
-      reduce_partials_kernel<<<1, VT, 0, st>>>(wk.partial.as<double>(), nb, 1, wk.sdev.as<double>());
-      count_launch(2);
-      OBTE_CUDA(cudaGetLastError());
-      double ss;
-      OBTE_CUDA(cudaMemcpyAsync(&ss, wk.sdev.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-      OBTE_CUDA(cudaStreamSynchronize(st));
-      nrm = std::sqrt(std::max(ss, 0.0));
-      return OBTE_OK;
-    };
     while (true) {
       double xn;
       OBTE_TRY(norm(x, xn));
@@ -472,7 +533,7 @@ struct Solver {
       for (; j < m && sweeps < max_sweeps; ++j) {
         const auto w0 = std::chrono::steady_clock::now();
         if (trace) cudaEventRecord(ev[0], st);
-        widen_kernel<<<nb, VT, 0, st>>>(V + (int64_t)j * n, vj64, n);
+        widen_kernel<<<nb, VT, 0, st>>>(V + (int64_t)j * ld, vj64, n);
         count_launch();
         const double* zj = vj64;              // z_j = M^-1 v_j
         if (xp) {
@@ -484,18 +545,27 @@ struct Solver {
         diff_to_f32_kernel<<<nb, VT, 0, st>>>(zj, wk.tmp.as<double>(), w, n);
         count_launch();
         OBTE_CUDA(cudaGetLastError());
-        // classical Gram-Schmidt with one conditional re-orthogonalisation (as in gmres())
-        OBTE_TRY(dots(j + 1, true, h));
-        const double wn0 = std::sqrt(std::max(h[j + 1], 0.0));
-        h.resize(j + 1);
-        double hn;
-        OBTE_TRY(project(j + 1, h, hn));
-        if (hn < 0.7 * wn0) {
-          OBTE_TRY(dots(j + 1, false, h2));
-          OBTE_TRY(project(j + 1, h2, hn));
-          for (int i = 0; i <= j; ++i) h[i] += h2[i];
-        }
-        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = h[i];
+        // classical Gram-Schmidt with one conditional re-orthogonalisation (as in gmres()), all on the
+        // device: the second pass's kernels return at once when the DGKS test declines it, and the
+        // host reads the finished Hessenberg column once per step
+        const int k = j + 1;
+        multidot32v_kernel<<<nbg, VT, 0, st>>>(V, ld, k, 1, w, n, part, nullptr);
+        reduce_partials_kernel<<<k + 1, VT, 0, st>>>(part, nbg, k + 1, hdev);
+        update32v_kernel<<<nbg, VT, 0, st>>>(w, V, ld, k, hdev, n, part, nullptr);
+        reduce_partials_kernel<<<1, VT, 0, st>>>(part, nbg, 1, sd);
+        gs_check_kernel<<<1, 32, 0, st>>>(hdev, k, sd, skipd);
+        multidot32v_kernel<<<nbg, VT, 0, st>>>(V, ld, k, 0, w, n, part, skipd);
+        reduce_partials_kernel<<<k, VT, 0, st>>>(part, nbg, k, h2d);
+        update32v_kernel<<<nbg, VT, 0, st>>>(w, V, ld, k, h2d, n, part, skipd);
+        reduce_partials_kernel<<<1, VT, 0, st>>>(part, nbg, 1, sd + 1);
+        gs_finish_kernel<<<1, 128, 0, st>>>(hdev, h2d, k, sd, skipd, cold, invd, gsd.inv64);
+        scale32d_kernel<<<nb, VT, 0, st>>>(invd, w, V + (int64_t)k * ld, n);
+        count_launch(11);
+        OBTE_CUDA(cudaGetLastError());
+        OBTE_CUDA(cudaMemcpyAsync(wk.hcol.p, cold, (size_t)(k + 2) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OBTE_CUDA(cudaStreamSynchronize(st));
+        const double hn = hc[k];
+        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hc[i];
         H[(size_t)(j + 1) * m + j] = hn;
         for (int i = 0; i < j; ++i) {
           const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
@@ -511,10 +581,6 @@ struct Solver {
         g[j + 1] = -sn[j] * g[j];
         g[j] = cs[j] * g[j];
         est = std::fabs(g[j + 1]);
-        if (hn > 0) {
-          scale32_kernel<<<nb, VT, 0, st>>>((float)(1.0 / hn), w, V + (int64_t)(j + 1) * n, n);
-          count_launch();
-        }
         if (trace) {
           cudaEventRecord(ev[2], st);
           cudaEventSynchronize(ev[2]);
@@ -539,12 +605,12 @@ struct Solver {
         if (xp) {                             // x += M^-1 (V y)
           double* z = wk.pz.as<double>();
           OBTE_CUDA(cudaMemsetAsync(z, 0, (size_t)n * sizeof(double), st));
-          xupdate32_kernel<<<nb, VT, 0, st>>>(z, V, n, j, wk.hdev.as<double>(), n);
+          xupdate32_kernel<<<nb, VT, 0, st>>>(z, V, ld, j, wk.hdev.as<double>(), n);
           count_launch();
           OBTE_TRY(axpby(1.0, z, 1.0, x));
           xprec_add(plan, z, x, true);
         } else {
-          xupdate32_kernel<<<nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n);
+          xupdate32_kernel<<<nb, VT, 0, st>>>(x, V, ld, j, wk.hdev.as<double>(), n);
           count_launch();
         }
         OBTE_CUDA(cudaGetLastError());
@@ -575,7 +641,13 @@ struct Solver {
     double* V = wk.V.as<double>();
     double* w = wk.w.as<double>();
     double* r = wk.r.as<double>();
-    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), h, h2;
+    GsScratch gsd;
+    OBTE_TRY(gs_scratch(gsd));
+    const double* hc = wk.hcol.as<double>();
+    double* hdev = wk.hdev.as<double>();
+    double* part = wk.partial.as<double>();
+    const int nb = wk.nb;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
     ok = false;
     if (x_zero && rhs) OBTE_TRY(lincomb(1.0, rhs, 0.0, rhs, r));
     else OBTE_TRY(residual(fp32, rhs, x, r));
@@ -607,21 +679,28 @@ struct Solver {
         if (trace) cudaEventRecord(ev[1], st);
         OBTE_TRY(lincomb(1.0, zj, -1.0, wk.tmp.as<double>(), w));
         // classical Gram-Schmidt; a second pass only when the first one cancelled most of w
-        // (Daniel-Gragg-Kaufman-Stewart criterion, ‖w‖ after < 0.7 ‖w‖ before)
-        OBTE_TRY(multidot(V, j + 1, w, h, true));   // h[0..j] and w.w in one pass
-        const double wn0 = std::sqrt(std::max(h[j + 1], 0.0));
-        h.resize(j + 1);
-        OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, h.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
-        double hn;
-        OBTE_TRY(update_norm(w, V, j + 1, hn));
-        if (hn < 0.7 * wn0) {
-          OBTE_TRY(multidot(V, j + 1, w, h2));
-          OBTE_CUDA(cudaMemcpyAsync(wk.hdev.p, h2.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
-          OBTE_TRY(update_norm(w, V, j + 1, hn));
-          for (int i = 0; i <= j; ++i) h[i] += h2[i];
-        }
+        // (Daniel-Gragg-Kaufman-Stewart criterion, ‖w‖ after < 0.7 ‖w‖ before).  The whole step runs on
+        // the device (the second pass's kernels return at once when the test declines it) and the host
+        // reads the Hessenberg column once.
+        const int k = j + 1;
+        multidot_kernel<<<nb, VT, 0, st>>>(V, n, k, 1, w, n, part, nullptr);   // h[0..j] and w.w in one pass
+        reduce_partials_kernel<<<k + 1, VT, 0, st>>>(part, nb, k + 1, hdev);
+        update_kernel<<<nb, VT, 0, st>>>(w, V, n, k, hdev, n, part, nullptr);
+        reduce_partials_kernel<<<1, VT, 0, st>>>(part, nb, 1, gsd.s);
+        gs_check_kernel<<<1, 32, 0, st>>>(hdev, k, gsd.s, gsd.skip);
+        multidot_kernel<<<nb, VT, 0, st>>>(V, n, k, 0, w, n, part, gsd.skip);
+        reduce_partials_kernel<<<k, VT, 0, st>>>(part, nb, k, gsd.h2);
+        update_kernel<<<nb, VT, 0, st>>>(w, V, n, k, gsd.h2, n, part, gsd.skip);
+        reduce_partials_kernel<<<1, VT, 0, st>>>(part, nb, 1, gsd.s + 1);
+        gs_finish_kernel<<<1, 128, 0, st>>>(hdev, gsd.h2, k, gsd.s, gsd.skip, gsd.col, gsd.inv, gsd.inv64);
+        scaled_kernel<<<nb, VT, 0, st>>>(gsd.inv64, w, V + (int64_t)k * n, n);
+        count_launch(11);
+        OBTE_CUDA(cudaGetLastError());
+        OBTE_CUDA(cudaMemcpyAsync(wk.hcol.p, gsd.col, (size_t)(k + 2) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        OBTE_CUDA(cudaStreamSynchronize(st));
+        const double hn = hc[k];
         // Hessenberg column j
-        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = h[i];
+        for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hc[i];
         H[(size_t)(j + 1) * m + j] = hn;
         for (int i = 0; i < j; ++i) {
           const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
@@ -637,7 +716,6 @@ struct Solver {
         g[j + 1] = -sn[j] * g[j];
         g[j] = cs[j] * g[j];
         est = std::fabs(g[j + 1]);
-        if (hn > 0) OBTE_TRY(lincomb(1.0 / hn, w, 0.0, w, V + (int64_t)(j + 1) * n));
         if (trace) {
           cudaEventRecord(ev[2], st);
           cudaEventSynchronize(ev[2]);
@@ -664,12 +742,12 @@ struct Solver {
         if (xp) {                             // x += M^-1 (V y)
           double* z = wk.pz.as<double>();
           OBTE_CUDA(cudaMemsetAsync(z, 0, (size_t)n * sizeof(double), st));
-          update_kernel<<<wk.nb, VT, 0, st>>>(z, V, n, j, wk.hdev.as<double>(), n, nullptr);
+          update_kernel<<<wk.nb, VT, 0, st>>>(z, V, n, j, wk.hdev.as<double>(), n, nullptr, nullptr);
           count_launch();
           OBTE_TRY(axpby(1.0, z, 1.0, x));
           xprec_add(plan, z, x, false);
         } else {
-          update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n, nullptr);
+          update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n, nullptr, nullptr);
           count_launch();
         }
         OBTE_CUDA(cudaGetLastError());
@@ -716,9 +794,9 @@ static obte_status alloc_work(obte_plan plan, Work& wk, int restart) {
 int64_t solve_scratch_bytes(obte_plan plan, int restart) {
   const Schedule& s = plan->sched;
   const int64_t vb = plan->nu * (int64_t)sizeof(double);
-  // u Fu r w tmp delta pz rc, the FP64 and FP32 bases, two sets of J/K/S accumulators, partials
-  return vb * (8 + restart + 1) + plan->nu * 4LL * (restart + 2) + 2 * ((int64_t)s.n * s.ds * 8 + 2LL * s.n_mfp * s.n_dir * 8) +
-         (int64_t)plan->ctx->num_sms * 4 * (restart + 1) * 8;
+  // u Fu r w tmp delta pz rc, the FP64 and FP32 bases, two sets of J/K/S accumulators, partials, Arnoldi scratch
+  return vb * (8 + restart + 1) + ((plan->nu + 3) & ~3LL) * 4LL * (restart + 2) + 2 * ((int64_t)s.n * s.ds * 8 + 2LL * s.n_mfp * s.n_dir * 8) +
+         (int64_t)plan->ctx->num_sms * 4 * (restart + 1) * 8 + (2LL * restart + 9) * 8;
 }
 
 }  // namespace obte
