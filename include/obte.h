@@ -150,6 +150,19 @@ obte_status obte_bte_plan_create(obte_context ctx, const obte_problem* prob,
                                  const obte_material* mat, obte_plan* out);
 obte_status obte_bte_plan_destroy(obte_plan plan);
 /*
+ * New side transmissions [n_sides], each in (0, 1], for a plan created with side transmissions
+ * (the transmission-interface model of inverse design).  Replaces openbte/inverse/bte.py:147-173
+ * (get_rho_dependent: the transmission-dependent operator terms, recomputed per density field over
+ * the density-independent geometry of bte.py:116-140).  The sweep order, slots and table layout do not
+ * depend on t, so only the coefficients are recomputed and re-uploaded; the periodic-inflow
+ * preconditioner is dropped, and the previous solution stays as the start of a warm-started solve (the
+ * reference's design loop reuses it the same way, bte.py:234-236).  upload_bytes (may be NULL) receives
+ * the bytes copied to the device.  OBTE_ERR_UNSUPPORTED for problems with isothermal walls or nanowire
+ * terms (create a new plan), OBTE_ERR_BAD_ARG for a plan without side transmissions or a t outside (0, 1].
+ */
+obte_status obte_bte_plan_set_transmission(obte_plan plan, const double* side_transmission,
+                                           int64_t* upload_bytes);
+/*
  * Issue this plan's later work on `stream` (a cudaStream_t; work already issued is finished
  * first).  No counterpart in the reference: it lets a serving loop run plans concurrently on
  * separate streams.  One plan must not be used by two threads at the same time.

@@ -114,6 +114,16 @@ extern "C" obte_status obte_context_set_stream(obte_context ctx, void* stream) {
   return OBTE_OK;
 }
 
+// Conserved-offset weights over the full state (zero on the periodic part); returns their sum.
+static double offset_weights(const obte_plan p, std::vector<double>& ell) {
+  const Schedule& s = p->sched;
+  ell.assign(p->nu, 0.0);
+  double sum = 0;
+  for (int64_t e = 0; e < s.n; ++e) { ell[e] = s.ell_T[e]; sum += s.ell_T[e]; }
+  for (int64_t w = 0; w < s.nd; ++w) { ell[s.n + w] = s.ell_B[w]; sum += s.ell_B[w]; }
+  return sum;
+}
+
 extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem* prob, const obte_material* mat,
                                             obte_plan* out) {
   if (!out) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
@@ -125,12 +135,8 @@ extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem
   const Schedule& s = p->sched;
   p->nx = s.x_base[s.n_dir] * s.n_mfp;
   p->nu = s.n + s.nd + p->nx;
-  // conserved-offset weights over the full state
-  std::vector<double> ell(p->nu, 0.0);
-  double sum = 0;
-  for (int64_t e = 0; e < s.n; ++e) { ell[e] = s.ell_T[e]; sum += s.ell_T[e]; }
-  for (int64_t w = 0; w < s.nd; ++w) { ell[s.n + w] = s.ell_B[w]; sum += s.ell_B[w]; }
-  p->ell_sum = sum;
+  std::vector<double> ell;
+  p->ell_sum = offset_weights(p, ell);
   if (!ctx) { *out = p; return OBTE_OK; }   // host-only plan: schedule queries, no device tables
   auto fail = [&](obte_status code) { delete p; return code; };
   cudaStream_t strm = ctx->stream;
@@ -143,6 +149,30 @@ extern "C" obte_status obte_bte_plan_create(obte_context ctx, const obte_problem
   if ((st = upload(p->sshift, s.sshift, strm)) != OBTE_OK) return fail(st);
   if ((st = upload(p->x_base_dev, s.x_base, strm)) != OBTE_OK) return fail(st);
   *out = p;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_plan_set_transmission(obte_plan plan, const double* side_transmission,
+                                                      int64_t* upload_bytes) {
+  if (!plan || !side_transmission) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  if (upload_bytes) *upload_bytes = 0;
+  // nothing issued earlier may still read the coefficients being replaced
+  if (plan->ctx) OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  OBTE_TRY(set_transmission(plan->sched, side_transmission));
+  const Schedule& s = plan->sched;
+  std::vector<double> ell;
+  plan->ell_sum = offset_weights(plan, ell);
+  // the preconditioner belongs to the old transmissions; the last solution stays as a warm start
+  plan->xprec.reset();
+  plan->n_solves = 0;
+  if (!plan->ctx) return OBTE_OK;
+  cudaStream_t strm = plan->stream;
+  OBTE_TRY(upload(plan->ell, ell, strm));
+  OBTE_TRY(upload(plan->kconst, s.kconst, strm));
+  OBTE_TRY(upload(plan->kshift, s.kshift, strm));
+  int64_t bytes = (int64_t)(ell.size() + s.kconst.size() + s.kshift.size()) * 8;
+  OBTE_TRY(refresh_tables(plan, &bytes));
+  if (upload_bytes) *upload_bytes = bytes;
   return OBTE_OK;
 }
 

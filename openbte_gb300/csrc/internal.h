@@ -202,9 +202,28 @@ struct Schedule {
   bool extra_sources = false;                // isothermal walls, heat source or nanowire terms
   bool isothermal = false;                   // isothermal (mixed) walls: they fix the temperature level, so
                                              // I - K has no constant null mode and no offset is applied
+  // Transmission plans without isothermal walls or nanowire terms keep the transmission-free factor of
+  // every coefficient that depends on the side transmissions t: the sweep order, the levels, the slots and
+  // the packed table layout depend on the mesh and the directions only, so new transmissions replace
+  // coefficients and nothing else (set_transmission).
+  struct TransmissionFactors {
+    bool ok = false;
+    int contact_kind = 0;
+    std::vector<double> g0;                  // [n_dir * n * nf] inflow coefficient without t
+    std::vector<int32_t> mode;               // same layout: side s (x t_s), -(s + 2) (x (1 - t_s)), -1 (x 1)
+    std::vector<int32_t> per_i, per_j, per_side;   // [np] periodic sides: their two elements and side id
+    std::vector<double> per_a;               // [n_dir * np * 2] jump terms of P without t
+    std::vector<int32_t> c_side;             // [nc] contact sides
+    std::vector<double> c_na;                // [nc * dim] their area vectors
+    std::vector<int32_t> co_ptr, co_k, co_role;   // element -> (contact side, role 1 = e1 / 2 = e2)
+    std::vector<double> ell0;                // [nd] ell_B without the wall's scale
+    std::vector<int32_t> w_side;             // [nd] side of a reflecting wall (-1: diffuse wall, scale 1)
+  } tf;
 };
 
 obte_status build_schedule(const obte_problem* prob, const obte_material* mat, Schedule& s);
+// New side transmissions [n_sides] for a plan built with side transmissions (coefficients only).
+obte_status set_transmission(Schedule& s, const double* side_transmission);
 
 // Device copy of the schedule in precision Real.
 //   rec      packed per-item records (level order, all directions)
@@ -220,6 +239,10 @@ struct DevSchedule {
   DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, sx, ksx, mfp, tco, sig, wo_wall, wo_geo, kcoef, scoef, hs, vals, cellmap,
       Pq, si, sr, wo_off, spec;
   DevBuf lpt;                              // launch order: CTAs of the directions with the most units first
+  // transmission plans: host copies of the packed records and of the special-entry index, so that new
+  // transmissions rewrite the coefficient words in place (refresh_tables)
+  std::vector<int32_t> h_rec, h_spec;
+  int64_t n_spec = 0;
   size_t bytes() const;
 };
 
@@ -291,6 +314,8 @@ namespace obte {
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
                          bool final_pass, double* Jraw, double* K, double* S);
 obte_status ensure_tables(obte_plan plan, bool fp32);
+// After set_transmission: the coefficient words of the device tables that exist (bytes uploaded added to *bytes).
+obte_status refresh_tables(obte_plan plan, int64_t* bytes);
 // Periodic-inflow preconditioner (xprec.cu): built once per plan.
 obte_status ensure_xprec(obte_plan plan, SolveWork& wk);
 // out[X blocks] += W in[X blocks] (fp32: FP32 accumulation, for stages with an FP32 Krylov basis)

@@ -15,6 +15,7 @@
 // per-direction buffers and merged in direction order, so the result does not
 // depend on the thread count.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -82,6 +83,12 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     }
   }
   const bool reflect = pb->reflect_internal != 0;
+  // transmission plans keep the transmission-free factors of their coefficients (set_transmission)
+  const bool keep_tf = pb->side_transmission != nullptr && pb->n_mixed == 0 && !pb->is_nanowire;
+  Schedule::TransmissionFactors& tf = s.tf;
+  tf = Schedule::TransmissionFactors();
+  tf.ok = keep_tf;
+  tf.contact_kind = pb->contact_kind;
   std::vector<int32_t> f_row(nfd), f_nb(nfd);
   std::vector<char> f_cut(nfd);
   std::vector<double> f_k(nfd * dim), f_t(nfd);
@@ -136,12 +143,45 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     for (int d = 0; d < dim; ++d) v += mt->sigma[((int64_t)m * n_dir + q) * ds + d] * w_db[w * dim + d];
     return v;
   };
-  parallel_for(nd, [&](int64_t w) {
+  // Walls with the same w_db vector (bit for bit) have the same sigma . w_db products: on structured
+  // grids a handful of vectors cover every wall of the transmission-interface model (4 on a pixel
+  // grid against 2 x 32,768 walls), so the sums over (m, q) are taken once per distinct vector.
+  // key_out[k * n_dir + q]: some MFP of direction q leaves through walls of vector k (re-emission).
+  std::vector<int32_t> w_key(nd);
+  std::vector<int64_t> key_wall;
+  {
+    struct KeyHash {
+      size_t operator()(const std::array<uint64_t, 3>& a) const {
+        uint64_t h = 0x9e3779b97f4a7c15ull;
+        for (uint64_t v : a) h = (h ^ v) * 0x100000001b3ull + (h >> 29);
+        return (size_t)h;
+      }
+    };
+    std::unordered_map<std::array<uint64_t, 3>, int32_t, KeyHash> idx;
+    for (int64_t w = 0; w < nd; ++w) {
+      std::array<uint64_t, 3> k{0, 0, 0};
+      std::memcpy(k.data(), &w_db[w * dim], dim * sizeof(double));
+      auto it = idx.emplace(k, (int32_t)key_wall.size());
+      if (it.second) key_wall.push_back(w);
+      w_key[w] = it.first->second;
+    }
+  }
+  const int64_t n_key = (int64_t)key_wall.size();
+  std::vector<double> key_gbm(n_key);
+  std::vector<char> key_out((size_t)n_key * n_dir);
+  parallel_for(n_key, [&](int64_t k) {
+    const int64_t w = key_wall[k];
     double acc = 0;
     for (int m = 0; m < n_mfp; ++m)
       for (int q = 0; q < n_dir; ++q) acc += std::min(gb_of(m, q, w), 0.0);
-    gbm_sum[w] = acc;
+    key_gbm[k] = acc;
+    for (int q = 0; q < n_dir; ++q) {
+      bool any = false;
+      for (int m = 0; m < n_mfp && !any; ++m) any = gb_of(m, q, w) > 0;
+      key_out[(size_t)k * n_dir + q] = any;
+    }
   });
+  for (int64_t w = 0; w < nd; ++w) gbm_sum[w] = key_gbm[w_key[w]];
   s.w_db = w_db;
   s.gbm_sum = gbm_sum;
   // ---- contact (bte.py:132-158) ----
@@ -171,6 +211,27 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   for (int64_t k = 0; k < nc; ++k) {
     contact_of[c_e1[k]].push_back({k, 1});
     if (c_e2[k] >= 0) contact_of[c_e2[k]].push_back({k, 2});
+  }
+  if (keep_tf) {
+    for (int64_t k = 0; k < nc; ++k) tf.c_side.push_back((int32_t)pb->contact_sides[k]);
+    tf.c_na = c_na;
+    tf.co_ptr.assign(n + 1, 0);
+    for (int64_t k = 0; k < nc; ++k) {
+      tf.co_ptr[c_e1[k] + 1]++;
+      if (c_e2[k] >= 0) tf.co_ptr[c_e2[k] + 1]++;
+    }
+    for (int64_t e = 0; e < n; ++e) tf.co_ptr[e + 1] += tf.co_ptr[e];
+    tf.co_k.assign(tf.co_ptr[n], 0);
+    tf.co_role.assign(tf.co_ptr[n], 0);
+    std::vector<int32_t> fill(tf.co_ptr.begin(), tf.co_ptr.end() - 1);
+    for (int64_t k = 0; k < nc; ++k) {   // the insertion order of contact_of
+      tf.co_k[fill[c_e1[k]]] = (int32_t)k;
+      tf.co_role[fill[c_e1[k]]++] = 1;
+      if (c_e2[k] >= 0) {
+        tf.co_k[fill[c_e2[k]]] = (int32_t)k;
+        tf.co_role[fill[c_e2[k]]++] = 2;
+      }
+    }
   }
   auto sigma_n = [&](int m, int q, int64_t k) {
     double v = 0;
@@ -203,16 +264,27 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.sshift.assign((size_t)n_mfp * n_dir, 0.0);
   // offset weights
   s.ell_T.assign(vol, vol + n);
+  //   ell_B[w] = w_scale[w] sum_q max(-s_q . A_w, 0) sum_m t_coeff[m, q] mfp_m
   s.ell_B.assign(nd, 0.0);
-  for (int64_t w = 0; w < nd; ++w) {
-    double acc = 0;
-    for (int q = 0; q < n_dir; ++q) {
-      double sn = 0;
-      for (int d = 0; d < dim; ++d) sn += mt->vmfp[(int64_t)q * dd + d] * w_na[w * dim + d];
-      if (sn < 0)
-        for (int m = 0; m < n_mfp; ++m) acc += mt->t_coeff[(int64_t)m * n_dir + q] * mt->mfps[m] * (-sn);
+  {
+    std::vector<double> tl_q(n_dir, 0.0);
+    for (int q = 0; q < n_dir; ++q)
+      for (int m = 0; m < n_mfp; ++m) tl_q[q] += mt->t_coeff[(int64_t)m * n_dir + q] * mt->mfps[m];
+    if (keep_tf) {
+      tf.ell0.assign(nd, 0.0);
+      tf.w_side.assign(nd, -1);
+      for (int64_t w = nd0; w < nd; ++w) tf.w_side[w] = (int32_t)pb->internal[(w - nd0) % ni];
     }
-    s.ell_B[w] = acc * w_scale[w];
+    parallel_for(nd, [&](int64_t w) {
+      double acc = 0;
+      for (int q = 0; q < n_dir; ++q) {
+        double sn = 0;
+        for (int d = 0; d < dim; ++d) sn += mt->vmfp[(int64_t)q * dd + d] * w_na[w * dim + d];
+        if (sn < 0) acc += tl_q[q] * (-sn);
+      }
+      if (keep_tf) tf.ell0[w] = acc;
+      s.ell_B[w] = acc * w_scale[w];
+    });
   }
 
 
@@ -263,6 +335,21 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.P.assign((size_t)n_dir * n, 0.0);
   s.nlev.assign(n_dir, 0);
   s.nslots.assign(n_dir, 0);
+  if (keep_tf) {
+    tf.g0.assign((size_t)n_dir * n * nf, 0.0);
+    tf.mode.assign((size_t)n_dir * n * nf, -1);
+    const int64_t np = pb->n_periodic;
+    tf.per_i.resize(np);
+    tf.per_j.resize(np);
+    tf.per_side.resize(np);
+    for (int64_t k = 0; k < np; ++k) {
+      const int64_t sd = pb->periodic_sides[k];
+      tf.per_i[k] = (int32_t)sem[2 * sd];
+      tf.per_j[k] = (int32_t)sem[2 * sd + 1];
+      tf.per_side[k] = (int32_t)sd;
+    }
+    tf.per_a.assign((size_t)n_dir * np * 2, 0.0);
+  }
 
   struct DirOut {
     std::vector<int32_t> lev, x_cell, wo_wall;
@@ -315,6 +402,10 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       }
       P[i] += -std::min(v1, 0.0) * jump * t_side[sd];
       P[j] += std::min(v2, 0.0) * jump * t_side[sd];
+      if (keep_tf) {
+        tf.per_a[((size_t)q * pb->n_periodic + k) * 2] = -std::min(v1, 0.0) * jump;
+        tf.per_a[((size_t)q * pb->n_periodic + k) * 2 + 1] = std::min(v2, 0.0) * jump;
+      }
     }
     if (pb->is_nanowire)
       for (int64_t e = 0; e < n; ++e) P[e] += -sq[2];
@@ -356,13 +447,16 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       o.err = "upwind graph of direction " + std::to_string(q) + " has a cycle not broken by periodic cuts";
       return;
     }
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return level[a] < level[b]; });
+    // elements ordered by (level, element id): a counting sort on the level
     int32_t nl = 0;
     for (int64_t e = 0; e < n; ++e) nl = std::max(nl, level[e] + 1);
     o.lev.assign(nl + 1, 0);
     for (int64_t e = 0; e < n; ++e) o.lev[level[e] + 1]++;
     for (int L = 0; L < nl; ++L) o.lev[L + 1] += o.lev[L];
+    {
+      std::vector<int32_t> pos(o.lev.begin(), o.lev.end() - 1);
+      for (int64_t e = 0; e < n; ++e) order[pos[level[e]]++] = (int32_t)e;
+    }
 
     // periodic source cells of direction q (sorted unique upstream elements of cut inflow)
     std::vector<int32_t>& src = o.x_cell;
@@ -379,9 +473,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       double v = 0;
       for (int d = 0; d < dim; ++d) v += sq[d] * w_db[w * dim + d];
       if (v < 0) wall_in[w_cell[w]].push_back((int32_t)w);
-      bool any = false;
-      for (int m = 0; m < n_mfp && !any; ++m) any = gb_of(m, q, w) > 0;
-      if (any) wall_out[w_cell[w]].push_back((int32_t)w);
+      if (key_out[(size_t)w_key[w] * n_dir + q]) wall_out[w_cell[w]].push_back((int32_t)w);
     }
 
     // slots: an element is alive from its level to the last level of its consumers; elements
@@ -432,6 +524,10 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         if (f_cut[f]) s.in_idx[it * nf + k] = pack_item(ITEM_PERIODIC, src_idx[f_nb[f]]);
         else s.in_idx[it * nf + k] = pack_item(ITEM_CELL, slot_of[f_nb[f]]);
         s.in_coef[it * nf + k] = g[f] * f_t[f];
+        if (keep_tf) {
+          tf.g0[it * nf + k] = g[f];
+          tf.mode[it * nf + k] = (int32_t)pb->internal[f % ni];
+        }
         ++k;
       }
       for (int32_t w : wall_in[e]) {
@@ -440,6 +536,10 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         for (int d = 0; d < dim; ++d) v += sq[d] * w_db[(int64_t)w * dim + d];
         s.in_idx[it * nf + k] = pack_item(ITEM_WALL, w);
         s.in_coef[it * nf + k] = v * w_scale[w];
+        if (keep_tf) {
+          tf.g0[it * nf + k] = v;
+          tf.mode[it * nf + k] = w < nd0 ? -1 : -((int32_t)pb->internal[(w - nd0) % ni] + 2);
+        }
         ++k;
       }
       auto si = src_idx.find(e);
@@ -546,6 +646,77 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     s.max_wo = std::max(s.max_wo, s.wo_off[q + 1] - wo0);
     std::vector<int32_t>().swap(o.lev);
   }
+  return OBTE_OK;
+}
+
+// New transmissions: every coefficient that depends on t, from the factors kept by build_schedule and
+// with the same arithmetic (inflow coefficients bte.py-style g t or g (1 - t), the periodic jump terms
+// of P, the contact coefficients with their K shifts and alpha term, the offset weights of the walls).
+obte_status set_transmission(Schedule& s, const double* t) {
+  PhaseTimer timer("set_transmission");
+  if (!t) { set_error("null side transmissions"); return OBTE_ERR_BAD_ARG; }
+  if (!s.tim) { set_error("the plan was created without side transmissions"); return OBTE_ERR_BAD_ARG; }
+  const Schedule::TransmissionFactors& tf = s.tf;
+  if (!tf.ok) {
+    set_error("new transmissions need a new plan when the problem has isothermal walls or nanowire terms");
+    return OBTE_ERR_UNSUPPORTED;
+  }
+  for (int64_t k = 0; k < s.n_sides; ++k)
+    if (!(t[k] > 0 && t[k] <= 1)) { set_error("side transmission outside (0, 1]"); return OBTE_ERR_BAD_ARG; }
+  const int64_t n = s.n;
+  const int nf = s.nf, n_dir = s.n_dir, n_mfp = s.n_mfp, m_pad = s.m_pad, ds = s.ds, dim = s.dim;
+  parallel_for((int64_t)n_dir * n, [&](int64_t it) {
+    for (int k = 0; k < nf; ++k) {
+      const size_t e = (size_t)it * nf + k;
+      const int32_t md = tf.mode[e];
+      s.in_coef[e] = md >= 0 ? tf.g0[e] * t[md] : md == -1 ? tf.g0[e] * 1.0 : tf.g0[e] * (1.0 - t[-md - 2]);
+    }
+  });
+  const int64_t np = (int64_t)tf.per_i.size();
+  const int64_t nc = (int64_t)tf.c_side.size();
+  const double nrm = s.normalization;
+  auto sigma_n = [&](int m, int q, int64_t k) {
+    double v = 0;
+    for (int d = 0; d < dim; ++d) v += s.sig[((size_t)q * m_pad + m) * ds + d] * tf.c_na[k * dim + d];
+    return v;
+  };
+  std::fill(s.kshift.begin(), s.kshift.end(), 0.0);
+  parallel_for(n_dir, [&](int64_t qq) {
+    const int q = (int)qq;
+    std::vector<double> P(n, 0.0);
+    for (int64_t k = 0; k < np; ++k) {
+      const double tk = t[tf.per_side[k]];
+      P[tf.per_i[k]] += tf.per_a[((size_t)q * np + k) * 2] * tk;
+      P[tf.per_j[k]] += tf.per_a[((size_t)q * np + k) * 2 + 1] * tk;
+    }
+    const size_t base = (size_t)q * n;
+    for (int64_t p = 0; p < n; ++p) {
+      const size_t it = base + p;
+      const int32_t e = s.cell[it];
+      s.P[it] = P[e];
+      const int32_t ce = s.contact[it];
+      if (ce < 0) continue;
+      for (int m = 0; m < m_pad; ++m) {
+        double kc = 0;
+        if (m < n_mfp)
+          for (int32_t c = tf.co_ptr[e]; c < tf.co_ptr[e + 1]; ++c) {
+            const int32_t k = tf.co_k[c];
+            const double sn = sigma_n(m, q, k);
+            kc += (tf.co_role[c] == 1 ? std::max(sn, 0.0) : std::min(sn, 0.0)) * t[tf.c_side[k]];
+          }
+        s.kcoef[(size_t)ce * m_pad + m] = kc * nrm;
+      }
+      for (int m = 0; m < n_mfp; ++m) s.kshift[(size_t)m * n_dir + q] += s.kcoef[(size_t)ce * m_pad + m];
+    }
+    if (tf.contact_kind == OBTE_CONTACT_PERIODIC || tf.contact_kind == OBTE_CONTACT_MIXED)
+      for (int m = 0; m < n_mfp; ++m) {
+        double acc = 0;
+        for (int64_t k = 0; k < nc; ++k) acc += std::min(sigma_n(m, q, k), 0.0) * t[tf.c_side[k]];
+        s.kconst[(size_t)m * n_dir + q] = s.contact_alpha * acc * nrm;
+      }
+  });
+  for (int64_t w = 0; w < s.nd; ++w)
+    s.ell_B[w] = tf.ell0[w] * (tf.w_side[w] < 0 ? 1.0 : 1.0 - t[tf.w_side[w]]);
   return OBTE_OK;
 }
 

@@ -1006,7 +1006,58 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   // per-sweep values (b, p), padded by 32 B for the aligned TMA window
   OBTE_TRY(d.vals.alloc((size_t)s.n_dir * s.n * 2 * sizeof(Real) + 32));
   OBTE_CUDA(cudaMemsetAsync(d.vals.p, 0, d.vals.bytes, st));
+  if (s.tf.ok) {   // transmission plans: keep what refresh_tables rewrites
+    d.h_rec = std::move(pk.rec);
+    d.h_spec = std::move(pk.spec);
+    d.n_spec = (int64_t)(pk.sr.size() / SR);
+  }
   d.ready = true;
+  return OBTE_OK;
+}
+
+// New transmissions: rewrite the coefficient words of the records and the wall inflow coefficients of
+// the special entries (the same walk over the inflow entries as pack), then P and the contact
+// coefficients; indices, units and launch order stay.
+template <typename Real>
+static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) {
+  const Schedule& s = plan->sched;
+  cudaStream_t st = plan->stream;
+  if (d.h_rec.empty()) { d.ready = false; return OBTE_OK; }   // rebuilt on next use
+  const int W = rec_words(sizeof(Real), s.nf);
+  constexpr int CSTEP = sizeof(Real) / 4, COEF = 4;
+  std::vector<double> sr((size_t)d.n_spec * SR, 0.0);
+  int32_t* rec = d.h_rec.data();
+  parallel_for((int64_t)s.n_dir * s.n, [&](int64_t it) {
+    int32_t* r = rec + it * W;
+    int k = 0, j = 0;
+    for (int f = 0; f < s.nf; ++f) {
+      const int32_t code = s.in_idx[it * s.nf + f];
+      const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
+      const double g = s.in_coef[it * s.nf + f];
+      if (kind == ITEM_CELL || kind == ITEM_PERIODIC) {
+        const Real v = (Real)g;
+        std::memcpy(&r[COEF + k * CSTEP], &v, sizeof(Real));
+        ++k;
+      } else if (kind == ITEM_WALL) {
+        sr[(size_t)d.h_spec[it] * SR + j] = g;
+        ++j;
+      }
+    }
+  });
+  OBTE_CUDA(cudaMemcpyAsync(d.rec.p, rec, d.h_rec.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  OBTE_CUDA(cudaStreamSynchronize(st));
+  OBTE_TRY(upload_real<Real>(d.sr, sr, st));
+  OBTE_TRY(upload(d.Pq, s.P, st));
+  OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
+  if (bytes)
+    *bytes += (int64_t)(d.h_rec.size() * 4 + (sr.size() + s.kcoef.size()) * sizeof(Real) + s.P.size() * 8);
+  return OBTE_OK;
+}
+
+obte_status refresh_tables(obte_plan plan, int64_t* bytes) {
+  PhaseTimer timer("refresh_tables");
+  if (plan->d32.ready) OBTE_TRY(refresh_impl<float>(plan, plan->d32, bytes));
+  if (plan->d64.ready) OBTE_TRY(refresh_impl<double>(plan, plan->d64, bytes));
   return OBTE_OK;
 }
 

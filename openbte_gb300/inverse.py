@@ -98,10 +98,18 @@ class IsotropicMaterial:
 
 
 class PixelSolver:
-    """kappa_eff and dkappa/drho of an n x n pixel cell (one plan per density field)."""
+    """kappa_eff and dkappa/drho of an n x n pixel cell.
+
+    The plan (sweep order, slots, device tables) depends on the grid and the directions only: it is built on
+    the first call and later density fields replace its transmissions (``obte_bte_plan_set_transmission``),
+    as the reference recomputes only its density-dependent terms per field (openbte/inverse/bte.py:147-173)
+    over the geometry of bte.py:116-140.  ``reuse_plan=False`` builds a new plan per field instead.
+    ``warm_start=True`` starts each solve from the previous field's solution (the reference's x0 reuse,
+    bte.py:234-236); the default starts from zero, so results do not depend on the call history."""
 
     def __init__(self, n: int, material: IsotropicMaterial, size: float = 1.0, direction=(1, 0), device: int = 0,
-                 precision: str = "fp32_refine", rtol: float = 1e-8, restart: int = 100, max_sweeps: int = 3000):
+                 precision: str = "fp32_refine", rtol: float = 1e-8, restart: int = 100, max_sweeps: int = 3000,
+                 reuse_plan: bool = True, warm_start: bool = False):
         if tuple(direction) not in ((1, 0), (0, 1)):
             raise NotImplementedError("kappa along x ([1, 0]) or y ([0, 1])")
         self.lib = _lib.load()
@@ -118,6 +126,8 @@ class PixelSolver:
         self.empty = np.zeros(1, dtype=np.int64)
         self.last_info = None
         self.last_upload_bytes = 0
+        self.reuse_plan, self.warm_start = reuse_plan, warm_start
+        self._h = None
 
     def _problem(self, t_host):
         g = self.grid
@@ -137,6 +147,38 @@ class PixelSolver:
         p.side_transmission, p.reflect_internal = ptr(t_host), 1
         return p
 
+    def _plan(self, t_host):
+        """The plan with side transmissions t_host: the cached one updated, or a new one."""
+        if self._h is not None:
+            nb = C.c_int64()
+            _lib.check(self.lib.obte_bte_plan_set_transmission(self._h, ptr(t_host), C.byref(nb)),
+                       "obte_bte_plan_set_transmission")
+            self.last_upload_bytes = nb.value          # coefficients copied to the device
+            return self._h
+        ctx = context(self.device)
+        prob = self._problem(t_host)
+        mat = self.material.c_struct()
+        h = C.c_void_p()
+        _lib.check(self.lib.obte_bte_plan_create(ctx, C.byref(prob), C.byref(mat), C.byref(h)), "obte_bte_plan_create")
+        self._h = h
+        pb, sb = C.c_int64(), C.c_int64()
+        _lib.check(self.lib.obte_bte_plan_footprint(h, _lib.PRECISION[self.precision], self.restart, C.byref(pb),
+                                                    C.byref(sb)), "obte_bte_plan_footprint")
+        self.last_upload_bytes = pb.value              # device tables built from the host schedule (an upper bound)
+        return h
+
+    def close(self):
+        """Release the cached plan."""
+        if self._h is not None:
+            h, self._h = self._h, None
+            self.lib.obte_bte_plan_destroy(h)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
     def kappa_and_gradient(self, rho):
         """(kappa_eff, dkappa/drho as a float64 device tensor [n*n])."""
         torch = _torch()
@@ -144,26 +186,20 @@ class PixelSolver:
         rho = torch.as_tensor(rho, dtype=torch.float64, device=dev).reshape(-1)
         t, da, db = transmission(rho, self.grid)
         t_host = np.ascontiguousarray(t.detach().cpu().numpy())
-        ctx = context(self.device)
-        prob = self._problem(t_host)
-        mat = self.material.c_struct()
-        h = C.c_void_p()
-        _lib.check(self.lib.obte_bte_plan_create(ctx, C.byref(prob), C.byref(mat), C.byref(h)), "obte_bte_plan_create")
+        h = self._plan(t_host)
         try:
-            pb, sb = C.c_int64(), C.c_int64()
-            _lib.check(self.lib.obte_bte_plan_footprint(h, _lib.PRECISION[self.precision], self.restart, C.byref(pb),
-                                                        C.byref(sb)), "obte_bte_plan_footprint")
-            self.last_upload_bytes = pb.value      # device tables built from the host schedule (an upper bound)
             opts = _lib.SolveOpts(precision=_lib.PRECISION[self.precision], rtol=self.rtol, max_sweeps=self.max_sweeps,
-                                  restart=self.restart, refine_steps=20, inner_rtol=1e-5, warm_start=0)
+                                  restart=self.restart, refine_steps=20, inner_rtol=1e-5,
+                                  warm_start=1 if self.warm_start else 0)
             dT0 = torch.zeros(self.grid["n_elems"], dtype=torch.float64, device=dev)
-            grad_t = torch.empty(prob.n_sides, dtype=torch.float64, device=dev)
+            grad_t = torch.empty(self.grid["side_elem_map"].shape[0], dtype=torch.float64, device=dev)
             info = _lib.SolveInfo()
             st = self.lib.obte_bte_kappa_gradient(h, C.byref(opts), C.c_void_p(dT0.data_ptr()),
                                                   C.c_void_p(grad_t.data_ptr()), C.byref(info))
             _lib.check(st, "obte_bte_kappa_gradient")
         finally:
-            self.lib.obte_bte_plan_destroy(h)
+            if not self.reuse_plan:
+                self.close()
         self.last_info = info
         sem = torch.as_tensor(self.grid["side_elem_map"], device=dev)
         g = torch.zeros_like(rho)

@@ -82,3 +82,50 @@ def test_autograd_function_and_reference_factory():
     (kap, _), jac = func(d[name + "_rho"])
     assert abs(kap[0] - d[name + "_kappa"][0]) <= 1e-8 * abs(kap[0])
     np.testing.assert_allclose(jac[0], d[name + "_grad"], rtol=0, atol=1e-6 * np.abs(d[name + "_grad"]).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_refine"])
+def test_updated_plan_matches_new_plan(precision):
+    """A plan whose transmissions were replaced (obte_bte_plan_set_transmission) sweeps exactly like a plan
+    built for the new density field (same coefficients in the FP32 and FP64 tables), and gives its kappa and
+    gradient."""
+    import ctypes as C
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.inverse import IsotropicMaterial, PixelSolver
+    lib = _lib.load()
+    n = 16
+    rng = np.random.default_rng(5)
+    mat = IsotropicMaterial.lognormal(8, 16)
+    rtol = 1e-11 if precision == "fp64" else 1e-8
+    # FP64 solves repeat to rounding; FP32+refine solves differ run to run up to the solve tolerance (the
+    # order of the FP32 sweep's atomic accumulations moves where GMRES stops)
+    ktol, gtol = (1e-12, 1e-12) if precision == "fp64" else (2e-8, 1e-5)
+    reused = PixelSolver(n, mat, size=50.0, precision=precision, rtol=rtol)
+    for step in range(3):
+        rho = rng.uniform(0.05, 1.0, n * n)
+        fresh = PixelSolver(n, mat, size=50.0, precision=precision, rtol=rtol)
+        k1, g1 = reused.kappa_and_gradient(rho)
+        k2, g2 = fresh.kappa_and_gradient(rho)
+        if step:
+            assert reused.last_upload_bytes > 0      # the coefficients of the tables it holds
+        # one sweep of each table precision through both plans, on the same state
+        ne, nd, nx = C.c_int64(), C.c_int64(), C.c_int64()
+        _lib.check(lib.obte_bte_state_layout(fresh._h, C.byref(ne), C.byref(nd), C.byref(nx)), "layout")
+        nu = ne.value + nd.value + nx.value
+        u = torch.as_tensor(rng.standard_normal(nu), device="cuda")
+        torch.cuda.synchronize()
+        for prec in ("fp64", "fp32"):
+            outs = []
+            for h in (reused._h, fresh._h):
+                o = torch.empty_like(u)
+                _lib.check(lib.obte_bte_sweep(h, _lib.PRECISION[prec], C.c_void_p(u.data_ptr()),
+                                              C.c_void_p(o.data_ptr()), 1), "sweep")
+                outs.append(o.cpu().numpy())
+            tol = 1e-13 if prec == "fp64" else 1e-6
+            np.testing.assert_allclose(outs[0], outs[1], rtol=0, atol=tol * np.abs(outs[1]).max())
+        fresh.close()
+        assert abs(k1 - k2) <= ktol * abs(k2), (step, k1, k2)
+        g1, g2 = g1.cpu().numpy(), g2.cpu().numpy()
+        np.testing.assert_allclose(g1, g2, rtol=0, atol=gtol * np.abs(g2).max())
+    reused.close()
