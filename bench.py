@@ -281,6 +281,15 @@ def run_inverse(args, dev):
               for i in range(args.warmup + args.steps)]
     mat = IsotropicMaterial.lognormal(n_mfp, n_dir)
     solver = PixelSolver(n, mat, size=100.0, precision=args.precision, rtol=1e-8, restart=100)
+    if args.profile_gradients:
+        out = []
+        for i in range(args.profile_gradients):
+            t0 = time.perf_counter()
+            k, g = solver.kappa_and_gradient(rho if i == 0 else fields[i % len(fields)])
+            g.cpu()
+            out.append({"ms": (time.perf_counter() - t0) * 1e3, "sweeps": solver.last_info.n_sweeps, "kappa": k})
+        print(json.dumps({"profile_gradients": out, "workload": args.workload, "precision": args.precision}))
+        return
     for i in range(args.warmup):
         solver.kappa_and_gradient(fields[i])
     torch.cuda.synchronize()
@@ -424,6 +433,8 @@ def main():
                     help="only build the Fourier plan and run this many Fourier first-guess solves")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="only build the plan and run this many kappa_eff solves (for launch lists)")
+    ap.add_argument("--profile-gradients", type=int, default=0,
+                    help="config 4: only run this many gradient evaluations on new density fields (for launch lists)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
