@@ -245,6 +245,15 @@ obte_status obte_bte_precond_info(obte_plan plan, int32_t* n_blocks, int32_t* se
  */
 obte_status obte_bte_schedule(obte_plan plan, int32_t q, int64_t* order, int64_t* level_ptr,
                               int64_t* n_levels, int64_t* n_slots);
+/*
+ * Operator coefficients of direction q in the sweep order of obte_bte_schedule, as built on the host
+ * (openbte/bte.py:47-110 per ordinate direction; for bit-exact checks).  Any pointer may be NULL:
+ *   in_coef host [n_elems * elem_nv]  inflow coefficients of each position (upwind faces, then walls;
+ *                                     zero past the last inflow entry)
+ *   D       host [n_elems]            outflow diagonal
+ *   P       host [n_elems]            periodic jump source (and isothermal-wall / nanowire terms)
+ */
+obte_status obte_bte_schedule_coefficients(obte_plan plan, int32_t q, double* in_coef, double* D, double* P);
 
 /* ---- Fourier (openbte/fourier.py:15-185) -------------------------------- */
 typedef struct {

@@ -245,3 +245,15 @@ extern "C" obte_status obte_bte_schedule(obte_plan plan, int32_t q, int64_t* ord
     for (int L = 0; L <= nl; ++L) level_ptr[L] = s.lev_ptr[s.lev_off[q] + L];
   return OBTE_OK;
 }
+
+extern "C" obte_status obte_bte_schedule_coefficients(obte_plan plan, int32_t q, double* in_coef, double* D,
+                                                      double* P) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  const Schedule& s = plan->sched;
+  if (q < 0 || q >= s.n_dir) { set_error("direction out of range"); return OBTE_ERR_BAD_ARG; }
+  const size_t base = (size_t)q * s.n;
+  if (in_coef) std::copy(s.in_coef.begin() + base * s.nf, s.in_coef.begin() + (base + s.n) * s.nf, in_coef);
+  if (D) std::copy(s.D.begin() + base, s.D.begin() + base + s.n, D);
+  if (P) std::copy(s.P.begin() + base, s.P.begin() + base + s.n, P);
+  return OBTE_OK;
+}

@@ -79,6 +79,22 @@ def test_set_transmission_on_host_only_plan():
             assert lib.obte_bte_plan_set_transmission(h, t2.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nb)) == 0
         assert nb.value == 0                      # host-only: nothing uploaded
         assert all(np.array_equal(order(q), b) for q, b in enumerate(before))
+        # the coefficients equal those of a plan built with t2, bit for bit
+        fresh = ctypes.c_void_p()
+        _, prob_t2 = _pixel_problem(n, t2)
+        assert lib.obte_bte_plan_create(None, ctypes.byref(prob_t2), ctypes.byref(mat), ctypes.byref(fresh)) == 0
+        try:
+            nf = 4
+            for q in range(8):
+                got = [np.zeros(n * n * nf), np.zeros(n * n), np.zeros(n * n)]
+                want = [np.zeros(n * n * nf), np.zeros(n * n), np.zeros(n * n)]
+                for hh, arr in ((h, got), (fresh, want)):
+                    assert lib.obte_bte_schedule_coefficients(hh, q, *[a.ctypes.data_as(ctypes.c_void_p) for a in arr]) == 0
+                for a, b in zip(got, want):
+                    assert np.array_equal(a, b)
+                assert np.abs(got[2]).max() > 0          # the periodic jump source is present
+        finally:
+            lib.obte_bte_plan_destroy(fresh)
         bad = t2.copy()
         bad[5] = 0.0
         assert lib.obte_bte_plan_set_transmission(h, bad.ctypes.data_as(ctypes.c_void_p), None) == 1

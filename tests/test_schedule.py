@@ -38,3 +38,31 @@ def test_cycle_is_reported(case):
     with pytest.raises(_lib.OBTEError) as ei:
         Plan(hp, host_only=True)
     assert ei.value.status == 6
+
+
+@pytest.mark.parametrize("name", ["a600", "c0_2k", "cube1k5"])
+def test_operator_coefficients_match_oracle(case, name):
+    """Per direction, in sweep order: the outflow diagonal D, the periodic jump source P and the row sums of
+    the inflow coefficients (upwind faces, cut periodic faces and diffuse walls) equal the oracle's
+    restatement of openbte/bte.py:47-110 (D, P, Gm, Gbm2) to rounding."""
+    import ctypes as C
+    import bte_oracle
+    geo, mat, bcs, ek, _ = case(name)
+    plan = Plan(HostProblem(geo, mat, bcs, ek), host_only=True)
+    ops = bte_oracle.setup_operators(geo, mat, bcs)
+    n, nf = geo.n_elems, len(geo.elems[0])
+    inflow = np.zeros((ops["n_angles"], n))
+    np.add.at(inflow.T, ops["i_mat"], ops["Gm"].T)
+    if ops["Gbm2"] is not None:
+        np.add.at(inflow.T, ops["i_diffuse"], ops["Gbm2"].T)
+    for q in range(ops["n_angles"]):
+        order = plan.schedule(q)[0]
+        cf, D, P = np.zeros(n * nf), np.zeros(n), np.zeros(n)
+        _lib_check = plan.lib.obte_bte_schedule_coefficients(plan.handle, q, *[a.ctypes.data_as(C.c_void_p)
+                                                                             for a in (cf, D, P)])
+        assert _lib_check == 0
+        scale = np.abs(ops["D"][q]).max()
+        np.testing.assert_allclose(D, ops["D"][q][order], rtol=0, atol=1e-13 * scale)
+        np.testing.assert_allclose(P, ops["perturbation"][q][order], rtol=0,
+                                   atol=1e-13 * max(np.abs(ops["perturbation"]).max(), 1e-300))
+        np.testing.assert_allclose(cf.reshape(n, nf).sum(axis=1), inflow[q][order], rtol=0, atol=1e-13 * scale)
