@@ -91,22 +91,64 @@ def mesh_from_cell(cell) -> Mesh:
     face_type, bulk_type = (2, 4) if three else (1, 2)
     labels = {t: name for t, name in enumerate(regions, start=1)}
     labels[len(regions) + 1] = "Bulk"
-    elements = []
-    for t, name in enumerate(regions, start=1):
-        for f in cell.segments[name]:
-            elements.append((face_type, t, [int(x) for x in f]))
-    for e in cell.elems:
-        elements.append((bulk_type, len(regions) + 1, [int(x) for x in e]))
+    dimf = 3 if three else 2
+    segs = [np.asarray(cell.segments[name], dtype=np.int64).reshape(-1, dimf) for name in regions]
+    face_nodes = np.concatenate(segs) if segs else np.zeros((0, dimf), dtype=np.int64)
+    face_tags = np.concatenate([np.full(len(f), t, dtype=np.int64) for t, f in enumerate(segs, start=1)])
+    elems = np.asarray(cell.elems, dtype=np.int64)
     if three:
         nodes = np.asarray(cell.nodes, dtype=np.float64)
         periodic = [(2, 2, 3, cell.periodic["x"]), (2, 4, 5, cell.periodic["y"]), (2, 6, 7, cell.periodic["z"])]
     else:
         nodes = np.concatenate([cell.nodes, np.zeros((len(cell.nodes), 1))], axis=1)
         periodic = [(1, 2, 3, cell.periodic["x"]), (1, 4, 5, cell.periodic["y"])]
-    return build_mesh(labels, nodes, elements, periodic)
+    return _build_mesh(labels, nodes, elems, np.full(len(elems), len(regions) + 1, dtype=np.int64), face_nodes,
+                       face_tags, periodic)
+
+
+def _row_keys(rows, n_nodes):
+    """One int64 per row of sorted node indices, increasing in the rows' lexicographic order, or None when
+    n_nodes ** width does not fit."""
+    w = rows.shape[1]
+    if n_nodes ** w >= 2 ** 62:
+        return None
+    key = rows[:, 0].astype(np.int64)
+    for c in range(1, w):
+        key = key * n_nodes + rows[:, c]
+    return key
+
+
+def _groups(tags, labels):
+    """{label: [positions]} with labels in order of first appearance and positions in order (the grouping
+    of a loop over the elements that appends each position to its label's list)."""
+    out = {}
+    if len(tags) == 0:
+        return out
+    u, first = np.unique(tags, return_index=True)
+    for t in u[np.argsort(first)]:
+        out.setdefault(labels[int(t)], []).append(np.nonzero(tags == t)[0])
+    return {k: np.sort(np.concatenate(v)).tolist() for k, v in out.items()}
 
 
 def build_mesh(labels, nodes3, elements, periodic) -> Mesh:
+    """``Mesh`` from msh2 element records ``(type, tag, nodes)`` (openbte/mesh.py:54-348)."""
+    nodes = np.asarray(nodes3, dtype=np.float64)
+    dim = 2 if np.allclose(nodes[:, 2], np.zeros(nodes.shape[0])) else 3
+    bulk_type = {2: (2, 3), 3: (4,)}[dim]
+    face_type = {2: (1,), 3: (2,)}[dim]
+    bulk = [e for e in elements if e[0] in bulk_type]
+    faces = [e for e in elements if e[0] in face_type]
+    nv = len(bulk[0][2])
+    if any(len(e[2]) != nv for e in bulk):
+        raise ValueError("mixed element types are not supported")
+    elems = np.array([e[2] for e in bulk], dtype=np.int64)
+    bulk_tags = np.array([e[1] for e in bulk], dtype=np.int64)
+    face_nodes = np.array([e[2] for e in faces], dtype=np.int64).reshape(-1, dim)
+    face_tags = np.array([e[1] for e in faces], dtype=np.int64)
+    return _build_mesh(labels, nodes3, elems, bulk_tags, face_nodes, face_tags, periodic)
+
+
+def _build_mesh(labels, nodes3, elems, bulk_tags, face_nodes, face_tags, periodic) -> Mesh:
     nodes = np.asarray(nodes3, dtype=np.float64)
     if np.allclose(nodes[:, 2], np.zeros(nodes.shape[0])):
         dim = 2
@@ -117,21 +159,19 @@ def build_mesh(labels, nodes3, elements, periodic) -> Mesh:
     size = np.zeros(3)
     for i in range(dim):
         size[i] = np.max(nodes[:, i]) - np.min(nodes[:, i])
-
-    bulk_type = {2: (2, 3), 3: (4,)}[dim]
-    face_type = {2: (1,), 3: (2,)}[dim]
-    bulk = [e for e in elements if e[0] in bulk_type]
-    faces = [e for e in elements if e[0] in face_type]
-    nv = len(bulk[0][2])
-    if any(len(e[2]) != nv for e in bulk):
-        raise ValueError("mixed element types are not supported")
-    elems = np.array([e[2] for e in bulk], dtype=np.int64)
+    nv = elems.shape[1]
     n_elems = len(elems)
 
-    # sides in rotation order: side r of an element = sorted(elem[(r+1+j) % nv], j < dim)
+    # sides in rotation order: side r of an element = sorted(elem[(r+1+j) % nv], j < dim); the unique sides
+    # in lexicographic order (np.unique over rows, through one integer key per row when it fits)
     rot = np.array([[(r + 1 + j) % nv for j in range(dim)] for r in range(nv)])
     all_sides = np.sort(elems[:, rot], axis=2).reshape(-1, dim)
-    sides, inverse = np.unique(all_sides, axis=0, return_inverse=True)
+    all_keys = _row_keys(all_sides, n_nodes)
+    if all_keys is not None:
+        side_keys, first, inverse = np.unique(all_keys, return_index=True, return_inverse=True)
+        sides = all_sides[first]
+    else:
+        sides, inverse = np.unique(all_sides, axis=0, return_inverse=True)
     inverse = inverse.reshape(-1)
     n_sides = len(sides)
     esm = inverse.reshape(n_elems, nv).copy()          # elem -> sides (array form)
@@ -144,18 +184,21 @@ def build_mesh(labels, nodes3, elements, periodic) -> Mesh:
     last = np.searchsorted(s_sorted, np.arange(n_sides), side="right") - 1
     side_elem_map = np.stack([o_sorted[first], o_sorted[last]], axis=1).astype(np.int64)
 
-    elem_physical_regions = {}
-    bulk_pos = 0
-    for e in elements:
-        if e[0] in bulk_type:
-            elem_physical_regions.setdefault(labels[e[1]], []).append(bulk_pos)
-            bulk_pos += 1
+    elem_physical_regions = _groups(bulk_tags, labels)
 
-    # side lookup for face elements
-    side_index = {tuple(s): k for k, s in enumerate(sides.tolist())}
+    # side of each face element
+    fs = np.sort(face_nodes, axis=1)
+    if all_keys is not None and len(fs):
+        fk = _row_keys(fs, n_nodes)
+        face_side = np.searchsorted(side_keys, fk)
+        if np.any(face_side >= n_sides) or np.any(side_keys[np.minimum(face_side, n_sides - 1)] != fk):
+            raise KeyError("a face element is not a side of any bulk element")
+    else:
+        side_index = {tuple(s): k for k, s in enumerate(sides.tolist())}
+        face_side = np.array([side_index[tuple(f)] for f in fs.tolist()], dtype=np.int64)
     side_physical_regions = {}
-    for e in faces:
-        side_physical_regions.setdefault(labels[e[1]], []).append(side_index[tuple(sorted(e[2]))])
+    for name, pos in _groups(face_tags, labels).items():
+        side_physical_regions[name] = face_side[pos].tolist()
 
     if dim == 2:
         side_areas = np.linalg.norm(nodes[sides[:, 1]] - nodes[sides[:, 0]], axis=1)
@@ -204,10 +247,14 @@ def build_mesh(labels, nodes3, elements, periodic) -> Mesh:
     periodic_list = []
     periodic_sides_dict = {}
     if periodic:
-        node_side = {}
-        for s, side in enumerate(sides):
-            for t in side:
-                node_side.setdefault(int(t), []).append(s)
+        # node -> its sides in increasing side order
+        flat = sides.reshape(-1)
+        by_node = np.argsort(flat, kind="stable")
+        nptr = np.searchsorted(flat[by_node], np.arange(n_nodes + 1))
+        side_of = (by_node // dim).tolist()
+
+        def sides_of(t):
+            return side_of[nptr[t]:nptr[t + 1]]
         b_regions = [(k, set(v)) for k, v in side_physical_regions.items() if k[-2:] == "_b"]
         in_periodic = set()
         cent = side_centroids.tolist()
@@ -223,8 +270,8 @@ def build_mesh(labels, nodes3, elements, periodic) -> Mesh:
                 corr = []
                 # candidate sides are visited in Python-set order, as the reference does
                 # (openbte/mesh.py:236-244); in 3D one node pair matches several sides
-                for s1 in set(node_side.get(int(a), [])):
-                    for s2 in set(node_side.get(int(b), [])):
+                for s1 in set(sides_of(int(a))):
+                    for s2 in set(sides_of(int(b))):
                         if close(cent[s1], [c + d for c, d in zip(cent[s2], L)]):
                             corr.append((s1, s2))
                 for s1, s2 in corr:
@@ -298,7 +345,7 @@ def build_mesh(labels, nodes3, elements, periodic) -> Mesh:
     diff_dist[eb, slot(eb, sb)] = side_centroids[sb] - elem_centroids[eb]
     gradient_weights = np.linalg.pinv(diff_dist)
 
-    elem_side_map = {i: list(esm[i]) for i in range(n_elems)}
+    elem_side_map = dict(enumerate(esm.tolist()))
     return Mesh(n_elems, n_nodes, dim, size, nodes, sides, elems, elem_side_map, side_elem_map,
                 normal_areas, gradient_weights, interp_weights, elem_centroids, side_centroids,
                 elem_volumes, side_areas, dists, second_order_correction, internal, boundary_sides,
