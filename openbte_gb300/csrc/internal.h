@@ -11,6 +11,8 @@
 #include <memory>
 #include <thread>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/obte.h"
@@ -146,17 +148,39 @@ constexpr int32_t ITEM_MASK = (1 << ITEM_SHIFT) - 1;
 inline int32_t pack_item(int kind, int32_t idx) { return (int32_t)((uint32_t)kind << ITEM_SHIFT) | idx; }
 
 // Host-side sweep schedule: one direction per block of n_elems items (level order).
+// Allocator whose resize() leaves trivially constructible elements uninitialised: the per-direction
+// schedule arrays (hundreds of MB on large meshes) are first written by the parallel direction workers,
+// so their pages are touched in parallel instead of by one serial zero fill.
+template <typename T>
+struct DefaultInitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind { using other = DefaultInitAlloc<U>; };
+  DefaultInitAlloc() noexcept = default;
+  template <typename U>
+  DefaultInitAlloc(const DefaultInitAlloc<U>&) noexcept {}
+  template <typename U>
+  void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <typename U, typename... A>
+  void construct(U* p, A&&... a) {
+    ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <typename T>
+using RawVec = std::vector<T, DefaultInitAlloc<T>>;
+
 struct Schedule {
   int dim = 2;
   int nf = 3;                      // inflow slots per element (= sides per element)
   int64_t n = 0;                   // elements
   int n_dir = 0, n_mfp = 0, m_pad = 0, n_chunks = 0, ds = 2;
   int64_t nd = 0;                  // diffuse wall sides (T_B entries)
-  // per direction, per position (n_dir * n)
-  std::vector<int32_t> cell, slot, xk, wout, contact;
-  std::vector<int32_t> in_idx;     // n_dir * n * nf
-  std::vector<double> in_coef;     // n_dir * n * nf
-  std::vector<double> D, P;        // n_dir * n
+  // per direction, per position (n_dir * n); written by build_schedule's direction workers
+  RawVec<int32_t> cell, slot, xk, wout, contact;
+  RawVec<int32_t> in_idx;          // n_dir * n * nf
+  RawVec<double> in_coef;          // n_dir * n * nf
+  RawVec<double> D, P;             // n_dir * n
   // levels
   std::vector<int32_t> lev_ptr;    // concatenated level pointers
   std::vector<int64_t> lev_off;    // [n_dir] start of direction q in lev_ptr

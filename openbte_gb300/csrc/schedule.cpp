@@ -324,15 +324,16 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     if (!in_range(pb->mixed_sides[k], ns)) { set_error("mixed side out of range"); return OBTE_ERR_BAD_ARG; }
 
   // ---- per-direction schedule: directions in parallel, merged in direction order ----
-  s.cell.assign((size_t)n_dir * n, 0);
-  s.slot.assign((size_t)n_dir * n, -1);
-  s.xk.assign((size_t)n_dir * n, -1);
-  s.wout.assign((size_t)n_dir * n, 0);
-  s.contact.assign((size_t)n_dir * n, -1);
-  s.in_idx.assign((size_t)n_dir * n * nf, 0);
-  s.in_coef.assign((size_t)n_dir * n * nf, 0.0);
-  s.D.assign((size_t)n_dir * n, 0.0);
-  s.P.assign((size_t)n_dir * n, 0.0);
+  // uninitialised here: each direction worker initialises and fills its own range
+  s.cell.resize((size_t)n_dir * n);
+  s.slot.resize((size_t)n_dir * n);
+  s.xk.resize((size_t)n_dir * n);
+  s.wout.resize((size_t)n_dir * n);
+  s.contact.resize((size_t)n_dir * n);
+  s.in_idx.resize((size_t)n_dir * n * nf);
+  s.in_coef.resize((size_t)n_dir * n * nf);
+  s.D.resize((size_t)n_dir * n);
+  s.P.resize((size_t)n_dir * n);
   s.nlev.assign(n_dir, 0);
   s.nslots.assign(n_dir, 0);
   if (keep_tf) {
@@ -510,6 +511,11 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
 
     // items in level order (wout and contact indices local to the direction; rebased on merge)
     const size_t base = (size_t)q * n;
+    std::fill(s.xk.begin() + base, s.xk.begin() + base + n, -1);
+    std::fill(s.wout.begin() + base, s.wout.begin() + base + n, 0);
+    std::fill(s.contact.begin() + base, s.contact.begin() + base + n, -1);
+    std::fill(s.in_idx.begin() + base * nf, s.in_idx.begin() + (base + n) * nf, 0);
+    std::fill(s.in_coef.begin() + base * nf, s.in_coef.begin() + (base + n) * nf, 0.0);
     for (int64_t p = 0; p < n; ++p) {
       const int32_t e = order[p];
       const size_t it = base + p;
@@ -619,6 +625,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.kcoef.clear();
   s.scoef.clear();
   s.max_slots = s.max_src = s.max_wo = 0;
+  std::vector<int32_t> wo_base(n_dir), ce_base(n_dir);
   for (int q = 0; q < n_dir; ++q) {
     DirOut& o = outs[q];
     if (o.st != OBTE_OK) { set_error(o.err); return o.st; }
@@ -633,12 +640,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     const int32_t wo0 = (int32_t)s.wo_wall.size();
     const int32_t ce0 = (int32_t)s.scoef.size();
     s.wo_off[q] = wo0;
-    const size_t base = (size_t)q * n;
-    for (int64_t p = 0; p < n; ++p) {
-      const size_t it = base + p;
-      if (s.wout[it]) s.wout[it] = (((s.wout[it] >> 3) + wo0) << 3) | (s.wout[it] & 7);
-      if (s.contact[it] >= 0) s.contact[it] += ce0;
-    }
+    wo_base[q] = wo0;
+    ce_base[q] = ce0;
     s.wo_wall.insert(s.wo_wall.end(), o.wo_wall.begin(), o.wo_wall.end());
     s.kcoef.insert(s.kcoef.end(), o.kcoef.begin(), o.kcoef.end());
     s.scoef.insert(s.scoef.end(), o.scoef.begin(), o.scoef.end());
@@ -646,6 +649,16 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     s.max_wo = std::max(s.max_wo, s.wo_off[q + 1] - wo0);
     std::vector<int32_t>().swap(o.lev);
   }
+  // wall-output and contact indices from direction-local to global
+  parallel_for(n_dir, [&](int64_t q) {
+    const size_t base = (size_t)q * n;
+    const int32_t wo0 = wo_base[q], ce0 = ce_base[q];
+    for (int64_t p = 0; p < n; ++p) {
+      const size_t it = base + p;
+      if (s.wout[it]) s.wout[it] = (((s.wout[it] >> 3) + wo0) << 3) | (s.wout[it] & 7);
+      if (s.contact[it] >= 0) s.contact[it] += ce0;
+    }
+  });
   return OBTE_OK;
 }
 

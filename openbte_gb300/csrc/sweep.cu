@@ -1047,7 +1047,7 @@ static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) 
   OBTE_CUDA(cudaMemcpyAsync(d.rec.p, rec, d.h_rec.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
   OBTE_CUDA(cudaStreamSynchronize(st));
   OBTE_TRY(upload_real<Real>(d.sr, sr, st));
-  OBTE_TRY(upload(d.Pq, s.P, st));
+  OBTE_CUDA(cudaMemcpy(d.Pq.p, s.P.data(), s.P.size() * sizeof(double), cudaMemcpyHostToDevice));
   OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
   if (bytes)
     *bytes += (int64_t)(d.h_rec.size() * 4 + (sr.size() + s.kcoef.size()) * sizeof(Real) + s.P.size() * 8);
