@@ -59,3 +59,23 @@ def test_seeded_generator_is_deterministic():
     b = porous_cell_2d(800, 0.25, "square", seed=4)
     np.testing.assert_array_equal(a.nodes, b.nodes)
     np.testing.assert_array_equal(a.elems, b.elems)
+
+
+@pytest.mark.parametrize("three", [False, True])
+def test_row_key_and_fallback_paths_agree(monkeypatch, three):
+    """Sides and face lookups through integer row keys give the mesh of the np.unique(axis=0) / dict path
+    that very large meshes take (n_nodes ** dim beyond int64)."""
+    from openbte_gb300 import mesh as M
+    from openbte_gb300.geometry import porous_cube_3d
+    cell = porous_cube_3d(800, 0.1, seed=2) if three else porous_cell_2d(600, 0.25, "circle", seed=9)
+    a = mesh_from_cell(cell)
+    monkeypatch.setattr(M, "_row_keys", lambda rows, n_nodes: None)
+    b = mesh_from_cell(cell)
+    for fld in a._fields:
+        x, y = getattr(a, fld), getattr(b, fld)
+        if isinstance(x, dict):
+            assert list(x.keys()) == list(y.keys()), fld
+            for k in x:
+                np.testing.assert_array_equal(np.asarray(x[k]), np.asarray(y[k]), err_msg=f"{fld}[{k}]")
+        else:
+            np.testing.assert_array_equal(np.asarray(x), np.asarray(y), err_msg=fld)
