@@ -371,6 +371,17 @@ def run_inverse(args, dev):
     print(json.dumps(line))
 
 
+def max_over_ranks(x, world, device):
+    """The largest x over the ranks of the process group (one replica per rank; the slowest sets the time)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -558,11 +569,7 @@ def main():
         t_total = time.perf_counter() - t_start
     launches = (lib.obte_launch_count() - l0) / args.steps
     kappa = info.kappa_eff
-    t_step = max(sum(lat), 1e-12) / args.steps
-    if world > 1:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(max(sum(lat), 1e-12) / args.steps, world, dev)
     value = world / t_step
 
     # plain FP64 on the same GPU
