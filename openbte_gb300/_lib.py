@@ -106,6 +106,7 @@ SIGNATURES = [
                                         C.POINTER(C.c_double)]),
     ("obte_bte_schedule", C.c_int, [C.c_void_p, C.c_int32, p_i64, p_i64, p_i64, p_i64]),
     ("obte_bte_schedule_coefficients", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("obte_bte_tables_digest", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint64)]),
     ("obte_fourier_plan_create", C.c_int, [C.c_void_p, C.POINTER(FourierProblem), C.POINTER(C.c_void_p)]),
     ("obte_fourier_plan_destroy", C.c_int, [C.c_void_p]),
     ("obte_fourier_solve", C.c_int, [C.c_void_p, C.POINTER(FourierOpts), C.c_void_p, C.c_void_p,

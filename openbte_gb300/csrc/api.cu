@@ -56,6 +56,14 @@ obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
   }
   return OBTE_OK;
 }
+obte_status upload_bytes(DevBuf& b, const void* p, size_t bytes, cudaStream_t stream) {
+  OBTE_TRY(b.alloc(std::max<size_t>(bytes, 1)));
+  if (bytes) {
+    OBTE_CUDA(cudaMemcpyAsync(b.p, p, bytes, cudaMemcpyHostToDevice, stream));
+    OBTE_CUDA(cudaStreamSynchronize(stream));
+  }
+  return OBTE_OK;
+}
 template obte_status upload<int32_t>(DevBuf&, const std::vector<int32_t>&, cudaStream_t);
 template obte_status upload<int64_t>(DevBuf&, const std::vector<int64_t>&, cudaStream_t);
 template obte_status upload<double>(DevBuf&, const std::vector<double>&, cudaStream_t);
@@ -244,6 +252,11 @@ extern "C" obte_status obte_bte_schedule(obte_plan plan, int32_t q, int64_t* ord
   if (level_ptr)
     for (int L = 0; L <= nl; ++L) level_ptr[L] = s.lev_ptr[s.lev_off[q] + L];
   return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_tables_digest(obte_plan plan, int32_t precision, uint64_t* digest) {
+  if (!plan || !digest) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  return tables_digest(plan, precision != OBTE_FP64, digest);
 }
 
 extern "C" obte_status obte_bte_schedule_coefficients(obte_plan plan, int32_t q, double* in_coef, double* D,

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <algorithm>
+#include <atomic>
 #include <memory>
 #include <thread>
 #include <string>
@@ -57,6 +58,24 @@ void parallel_for(int64_t n, F&& f) {
   for (int t = 0; t < nt; ++t)
     pool.emplace_back([&, t] {
       for (int64_t i = n * t / nt; i < n * (t + 1) / nt; ++i) f(i);
+    });
+  for (auto& th : pool) th.join();
+}
+
+// f(i) for i in [0, n) where each i is a large task (a direction): one task at a time per host thread,
+// handed out in index order from a shared counter (results must not depend on the assignment).
+template <typename F>
+void parallel_tasks(int64_t n, F&& f) {
+  const int nt = (int)std::min<int64_t>(host_threads(), n);
+  if (nt <= 1) {
+    for (int64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int64_t> next(0);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&] {
+      for (int64_t i = next++; i < n; i = next++) f(i);
     });
   for (auto& th : pool) th.join();
 }
@@ -114,6 +133,7 @@ struct HostBuf {
 // Upload a host vector into a fresh device buffer (synchronous on `stream`).
 template <typename T>
 obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream);
+obte_status upload_bytes(DevBuf& b, const void* p, size_t bytes, cudaStream_t stream);
 
 // ---- smoothed-aggregation AMG (preconditioner of the Fourier CG, amg.cu) ---------------------------
 struct AmgHierarchy;
@@ -169,6 +189,10 @@ struct DefaultInitAlloc : std::allocator<T> {
 };
 template <typename T>
 using RawVec = std::vector<T, DefaultInitAlloc<T>>;
+template <typename T>
+obte_status upload(DevBuf& b, const RawVec<T>& v, cudaStream_t stream) {
+  return upload_bytes(b, v.data(), v.size() * sizeof(T), stream);
+}
 
 struct Schedule {
   int dim = 2;
@@ -265,7 +289,7 @@ struct DevSchedule {
   DevBuf lpt;                              // launch order: CTAs of the directions with the most units first
   // transmission plans: host copies of the packed records and of the special-entry index, so that new
   // transmissions rewrite the coefficient words in place (refresh_tables)
-  std::vector<int32_t> h_rec, h_spec;
+  RawVec<int32_t> h_rec, h_spec;
   int64_t n_spec = 0;
   size_t bytes() const;
 };
@@ -340,6 +364,8 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
 obte_status ensure_tables(obte_plan plan, bool fp32);
 // After set_transmission: the coefficient words of the device tables that exist (bytes uploaded added to *bytes).
 obte_status refresh_tables(obte_plan plan, int64_t* bytes);
+// Digest of the packed sweep tables of one precision, built on the host.
+obte_status tables_digest(obte_plan plan, bool fp32, uint64_t* digest);
 // Periodic-inflow preconditioner (xprec.cu): built once per plan.
 obte_status ensure_xprec(obte_plan plan, SolveWork& wk);
 // out[X blocks] += W in[X blocks] (fp32: FP32 accumulation, for stages with an FP32 Krylov basis)

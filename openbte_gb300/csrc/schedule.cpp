@@ -650,7 +650,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     std::vector<int32_t>().swap(o.lev);
   }
   // wall-output and contact indices from direction-local to global
-  parallel_for(n_dir, [&](int64_t q) {
+  parallel_tasks(n_dir, [&](int64_t q) {
     const size_t base = (size_t)q * n;
     const int32_t wo0 = wo_base[q], ce0 = ce_base[q];
     for (int64_t p = 0; p < n; ++p) {
@@ -694,7 +694,7 @@ obte_status set_transmission(Schedule& s, const double* t) {
     return v;
   };
   std::fill(s.kshift.begin(), s.kshift.end(), 0.0);
-  parallel_for(n_dir, [&](int64_t qq) {
+  parallel_tasks(n_dir, [&](int64_t qq) {
     const int q = (int)qq;
     std::vector<double> P(n, 0.0);
     for (int64_t k = 0; k < np; ++k) {

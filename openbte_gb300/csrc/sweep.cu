@@ -39,6 +39,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <numeric>
 
 #include "internal.h"
 
@@ -84,22 +85,20 @@ struct Units {
 
 static void build_units_capped(const Schedule& s, int cap_pf, int cap_sx, Units& un, int64_t* over_pf,
                                int64_t* over_sx) {
-  un.ptr.clear();
-  un.off.assign(s.n_dir, 0);
-  un.n.assign(s.n_dir, 0);
-  if (over_pf) *over_pf = 0;
-  if (over_sx) *over_sx = 0;
-  for (int q = 0; q < s.n_dir; ++q) {
-    un.off[q] = (int64_t)un.ptr.size();
+  // directions in parallel into their own lists, concatenated in direction order
+  std::vector<std::vector<int32_t>> per(s.n_dir);
+  std::vector<int64_t> opf(s.n_dir, 0), osx(s.n_dir, 0);
+  parallel_tasks(s.n_dir, [&](int64_t qq) {
+    const int q = (int)qq;
+    std::vector<int32_t>& ptr = per[q];
     const int32_t* lp = s.lev_ptr.data() + s.lev_off[q];
-    un.ptr.push_back(0);
+    ptr.push_back(0);
     for (int Lv = 0; Lv < s.nlev[q]; ++Lv) {
       int cnt = 0, npf = 0, nsx = 0;
       auto close = [&](int32_t end) {
-        un.ptr.push_back(end);
-        un.n[q]++;
-        if (over_pf && npf > kUnitPf) ++*over_pf;
-        if (over_sx && nsx > kUnitSx) ++*over_sx;
+        ptr.push_back(end);
+        if (npf > kUnitPf) ++opf[q];
+        if (nsx > kUnitSx) ++osx[q];
         cnt = npf = nsx = 0;
       };
       for (int32_t pos = lp[Lv]; pos < lp[Lv + 1]; ++pos) {
@@ -115,7 +114,20 @@ static void build_units_capped(const Schedule& s, int cap_pf, int cap_sx, Units&
       }
       if (cnt > 0) close(lp[Lv + 1]);
     }
+  });
+  un.ptr.clear();
+  un.off.assign(s.n_dir, 0);
+  un.n.assign(s.n_dir, 0);
+  size_t total = 0;
+  for (int q = 0; q < s.n_dir; ++q) total += per[q].size();
+  un.ptr.reserve(total);
+  for (int q = 0; q < s.n_dir; ++q) {
+    un.off[q] = (int64_t)un.ptr.size();
+    un.n[q] = (int32_t)per[q].size() - 1;
+    un.ptr.insert(un.ptr.end(), per[q].begin(), per[q].end());
   }
+  if (over_pf) *over_pf = std::accumulate(opf.begin(), opf.end(), (int64_t)0);
+  if (over_sx) *over_sx = std::accumulate(osx.begin(), osx.end(), (int64_t)0);
 }
 
 static void build_units(const Schedule& s, Units& un) {
@@ -129,8 +141,10 @@ static void build_units(const Schedule& s, Units& un) {
 }
 
 struct Packed {
-  std::vector<int32_t> rec, cellmap, si, spec;
-  std::vector<double> P, sr;
+  RawVec<int32_t> rec, cellmap, spec;   // one entry per item, every one written by pass 2
+  RawVec<double> P;
+  std::vector<int32_t> si;
+  std::vector<double> sr;
   // periodic inflow prefetch: the source indices read by unit u (one entry per cut inflow face, in
   // element then face order), each unit's list padded with -1 to a multiple of 4 ints; kpf[u] is the
   // absolute start of unit u's list (n[q] + 1 entries per direction, indexed like Units::ptr)
@@ -155,15 +169,21 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
   constexpr int CSTEP = sizeof(Real) / 4, COEF = 4;
   const int S = s.max_slots;
   const int zero_row = S, trash_row = S + 1, prow0 = S + 2;
-  // pass 1: per-unit counts of cut inflow faces and wall re-emission entries
+  // pass 1: per-unit counts of cut inflow faces, wall re-emission entries and output entries, in parallel
+  // over directions; per-unit starts are running sums within the direction (kwo) or over the directions
+  // in order (kpf, ksx), so the direction totals are summed in order between the two parallel steps
   pk.emax = pk.pf_pad = pk.unit_wo = pk.unit_sx = 0;
   pk.kwo.assign(un.ptr.size(), 0);
   pk.kpf.assign(un.ptr.size(), 0);
   pk.ksx.assign(un.ptr.size(), 0);
-  int64_t n_pf = 0, n_sx = 0;
-  for (int q = 0; q < s.n_dir; ++q) {
+  std::vector<int64_t> pf_tot(s.n_dir + 1, 0), sx_tot(s.n_dir + 1, 0);
+  std::vector<int> emax_q(s.n_dir, 0), pfpad_q(s.n_dir, 0), uwo_q(s.n_dir, 0), usx_q(s.n_dir, 0);
+  std::vector<char> wo_bad(s.n_dir, 0);
+  parallel_tasks(s.n_dir, [&](int64_t qq) {
+    const int q = (int)qq;
     const int32_t* up = un.ptr.data() + un.off[q];
     int32_t wo_run = 0;
+    int64_t pf_run = 0, sx_run = 0;
     for (int u = 0; u < un.n[q]; ++u) {
       int cnt = 0, wcnt = 0, scnt = 0;
       for (int32_t pos = up[u]; pos < up[u + 1]; ++pos) {
@@ -175,27 +195,45 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
       }
       const int padded = (cnt + 3) & ~3;
       pk.kwo[un.off[q] + u] = wo_run;
-      pk.kpf[un.off[q] + u] = (int32_t)n_pf;
-      pk.ksx[un.off[q] + u] = (int32_t)n_sx;
-      n_sx += scnt;
-      pk.unit_sx = std::max(pk.unit_sx, scnt);
+      pk.kpf[un.off[q] + u] = (int32_t)pf_run;   // relative here, made absolute below
+      pk.ksx[un.off[q] + u] = (int32_t)sx_run;
+      sx_run += scnt;
+      usx_q[q] = std::max(usx_q[q], scnt);
       wo_run += wcnt;
-      n_pf += padded;
-      pk.emax = std::max(pk.emax, cnt);
-      pk.pf_pad = std::max(pk.pf_pad, padded);
-      pk.unit_wo = std::max(pk.unit_wo, wcnt);
+      pf_run += padded;
+      emax_q[q] = std::max(emax_q[q], cnt);
+      pfpad_q[q] = std::max(pfpad_q[q], padded);
+      uwo_q[q] = std::max(uwo_q[q], wcnt);
     }
     pk.kwo[un.off[q] + un.n[q]] = wo_run;
-    pk.kpf[un.off[q] + un.n[q]] = (int32_t)n_pf;
-    pk.ksx[un.off[q] + un.n[q]] = (int32_t)n_sx;
-    if (wo_run != s.wo_off[q + 1] - s.wo_off[q]) {
+    pk.kpf[un.off[q] + un.n[q]] = (int32_t)pf_run;
+    pk.ksx[un.off[q] + un.n[q]] = (int32_t)sx_run;
+    pf_tot[q + 1] = pf_run;
+    sx_tot[q + 1] = sx_run;
+    wo_bad[q] = wo_run != s.wo_off[q + 1] - s.wo_off[q];
+  });
+  for (int q = 0; q < s.n_dir; ++q) {
+    if (wo_bad[q]) {
       set_error("wall re-emission entries are not in sweep order");
       return OBTE_ERR_BAD_ARG;
     }
+    pf_tot[q + 1] += pf_tot[q];
+    sx_tot[q + 1] += sx_tot[q];
+    pk.emax = std::max(pk.emax, emax_q[q]);
+    pk.pf_pad = std::max(pk.pf_pad, pfpad_q[q]);
+    pk.unit_wo = std::max(pk.unit_wo, uwo_q[q]);
+    pk.unit_sx = std::max(pk.unit_sx, usx_q[q]);
   }
+  const int64_t n_pf = pf_tot[s.n_dir], n_sx = sx_tot[s.n_dir];
   if (n_pf >= (int64_t)1 << 31 || n_sx >= (int64_t)1 << 31) {
     set_error("too many periodic inflow faces or output entries"); return OBTE_ERR_UNSUPPORTED;
   }
+  parallel_tasks(s.n_dir, [&](int64_t q) {
+    for (int u = 0; u <= un.n[q]; ++u) {
+      pk.kpf[un.off[q] + u] += (int32_t)pf_tot[q];
+      pk.ksx[un.off[q] + u] += (int32_t)sx_tot[q];
+    }
+  });
   pk.sx.assign((size_t)std::max<int64_t>(n_sx, 1) * 4, 0);
   pk.rows = ring_rows(s, pk.emax);
   if (pk.rows >= 65535 || s.max_src >= (1 << 30)) {
@@ -204,10 +242,10 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
   }
   pk.pf.assign((size_t)n_pf, -1);
   const size_t total = (size_t)s.n_dir * s.n;
-  pk.rec.assign(total * W, 0);
-  pk.cellmap.assign(total, 0);
-  pk.spec.assign(total, -1);
-  pk.P.assign(total, 0.0);
+  pk.rec.resize(total * W);     // uninitialised: pass 2 writes every word of every record
+  pk.cellmap.resize(total);
+  pk.spec.resize(total);
+  pk.P.resize(total);
   pk.si.clear();
   pk.sr.clear();
   // pass 2: records, in parallel over directions.  Elements with outputs or wall inflow get a "special"
@@ -219,7 +257,7 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
     return false;
   };
   std::vector<int64_t> spec_base(s.n_dir + 1, 0);
-  parallel_for(s.n_dir, [&](int64_t q) {
+  parallel_tasks(s.n_dir, [&](int64_t q) {
     int64_t c = 0;
     for (int64_t pos = 0; pos < s.n; ++pos) c += is_special((size_t)q * s.n + pos) ? 1 : 0;
     spec_base[q + 1] = c;
@@ -228,7 +266,7 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
   pk.si.assign((size_t)spec_base[s.n_dir] * SI, 0);
   pk.sr.assign((size_t)spec_base[s.n_dir] * SR, 0.0);
   std::vector<int> dir_err(s.n_dir, 0);   // 1: outputs without a ring slot, 2: more than three wall inflows
-  parallel_for(s.n_dir, [&](int64_t qq) {
+  parallel_tasks(s.n_dir, [&](int64_t qq) {
     const int q = (int)qq;
     int64_t nsp = spec_base[q];
     const int32_t* up = un.ptr.data() + un.off[q];
@@ -293,6 +331,8 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
           std::copy(si, si + SI, pk.si.begin() + (size_t)nsp * SI);
           std::copy(sr, sr + SR, pk.sr.begin() + (size_t)nsp * SR);
           ++nsp;
+        } else {
+          pk.spec[it] = -1;
         }
         for (int f = 0; f < s.nf; ++f) {
           const Real v = (Real)coef[f];
@@ -300,6 +340,7 @@ static obte_status pack(const Schedule& s, const Units& un, Packed& pk) {
         }
         const Real dv = (Real)s.D[it];
         std::memcpy(&r[COEF + s.nf * CSTEP], &dv, sizeof(Real));
+        for (int wd = COEF + (s.nf + 1) * CSTEP; wd < W; ++wd) r[wd] = 0;   // padding to 16 bytes
       }
     }
   });
@@ -1052,6 +1093,50 @@ static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) 
   if (bytes)
     *bytes += (int64_t)(d.h_rec.size() * 4 + (sr.size() + s.kcoef.size()) * sizeof(Real) + s.P.size() * 8);
   return OBTE_OK;
+}
+
+// FNV-1a over the packed tables of one precision, built on the host (no device involved).
+namespace {
+struct Fnv {
+  uint64_t h = 1469598103934665603ull;
+  void bytes(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  }
+  template <typename V>
+  void vec(const V& v) {
+    const uint64_t n = v.size();
+    bytes(&n, sizeof n);
+    if (n) bytes(v.data(), n * sizeof(v[0]));
+  }
+  void i(int64_t x) { bytes(&x, sizeof x); }
+};
+}  // namespace
+
+template <typename Real>
+static obte_status tables_digest_impl(const Schedule& s, uint64_t* digest) {
+  Units un;
+  {
+    PhaseTimer tu("units");
+    build_units(s, un);
+  }
+  Packed pk;
+  {
+    PhaseTimer tp("pack");
+    OBTE_TRY(pack<Real>(s, un, pk));
+  }
+  Fnv f;
+  f.vec(un.ptr); f.vec(un.off); f.vec(un.n);
+  f.vec(pk.rec); f.vec(pk.cellmap); f.vec(pk.si); f.vec(pk.spec); f.vec(pk.P); f.vec(pk.sr);
+  f.vec(pk.pf); f.vec(pk.kpf); f.vec(pk.sx); f.vec(pk.ksx); f.vec(pk.kwo);
+  f.i(pk.unit_sx); f.i(pk.emax); f.i(pk.pf_pad); f.i(pk.unit_wo); f.i(pk.rows);
+  *digest = f.h;
+  return OBTE_OK;
+}
+
+obte_status tables_digest(obte_plan plan, bool fp32, uint64_t* digest) {
+  PhaseTimer timer("tables_digest");
+  return fp32 ? tables_digest_impl<float>(plan->sched, digest) : tables_digest_impl<double>(plan->sched, digest);
 }
 
 obte_status refresh_tables(obte_plan plan, int64_t* bytes) {
