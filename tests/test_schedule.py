@@ -66,3 +66,23 @@ def test_operator_coefficients_match_oracle(case, name):
         np.testing.assert_allclose(P, ops["perturbation"][q][order], rtol=0,
                                    atol=1e-13 * max(np.abs(ops["perturbation"]).max(), 1e-300))
         np.testing.assert_allclose(cf.reshape(n, nf).sum(axis=1), inflow[q][order], rtol=0, atol=1e-13 * scale)
+
+
+@pytest.mark.parametrize("name", ["c0_2k", "cube1k5"])
+def test_tables_do_not_depend_on_host_threads(case, name, monkeypatch):
+    """The schedule and the packed sweep tables (FP32 and FP64) are the same for 1, 3 and 8 host threads."""
+    import ctypes as C
+    from openbte_gb300 import _lib
+    geo, mat, bcs, ek, _ = case(name)
+    digests = set()
+    for threads in ("1", "3", "8"):
+        monkeypatch.setenv("OBTE_HOST_THREADS", threads)
+        plan = Plan(HostProblem(geo, mat, bcs, ek), host_only=True)
+        d = []
+        for prec in ("fp32", "fp64"):
+            v = C.c_uint64()
+            _lib.check(plan.lib.obte_bte_tables_digest(plan.handle, _lib.PRECISION[prec], C.byref(v)), "digest")
+            d.append(v.value)
+        d.append(tuple(int(x) for q in range(mat.vmfp.shape[0]) for x in plan.schedule(q)[0][:50]))
+        digests.add(tuple(d))
+    assert len(digests) == 1
