@@ -206,32 +206,33 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   }
   if (ck == OBTE_CONTACT_NANOWIRE && ds < 3) { set_error("nanowire contact needs sigma_z"); return OBTE_ERR_BAD_ARG; }
   const int64_t nc = (int64_t)c_e1.size();
-  // contact element -> list of (contact side, role) ; role 1 = e1, 2 = e2
-  std::unordered_map<int32_t, std::vector<std::pair<int64_t, int>>> contact_of;
+  // contact element e -> its (contact side k, role) pairs, role 1 = e1, 2 = e2, in contact-side order:
+  // co_k / co_role [co_ptr[e], co_ptr[e + 1])
+  std::vector<int32_t> co_ptr(n + 1, 0), co_k, co_role;
   for (int64_t k = 0; k < nc; ++k) {
-    contact_of[c_e1[k]].push_back({k, 1});
-    if (c_e2[k] >= 0) contact_of[c_e2[k]].push_back({k, 2});
+    co_ptr[c_e1[k] + 1]++;
+    if (c_e2[k] >= 0) co_ptr[c_e2[k] + 1]++;
+  }
+  for (int64_t e = 0; e < n; ++e) co_ptr[e + 1] += co_ptr[e];
+  co_k.assign(co_ptr[n], 0);
+  co_role.assign(co_ptr[n], 0);
+  {
+    std::vector<int32_t> fill(co_ptr.begin(), co_ptr.end() - 1);
+    for (int64_t k = 0; k < nc; ++k) {
+      co_k[fill[c_e1[k]]] = (int32_t)k;
+      co_role[fill[c_e1[k]]++] = 1;
+      if (c_e2[k] >= 0) {
+        co_k[fill[c_e2[k]]] = (int32_t)k;
+        co_role[fill[c_e2[k]]++] = 2;
+      }
+    }
   }
   if (keep_tf) {
     for (int64_t k = 0; k < nc; ++k) tf.c_side.push_back((int32_t)pb->contact_sides[k]);
     tf.c_na = c_na;
-    tf.co_ptr.assign(n + 1, 0);
-    for (int64_t k = 0; k < nc; ++k) {
-      tf.co_ptr[c_e1[k] + 1]++;
-      if (c_e2[k] >= 0) tf.co_ptr[c_e2[k] + 1]++;
-    }
-    for (int64_t e = 0; e < n; ++e) tf.co_ptr[e + 1] += tf.co_ptr[e];
-    tf.co_k.assign(tf.co_ptr[n], 0);
-    tf.co_role.assign(tf.co_ptr[n], 0);
-    std::vector<int32_t> fill(tf.co_ptr.begin(), tf.co_ptr.end() - 1);
-    for (int64_t k = 0; k < nc; ++k) {   // the insertion order of contact_of
-      tf.co_k[fill[c_e1[k]]] = (int32_t)k;
-      tf.co_role[fill[c_e1[k]]++] = 1;
-      if (c_e2[k] >= 0) {
-        tf.co_k[fill[c_e2[k]]] = (int32_t)k;
-        tf.co_role[fill[c_e2[k]]++] = 2;
-      }
-    }
+    tf.co_ptr = co_ptr;
+    tf.co_k = co_k;
+    tf.co_role = co_role;
   }
   auto sigma_n = [&](int m, int q, int64_t k) {
     double v = 0;
@@ -365,7 +366,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
                        std::vector<int32_t>& indeg, std::vector<int32_t>& level, std::vector<int32_t>& order,
                        std::vector<int32_t>& last_use, std::vector<int32_t>& slot_of, std::vector<int64_t>& out_ptr,
                        std::vector<int64_t>& in_ptr, std::vector<int32_t>& out_adj, std::vector<int32_t>& in_face,
-                       std::vector<std::vector<int32_t>>& wall_in, std::vector<std::vector<int32_t>>& wall_out) {
+                       std::vector<std::vector<int32_t>>& wall_in, std::vector<std::vector<int32_t>>& wall_out,
+                       std::vector<int32_t>& src_of) {
     const double* sq = mt->vmfp + (int64_t)q * dd;
     std::fill(D.begin(), D.end(), 0.0);
     std::fill(P.begin(), P.end(), 0.0);
@@ -465,8 +467,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       if (g[f] < 0 && f_cut[f]) src.push_back(f_nb[f]);
     std::sort(src.begin(), src.end());
     src.erase(std::unique(src.begin(), src.end()), src.end());
-    std::unordered_map<int32_t, int32_t> src_idx;
-    for (size_t k = 0; k < src.size(); ++k) src_idx[src[k]] = (int32_t)k;
+    for (size_t k = 0; k < src.size(); ++k) src_of[src[k]] = (int32_t)k;   // reset when the direction is done
 
     // inflow walls / wall outputs per element
     for (int64_t e = 0; e < n; ++e) { wall_in[e].clear(); wall_out[e].clear(); }
@@ -483,8 +484,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     for (int64_t e = 0; e < n; ++e) {
       int32_t lu = -1;
       for (int64_t k = out_ptr[e]; k < out_ptr[e + 1]; ++k) lu = std::max(lu, level[out_adj[k]]);
-      const bool special = src_idx.count((int32_t)e) || !wall_out[e].empty() || ck == OBTE_CONTACT_NANOWIRE ||
-                           contact_of.find((int32_t)e) != contact_of.end();
+      const bool special = src_of[e] >= 0 || !wall_out[e].empty() || ck == OBTE_CONTACT_NANOWIRE ||
+                           co_ptr[e] != co_ptr[e + 1];
       if (special) lu = std::max(lu, level[e]);
       last_use[e] = lu;
       slot_of[e] = -1;
@@ -527,7 +528,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
       for (int64_t t = in_ptr[e]; t < in_ptr[e + 1]; ++t) {
         const int32_t f = in_face[t];
         if (k >= nf) { o.st = OBTE_ERR_BAD_ARG; o.err = "more inflow faces than element sides"; return; }
-        if (f_cut[f]) s.in_idx[it * nf + k] = pack_item(ITEM_PERIODIC, src_idx[f_nb[f]]);
+        if (f_cut[f]) s.in_idx[it * nf + k] = pack_item(ITEM_PERIODIC, src_of[f_nb[f]]);
         else s.in_idx[it * nf + k] = pack_item(ITEM_CELL, slot_of[f_nb[f]]);
         s.in_coef[it * nf + k] = g[f] * f_t[f];
         if (keep_tf) {
@@ -548,8 +549,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         }
         ++k;
       }
-      auto si = src_idx.find(e);
-      if (si != src_idx.end()) s.xk[it] = si->second;
+      if (src_of[e] >= 0) s.xk[it] = src_of[e];
       if (!wall_out[e].empty()) {
         const int32_t begin = (int32_t)o.wo_wall.size();
         if (wall_out[e].size() > 7) { o.st = OBTE_ERR_BAD_ARG; o.err = "too many wall sides on one element"; return; }
@@ -557,8 +557,7 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
         s.wout[it] = (begin << 3) | (int32_t)wall_out[e].size();
       }
       // contact coefficients
-      auto co = contact_of.find(e);
-      if (ck == OBTE_CONTACT_NANOWIRE || co != contact_of.end()) {
+      if (ck == OBTE_CONTACT_NANOWIRE || co_ptr[e] != co_ptr[e + 1]) {
         const int32_t ce = (int32_t)o.scoef.size();
         double sc = 0;
         for (int m = 0; m < m_pad; ++m) {
@@ -567,17 +566,17 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
             if (ck == OBTE_CONTACT_NANOWIRE) {
               kc = mt->sigma[((int64_t)m * n_dir + q) * ds + 2] * vol[e];
             } else {
-              for (auto& pr : co->second) {
-                const double sn = sigma_n(m, q, pr.first);
-                kc += (pr.second == 1 ? std::max(sn, 0.0) : std::min(sn, 0.0)) * c_t[pr.first];
+              for (int32_t c = co_ptr[e]; c < co_ptr[e + 1]; ++c) {
+                const double sn = sigma_n(m, q, co_k[c]);
+                kc += (co_role[c] == 1 ? std::max(sn, 0.0) : std::min(sn, 0.0)) * c_t[co_k[c]];
               }
             }
           }
           o.kcoef.push_back(kc * nrm);
         }
         if (ck != OBTE_CONTACT_NANOWIRE)
-          for (auto& pr : co->second)
-            if (pr.second == 1) sc += c_area[pr.first];
+          for (int32_t c = co_ptr[e]; c < co_ptr[e + 1]; ++c)
+            if (co_role[c] == 1) sc += c_area[co_k[c]];
         o.scoef.push_back(sc * nrm);
         s.contact[it] = ce;
         for (int m = 0; m < n_mfp; ++m) {
@@ -603,9 +602,12 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     std::vector<int32_t> indeg(n), level(n), order(n), last_use(n), slot_of(n), out_adj, in_face;
     std::vector<int64_t> out_ptr(n + 1), in_ptr(n + 1);
     std::vector<std::vector<int32_t>> wall_in(n), wall_out(n);
-    for (int q = tid; q < n_dir; q += nthreads)
+    std::vector<int32_t> src_of(n, -1);   // periodic source index of an element in the current direction
+    for (int q = tid; q < n_dir; q += nthreads) {
       build_dir(q, outs[q], D, P, g, indeg, level, order, last_use, slot_of, out_ptr, in_ptr, out_adj, in_face,
-                wall_in, wall_out);
+                wall_in, wall_out, src_of);
+      for (int32_t e : outs[q].x_cell) src_of[e] = -1;
+    }
   };
   if (nthreads == 1) {
     worker(0);
