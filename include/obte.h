@@ -256,7 +256,8 @@ obte_status obte_bte_schedule(obte_plan plan, int32_t q, int64_t* order, int64_t
 obte_status obte_bte_schedule_coefficients(obte_plan plan, int32_t q, double* in_coef, double* D, double* P);
 /*
  * 64-bit FNV-1a digest of the packed sweep tables (level units, per-item records, special entries, periodic
- * prefetch lists, output entries) that a plan uploads for `precision` (OBTE_FP64: FP64 tables, else FP32),
+ * prefetch lists, output entries, contact coefficients and K shifts, wall outputs, periodic sources, wall
+ * offset weights) that a plan uploads for `precision` (OBTE_FP64: FP64 tables, else FP32),
  * built on the host; works on host-only plans.  Two hosts or builds that pack the same plan identically
  * give the same digest.
  */

@@ -1130,6 +1130,9 @@ static obte_status tables_digest_impl(const Schedule& s, uint64_t* digest) {
   f.vec(pk.rec); f.vec(pk.cellmap); f.vec(pk.si); f.vec(pk.spec); f.vec(pk.P); f.vec(pk.sr);
   f.vec(pk.pf); f.vec(pk.kpf); f.vec(pk.sx); f.vec(pk.ksx); f.vec(pk.kwo);
   f.i(pk.unit_sx); f.i(pk.emax); f.i(pk.pf_pad); f.i(pk.unit_wo); f.i(pk.rows);
+  // the schedule's own uploads: contact coefficients, K shifts, wall outputs, periodic sources
+  f.vec(s.kcoef); f.vec(s.scoef); f.vec(s.kconst); f.vec(s.kshift); f.vec(s.sshift);
+  f.vec(s.wo_wall); f.vec(s.wo_off); f.vec(s.x_cell); f.vec(s.x_base); f.vec(s.ell_B);
   *digest = f.h;
   return OBTE_OK;
 }
