@@ -320,6 +320,11 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
     }
   }
 
+  // directed faces across kept periodic sides (the only ones whose inflow becomes a periodic source)
+  std::vector<int32_t> cut_faces;
+  for (int64_t f = 0; f < nfd; ++f)
+    if (f_cut[f]) cut_faces.push_back((int32_t)f);
+
   // mixed sides are validated up front (the per-direction workers do not report errors for them)
   for (int64_t k = 0; k < pb->n_mixed; ++k)
     if (!in_range(pb->mixed_sides[k], ns)) { set_error("mixed side out of range"); return OBTE_ERR_BAD_ARG; }
@@ -463,8 +468,8 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
 
     // periodic source cells of direction q (sorted unique upstream elements of cut inflow)
     std::vector<int32_t>& src = o.x_cell;
-    for (int64_t f = 0; f < nfd; ++f)
-      if (g[f] < 0 && f_cut[f]) src.push_back(f_nb[f]);
+    for (int32_t f : cut_faces)
+      if (g[f] < 0) src.push_back(f_nb[f]);
     std::sort(src.begin(), src.end());
     src.erase(std::unique(src.begin(), src.end()), src.end());
     for (size_t k = 0; k < src.size(); ++k) src_of[src[k]] = (int32_t)k;   // reset when the direction is done
