@@ -87,3 +87,20 @@ def test_backend_errors_are_reported_per_request():
     srv.close()
     st = {r.rid: r.status for r in res}
     assert st == {0: "ok", 1: "error", 2: "ok"}
+
+
+def test_plan_cache_key_separates_contents():
+    """The plan-cache key (SHA-256 over dtype, shape and bytes) is equal for equal arrays and differs when any
+    value, dtype or shape differs; non-contiguous views hash like their contiguous copies."""
+    import numpy as np
+    from openbte_gb300.runtime import fingerprint
+    a = np.arange(12.0).reshape(3, 4)
+    assert fingerprint(a, 1, None) == fingerprint(a.copy(), 1, None)
+    assert fingerprint(a) != fingerprint(a.reshape(4, 3))
+    assert fingerprint(a) != fingerprint(a.astype(np.float32))
+    b = a.copy()
+    b[2, 3] = np.nextafter(b[2, 3], 99)
+    assert fingerprint(a) != fingerprint(b)
+    assert fingerprint(a.T) == fingerprint(np.ascontiguousarray(a.T))
+    assert fingerprint(np.zeros((3, 0))) != fingerprint(np.zeros((0, 3)))
+    assert fingerprint(None) != fingerprint(0)
