@@ -257,45 +257,60 @@ def _build_mesh(labels, nodes3, elems, bulk_tags, face_nodes, face_tags, periodi
             return side_of[nptr[t]:nptr[t + 1]]
         b_regions = [(k, set(v)) for k, v in side_physical_regions.items() if k[-2:] == "_b"]
         in_periodic = set()
-        cent = side_centroids.tolist()
-        nl = nodes.tolist()
-
-        def close(p, q):
-            # the default np.allclose test |p - q| <= 1e-8 + 1e-5 |q| on every component
-            return all(abs(x - y) <= 1e-8 + 1e-5 * abs(y) for x, y in zip(p, q))
-
-        for (_, _, _, pairs) in periodic:
-            for a, b in pairs.tolist():
-                L = [u - v for u, v in zip(nl[a], nl[b])]
-                corr = []
-                # candidate sides are visited in Python-set order, as the reference does
-                # (openbte/mesh.py:236-244); in 3D one node pair matches several sides
-                for s1 in set(sides_of(int(a))):
-                    for s2 in set(sides_of(int(b))):
-                        if close(cent[s1], [c + d for c, d in zip(cent[s2], L)]):
-                            corr.append((s1, s2))
-                for s1, s2 in corr:
-                    for key, value in b_regions:
-                        if s1 in value and s1 not in in_periodic:
-                            periodic_sides_dict.setdefault(key[:-2], []).append(s1)
-                            periodic_list.append(s1)
-                            in_periodic.add(s1)
-                            to_discard.append(s2)
-                        if s2 in value and s2 not in in_periodic:
-                            periodic_sides_dict.setdefault(key[:-2], []).append(s2)
-                            periodic_list.append(s2)
-                            in_periodic.add(s2)
-                            to_discard.append(s1)
+        # candidate side pairs of every node pair (a, b): the sides of a x the sides of b, each visited in
+        # Python-set order, as the reference does (openbte/mesh.py:236-244); in 3D one node pair matches
+        # several sides.  The centroid test is the default np.allclose, |p - q| <= 1e-8 + 1e-5 |q| on every
+        # component with q = centroid(s2) + (node a - node b), evaluated for all candidates at once.
+        node_pairs = [(int(a), int(b)) for (_, _, _, pairs) in periodic for a, b in pairs.tolist()]
+        c1, c2, cnt = [], [], []
+        for a, b in node_pairs:
+            S1 = np.fromiter(set(sides_of(a)), dtype=np.int64)
+            S2 = np.fromiter(set(sides_of(b)), dtype=np.int64)
+            c1.append(np.repeat(S1, len(S2)))
+            c2.append(np.tile(S2, len(S1)))
+            cnt.append(len(S1) * len(S2))
+        offs = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+        if node_pairs:
+            c1 = np.concatenate(c1)
+            c2 = np.concatenate(c2)
+            na_ = np.repeat(np.array([a for a, _ in node_pairs], dtype=np.int64), cnt)
+            nb_ = np.repeat(np.array([b for _, b in node_pairs], dtype=np.int64), cnt)
+            q = side_centroids[c2] + (nodes[na_] - nodes[nb_])
+            match = np.all(np.abs(side_centroids[c1] - q) <= 1e-8 + 1e-5 * np.abs(q), axis=1)
+            hits = np.nonzero(match)[0]
+            hit_pair = np.searchsorted(offs, hits, side="right") - 1
+            h1, h2 = c1[hits].tolist(), c2[hits].tolist()
+            bounds = np.searchsorted(hit_pair, np.arange(len(node_pairs) + 1)).tolist()
+        for k in range(len(node_pairs)):
+            corr = list(zip(h1[bounds[k]:bounds[k + 1]], h2[bounds[k]:bounds[k + 1]]))
+            for s1, s2 in corr:
+                for key, value in b_regions:
+                    if s1 in value and s1 not in in_periodic:
+                        periodic_sides_dict.setdefault(key[:-2], []).append(s1)
+                        periodic_list.append(s1)
+                        in_periodic.add(s1)
+                        to_discard.append(s2)
+                    if s2 in value and s2 not in in_periodic:
+                        periodic_sides_dict.setdefault(key[:-2], []).append(s2)
+                        periodic_list.append(s2)
+                        in_periodic.add(s2)
+                        to_discard.append(s1)
         for key in periodic_sides_dict:
             side_physical_regions.pop(key + "_a", None)
             side_physical_regions.pop(key + "_b", None)
-        for s1, s2 in zip(to_discard, periodic_list):
-            eb = side_elem_map[s2][0]
-            ea = side_elem_map[s1][0]
-            side_elem_map[s2][1] = ea
-            row = esm[ea]
-            row[np.where(row == s1)[0][0]] = s2
-            dists[s2] = elem_centroids[ea] + side_centroids[s2] - side_centroids[s1] - elem_centroids[eb]
+        # each kept side s2 couples to the element ea behind its discarded image s1, which takes s2 in
+        # place of s1 in its side list (the pairs touch distinct s2 and distinct (ea, s1))
+        if periodic_list:
+            s1a = np.asarray(to_discard, dtype=np.int64)
+            s2a = np.asarray(periodic_list, dtype=np.int64)
+            ea = side_elem_map[s1a, 0]
+            eb = side_elem_map[s2a, 0]
+            side_elem_map[s2a, 1] = ea
+            hit = esm[ea] == s1a[:, None]
+            if not hit.any(axis=1).all() or len(np.unique(ea * n_sides + s1a)) != len(s1a):
+                raise ValueError("periodic sides: a discarded image is not (or twice) a side of its element")
+            esm[ea, np.argmax(hit, axis=1)] = s2a
+            dists[s2a] = elem_centroids[ea] + side_centroids[s2a] - side_centroids[s1a] - elem_centroids[eb]
 
     boundary_sides = []
     for value in side_physical_regions.values():
