@@ -79,3 +79,18 @@ def test_row_key_and_fallback_paths_agree(monkeypatch, three):
                 np.testing.assert_array_equal(np.asarray(x[k]), np.asarray(y[k]), err_msg=f"{fld}[{k}]")
         else:
             np.testing.assert_array_equal(np.asarray(x), np.asarray(y), err_msg=fld)
+
+
+def test_3d_mesh_matches_reference_fields(case):
+    """The tetrahedral cell of cube1k5 against the reference get_mesh on the same cell
+    (tests/golden/make_golden_mesh3d.py)."""
+    geo, _, _, _, _ = case("cube1k5")
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "mesh3d_cube1k5.npz"))
+    for fld in ["side_elem_map", "normal_areas", "elem_volumes", "side_areas", "internal", "interp_weights",
+                "gradient_weights", "dists", "elem_centroids", "side_centroids", "second_order_correction"]:
+        a, b = np.asarray(getattr(geo, fld)), d[fld]
+        assert a.shape == b.shape, fld
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12, err_msg=fld)
+    for k in ("Periodic_x", "Periodic_y", "Periodic_z"):
+        np.testing.assert_array_equal(geo.periodic_sides[k], d["periodic_" + k])
+    np.testing.assert_array_equal(geo.side_physical_regions["Boundary"], d["region_Boundary"])
