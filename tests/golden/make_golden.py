@@ -103,7 +103,7 @@ def main():
     import tempfile
     R = ref_loader.load()
     only = sys.argv[1:]
-    with tempfile.TemporaryDirectory() as tmp:
+    with tempfile.TemporaryDirectory(dir=HERE) as tmp:   # scratch msh files beside the fixtures
         for c in CASES:
             if only and c[0] not in only:
                 continue
