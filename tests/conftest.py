@@ -11,7 +11,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
 def pytest_configure(config):
-    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
+    # temporary files of tests (tmp_path) stay inside the checkout unless a base directory is given
+    if not config.option.basetemp:
+        config.option.basetemp = os.path.join(ROOT, ".pytest_tmp")
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
     config.addinivalue_line("markers", "slow: longer CPU test")
 
 
