@@ -7,7 +7,7 @@
  *     Fourier(geometry, thermal_conductivity, boundary_conditions, ...)      openbte/fourier.py:15-185
  * A Python FFI for that path (ctypes / cffi) binds the functions below; the
  * package's ``openbte_gb300.BTE_RTA`` / ``Fourier`` wrappers are exactly that
- * binding.
+ * binding (openbte_gb300/_lib.py declares the prototypes).
  *
  * Conventions
  *   - every call returns an obte_status; obte_status_string() names it;
@@ -209,11 +209,32 @@ obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const double* u_in
  * address (once per device); make that first call before any stream capture.
  * All calls share the one array: calls whose GPU work overlaps (other threads,
  * other streams, other plans) race on it and must be serialised by the caller.
- * Each call synchronises the plan's stream before it returns.
+ * Each call synchronises the plan's stream before it returns.  The device address
+ * looked up on the first call is kept for the life of the process: resetting
+ * the device (cudaDeviceReset) after that first call is not supported.
  * No counterpart in the reference (it has no device code).
  */
 obte_status obte_bte_sweep_static(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
                                   int32_t with_source);
+/*
+ * One sweep like obte_bte_sweep that also stores every per-ordinate temperature: the solutions
+ * T_mq = A_mq^-1 B_mq of openbte/bte.py:217-218, which the reference keeps inside its worker processes
+ * and returns only reduced (ΔT, J, K, S).  For checks of single ordinates against exact solves, or for
+ * callers that want the phonon temperatures themselves.
+ *   T  device [n_dir, n_elems, n_mfp]: float for OBTE_FP32 / OBTE_FP32_REFINE, double for OBTE_FP64
+ * u_in, u_out and with_source as for obte_bte_sweep.
+ */
+obte_status obte_bte_sweep_fields(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
+                                  int32_t with_source, void* T);
+/*
+ * Test hook of the bounded device waits (no counterpart in the reference, whose Barrier.wait has no
+ * timeout, openbte/objects.py:88-101): the plan's later sweeps do not issue the bulk copy of level
+ * unit skip_unit of any direction (-1: none) and stop waiting for a unit's copy after wait_limit polls
+ * (0: the default cap).  A sweep that reaches the skipped unit gives up, lets the copies it has in
+ * flight land and returns OBTE_ERR_DEVICE_TIMEOUT; nothing faults or hangs, and the plan sweeps
+ * normally again after (-1, 0).
+ */
+obte_status obte_bte_plan_test_wait_timeout(obte_plan plan, int32_t skip_unit, int32_t wait_limit);
 
 /*
  * Inverse design: dkappa_eff/dt_s for every side of a plan created with side_transmission

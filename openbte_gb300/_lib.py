@@ -16,8 +16,11 @@ LIB_PATH = os.path.join(HERE, "libobte_gb300.so")
 OBTE_OK = 0
 STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "OOM", 3: "ADMISSION_REJECTED", 4: "NOT_CONVERGED",
                 5: "CUDA_ERROR", 6: "CYCLE", 7: "UNSUPPORTED", 8: "DEVICE_TIMEOUT"}
-OBTE_ERR_NOT_CONVERGED = 4
+OBTE_ERR_BAD_ARG = 1
 OBTE_ERR_ADMISSION = 3
+OBTE_ERR_NOT_CONVERGED = 4
+OBTE_ERR_UNSUPPORTED = 7
+OBTE_ERR_DEVICE_TIMEOUT = 8
 
 PRECISION = {"fp64": 0, "fp32_refine": 1, "fp32": 2}
 CONTACT_NONE, CONTACT_PERIODIC, CONTACT_MIXED, CONTACT_NANOWIRE = 0, 1, 2, 3
@@ -99,6 +102,8 @@ SIGNATURES = [
                                  C.c_void_p, C.POINTER(SolveInfo)]),
     ("obte_bte_sweep", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
     ("obte_bte_sweep_static", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
+    ("obte_bte_sweep_fields", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    ("obte_bte_plan_test_wait_timeout", C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     ("obte_bte_kappa_gradient", C.c_int, [C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p,
                                           C.POINTER(SolveInfo)]),
     ("obte_bte_state_layout", C.c_int, [C.c_void_p, p_i64, p_i64, p_i64]),

@@ -270,3 +270,38 @@ extern "C" obte_status obte_bte_schedule_coefficients(obte_plan plan, int32_t q,
   if (P) std::copy(s.P.begin() + base, s.P.begin() + base + s.n, P);
   return OBTE_OK;
 }
+
+extern "C" obte_status obte_bte_sweep_fields(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
+                                             int32_t with_source, void* T) {
+  if (!plan || !u_in || !u_out || !T) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  if (!plan->ctx) { set_error("host-only plan cannot sweep"); return OBTE_ERR_BAD_ARG; }
+  if (precision != OBTE_FP64 && precision != OBTE_FP32 && precision != OBTE_FP32_REFINE) {
+    set_error("bad precision"); return OBTE_ERR_BAD_ARG;
+  }
+  if (plan->xstore) { set_error("a gradient solve is using the per-ordinate store"); return OBTE_ERR_BAD_ARG; }
+  const Schedule& s = plan->sched;
+  const bool fp32 = precision != OBTE_FP64;
+  // the final-pass kernel also accumulates J, K and S; they go to plan-owned buffers and are discarded
+  if (!plan->fields_J.p) {
+    OBTE_TRY(plan->fields_J.alloc((size_t)s.n * s.ds * sizeof(double)));
+    OBTE_TRY(plan->fields_K.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+    OBTE_TRY(plan->fields_S.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+  }
+  if (fp32) plan->xstore = static_cast<float*>(T);
+  else plan->xstore64 = static_cast<double*>(T);
+  const obte_status st = launch_sweep(plan, fp32, u_in, u_out, with_source != 0, true, plan->fields_J.as<double>(),
+                                      plan->fields_K.as<double>(), plan->fields_S.as<double>());
+  plan->xstore = nullptr;
+  plan->xstore64 = nullptr;
+  OBTE_TRY(st);
+  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  return check_device_error(plan);
+}
+
+extern "C" obte_status obte_bte_plan_test_wait_timeout(obte_plan plan, int32_t skip_unit, int32_t wait_limit) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  if (skip_unit < -1 || wait_limit < 0) { set_error("skip_unit must be >= -1 and wait_limit >= 0"); return OBTE_ERR_BAD_ARG; }
+  plan->test_skip_unit = skip_unit;
+  plan->test_wait_limit = wait_limit;
+  return OBTE_OK;
+}

@@ -347,6 +347,12 @@ struct obte_plan_s {
   int64_t nu = 0;                   // state length
   bool has_solution = false;        // work->u holds the last converged state
   float* xstore = nullptr;          // set during a gradient solve: final-pass per-ordinate temperatures
+  double* xstore64 = nullptr;       // set during obte_bte_sweep_fields in FP64: the same in FP64
+  obte::DevBuf fields_J, fields_K, fields_S;   // final-pass outputs of obte_bte_sweep_fields (discarded)
+  // bounded-wait test (obte_bte_plan_test_wait_timeout): level unit whose bulk copy the sweeps skip
+  // (-1: none) and the poll cap of their copy waits (0: the default)
+  int test_skip_unit = -1;
+  int test_wait_limit = 0;
   std::unique_ptr<obte::TimDevice> tim;   // transmission-interface gradient tables and scratch
   // non-final sweeps run only these CTAs (direction * n_chunks + chunk) while set (preconditioner setup)
   const int32_t* sweep_cta_map = nullptr;

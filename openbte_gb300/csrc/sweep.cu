@@ -393,8 +393,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-  for (int i = 0; i < (1 << 22); ++i)
+// Default cap on the polls of one mbarrier wait (each poll may suspend the thread for a while before it
+// returns), far above any copy's latency; a wait that reaches it gives up and reports a timeout.
+constexpr int kWaitPolls = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int limit = kWaitPolls) {
+  for (int i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -463,12 +466,17 @@ struct SweepParams {
   double* __restrict__ S_out;
   int* __restrict__ err;
   float* __restrict__ Xs;   // final pass only: per-ordinate temperatures [n_dir][n][n_mfp], or null
+  double* __restrict__ Xd;  // the same in FP64 (FP64 sweeps of obte_bte_sweep_fields), or null
   const int32_t* __restrict__ cta_map;   // CTA -> direction * n_chunks + chunk (a subset), or null: all
   // batched subset sweeps (batch_stride > 0): CTA b runs entry b % n_cta_batch of cta_map on the state
   // vectors u_in / u_out + (b / n_cta_batch) batch_stride.  The batch shares one set of staged values
   // (computed from the first state), so its states must agree on DeltaT and T_B.
   int n_cta_batch;
   int64_t batch_stride;
+  // bounded-wait test (obte_bte_plan_test_wait_timeout): level unit whose bulk copy is not issued (-1: none)
+  // and the poll cap of the wait for a unit's copy (kWaitPolls normally)
+  int skip_unit;
+  int wait_limit;
 };
 
 template <typename Real>
@@ -673,6 +681,7 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
   // TMA of unit u into buffer bi: records [a, e), values [a, e) (16-B aligned window), the
   // wall weights of the unit's wall entries and the prefetch list of unit u + 1
   auto issue = [&](int u, int bi) {
+    if (u == p.skip_unit) return;   // test of the bounded wait: this unit's copy never arrives
     const int a = lev[u], e = lev[u + 1];
     const unsigned rbytes = (unsigned)(e - a) * RW * 4u;
     const int64_t vb0 = (val_q0 + (int64_t)a * VB) & ~(int64_t)15;
@@ -706,7 +715,7 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
     const int prow_next = prow0 + ((u + 1) & 1) * p.emax;
     // buffer (u + nbuf - 1) mod nbuf was last read during unit u - 1, finished at the barrier below
     if (tid == 0 && u + nbuf - 1 < nlev) issue(u + nbuf - 1, bi == 0 ? nbuf - 1 : bi - 1);
-    const bool ready = mbar_wait_bounded(&bars[bi], phase);
+    const bool ready = mbar_wait_bounded(&bars[bi], phase, p.wait_limit);
     if (!ready) {
       s_abort[cur] = 1;
       atomicOr(p.err, 1);
@@ -805,6 +814,11 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
 #pragma unroll
           for (int j = 0; j < KV; ++j)
             if (mo + j < mc) p.Xs[((int64_t)q * p.n + c) * p.n_mfp + m0 + mo + j] = (float)T[j];
+        }
+        if (FINAL && p.Xd != nullptr) {
+#pragma unroll
+          for (int j = 0; j < KV; ++j)
+            if (mo + j < mc) p.Xd[((int64_t)q * p.n + c) * p.n_mfp + m0 + mo + j] = (double)T[j];
         }
         dacc = group_sum<G>(dacc, gmask);
         if (lane == 0) atomicAdd(&dT_out[c], (double)dacc);
@@ -1197,6 +1211,9 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S_out = S;
   p.err = plan->err.as<int>();
   p.Xs = FINAL ? plan->xstore : nullptr;
+  p.Xd = FINAL ? plan->xstore64 : nullptr;
+  p.skip_unit = plan->test_skip_unit;
+  p.wait_limit = plan->test_wait_limit > 0 ? plan->test_wait_limit : kWaitPolls;
   const bool subset = !FINAL && plan->sweep_cta_map != nullptr;
   static const bool index_order = std::getenv("OBTE_SWEEP_NO_LPT") != nullptr;   // plain index order
   p.cta_map = subset ? plan->sweep_cta_map : (index_order ? nullptr : d.lpt.as<int32_t>());
@@ -1332,9 +1349,14 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.u_in = u_in; p.u_out = u_out; p.Jraw = nullptr; p.K = nullptr; p.S_out = nullptr;
   p.err = err;
   p.Xs = nullptr;
-  p.cta_map = nullptr;
+  p.Xd = nullptr;
+  // the launch order of obte_bte_sweep: longest chains first (FP32 tables), unless OBTE_SWEEP_NO_LPT is set
+  static const bool index_order = std::getenv("OBTE_SWEEP_NO_LPT") != nullptr;
+  p.cta_map = index_order ? nullptr : d.lpt.as<int32_t>();
   p.n_cta_batch = 0;
   p.batch_stride = 0;
+  p.skip_unit = -1;
+  p.wait_limit = kWaitPolls;
   kern<<<s.n_dir * d.n_chunks, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());

@@ -213,6 +213,48 @@ def bte_rta(geo, mat, bcs, fourier=None, effective_thermal_conductivity=None, he
     return float(np.sum(K)), DeltaT, J, K, S, n_iter
 
 
+def cut_ordinate_solve(solver, faces, q, m, B, x_src, src, order):
+    """One transport solve with the periodic inflow given instead of solved for.
+
+    The reference's operator A_mq = I + mfp_m (diag D_q + offdiag Gm_q) (openbte/bte.py:181-185) couples
+    the two sides of every kept periodic side inside one solve.  Here its entries on the directed faces
+    that cross the periodic boundary (``faces`` from ``sweep_order.directed_faces``, flag ``cut``) move
+    to the right-hand side, where they multiply given inflow values: ``x_src[k]`` is the temperature of
+    ordinate (m, q) at periodic source element ``src[k]`` (sorted), read across every cut inflow face
+    from that element.  With x_src equal to the exact periodic solution at those elements this returns
+    the reference's exact solve; for any x_src it is the transport solve a sweep evaluates.
+
+    The cut operator has an acyclic upwind graph, so in a topological ``order`` it is lower triangular;
+    it is solved by sparse triangular substitution after the order is checked to make it so (an order
+    that is not topological raises).
+    """
+    row, nb, _, cut = faces
+    ops = solver.ops
+    n = solver.n
+    mfp = solver.mfps[m]
+    gm = np.asarray(ops["Gm"][q])
+    keep = ~cut
+    d = np.concatenate((mfp * gm[keep], mfp * ops["D"][q] + 1.0))
+    im = np.concatenate((ops["i_mat"][keep], np.arange(n)))
+    jm = np.concatenate((ops["j_mat"][keep], np.arange(n)))
+    A = sp.csr_matrix((d, (im, jm)), shape=(n, n), dtype=np.float64)
+    A.eliminate_zeros()   # outflow faces carry Gm = 0
+    rhs = np.array(B, dtype=np.float64, copy=True)
+    cf = np.nonzero(cut & (gm < 0))[0]
+    if len(cf):
+        pos = np.searchsorted(src, nb[cf])
+        if np.any(pos >= len(src)) or np.any(src[np.minimum(pos, len(src) - 1)] != nb[cf]):
+            raise ValueError("a cut inflow face reads an element outside the periodic source list")
+        np.add.at(rhs, row[cf], -mfp * gm[cf] * np.asarray(x_src)[pos])
+    order = np.asarray(order)
+    Ap = A[order][:, order].tocsr()
+    if sp.triu(Ap, k=1).nnz:
+        raise ValueError("the order does not make the cut operator lower triangular")
+    T = np.empty(n)
+    T[order] = spla.spsolve_triangular(Ap, rhs[order], lower=True)
+    return T
+
+
 def solve_ordinate(geo, mat, bcs, q, m, B):
     """One exact transport solve A_mq T = B (the reference's per-ordinate splu)."""
     ops = setup_operators(geo, mat, bcs)

@@ -1,8 +1,14 @@
 """Import the unmodified OpenBTE reference solver in a container without its GUI/IO deps.
 
-Test infrastructure only: used to generate the golden fixtures in this
-directory and by CPU tests that are skipped when the reference checkout is
-absent. It never runs on the product path.
+Test and measurement infrastructure only: it generates the golden fixtures
+under ``tests/golden``, backs CPU tests that are skipped when the reference is
+absent, and runs the reference's own solver for ``bench.py --impl reference``.
+It never runs on the product path.
+
+Where the reference lives: ``OBTE_REFERENCE`` (a directory holding
+``openbte/bte.py``), else ``baseline/_ref`` in this checkout, which is where
+``pip install --no-deps --target baseline/_ref <reference checkout>`` puts the
+unmodified package.
 
 The reference (romanodev/OpenBTE 3.0.16) imports shapely, sqlitedict,
 pickle5, plotly, jax, icosphere, nptyping, matplotlib and cachetools at module
@@ -32,11 +38,18 @@ import types
 
 import numpy as np
 
-REF_ROOT = os.environ.get("OBTE_REFERENCE", "/root/reference")
+_CHECKOUT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_ROOT = os.environ.get("OBTE_REFERENCE") or os.path.join(_CHECKOUT, "baseline", "_ref")
 
 
 def available() -> bool:
     return os.path.isfile(os.path.join(REF_ROOT, "openbte", "bte.py"))
+
+
+def available_inverse() -> bool:
+    """The inverse-design modules are present (a pip install of the reference leaves them out: the
+    ``openbte/inverse`` folder has no ``__init__.py``, so only a source checkout has them)."""
+    return os.path.isfile(os.path.join(REF_ROOT, "openbte", "inverse", "matinverse.py"))
 
 
 def _stub(name, **attrs):

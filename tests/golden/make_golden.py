@@ -1,7 +1,7 @@
 """Generate golden fixtures by running the unmodified OpenBTE reference.
 
 Run in a checkout where the reference is available (``OBTE_REFERENCE``, by
-default the read-only reference tree); the fixtures are committed so the
+default the copy installed under baseline/_ref); the fixtures are committed so the
 tests never need the reference at run time:
 
     python tests/golden/make_golden.py
@@ -25,6 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle"))   # ref_loader
 
 import ref_loader  # noqa: E402
 from openbte_gb300.geometry import porous_cell_2d, porous_cube_3d, write_msh2  # noqa: E402

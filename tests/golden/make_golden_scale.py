@@ -1,0 +1,123 @@
+"""Golden fixtures on the benchmark meshes: the unmodified OpenBTE reference at full mesh size with a
+reduced ordinate set.
+
+The benchmark workloads (60,000-triangle square-pore cell with 100 MFPs x 96 directions; 100,000-
+tetrahedron spherical-pore cube with 30 x 16 x 32) are far beyond what the reference can solve in
+full: its per-ordinate SuperLU factorisation (openbte/bte.py:181-185) costs 0.5 s per ordinate on the
+2D mesh and ~290 s on the 3D one, on one core.  These cases keep the meshes and cut the ordinates, so the
+reference's own solver (``BTE_RTA``, openbte/bte.py:19-271, with its forking process pool,
+openbte/utils.py:186-219) runs them to bte_rtol=1e-12:
+
+* ``c1scale``: the 60k-triangle mesh of the 2D benchmark (porous_cell_2d(60000, 0.25, 'square', seed=1)),
+  8 MFPs x 16 directions, Fourier first guess (openbte/fourier.py) then BTE;
+* ``c2scale``: the 110k-tetrahedron mesh of the 3D benchmark (porous_cube_3d(100000, 0.10, seed=1)),
+  2 MFPs (100 nm, 10 um) x 2 polar x 4 azimuthal directions, BTE from DeltaT = 0 (the reference's 3D
+  Fourier factorisation is skipped; the GPU test starts from zeros as well).
+
+Run where the reference is importable (``oracle/ref_loader.py``); writes ``tests/golden/<case>.npz`` with
+the cell (nodes, elements, boundary segments, periodic pairs), the material and the reference outputs:
+
+    python tests/golden/make_golden_scale.py [c1scale] [c2scale] [-np N]
+"""
+from __future__ import annotations
+
+import contextlib
+import io
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle"))   # ref_loader
+
+import ref_loader  # noqa: E402
+from openbte_gb300.geometry import porous_cell_2d, porous_cube_3d, write_msh2  # noqa: E402
+from openbte_gb300.material import synthetic_isotropic_2d, synthetic_isotropic_3d  # noqa: E402
+
+CASES = {
+    # name: (dimension, n_elems target, porosity, pore, seed, material args, Fourier first guess)
+    "c1scale": (2, 60000, 0.25, "square", 1, dict(n_mfp=8, n_phi=16), True),
+    "c2scale": (3, 100000, 0.10, "sphere", 1, dict(n_mfp=2, n_theta=2, n_phi=4, mfp_min=100.0, mfp_max=1.0e4),
+                False),
+}
+
+
+def run_case(R, name, n_process, tmpdir):
+    dim, n_target, porosity, pore, seed, margs, with_fourier = CASES[name]
+    t0 = time.time()
+    if dim == 3:
+        cell = porous_cube_3d(n_target, porosity, seed=seed)
+        periodic = {"Periodic_x": 1, "Periodic_y": 0, "Periodic_z": 0}
+        mat = synthetic_isotropic_3d(**margs)
+        normalization = -1.0 / cell.size
+    else:
+        cell = porous_cell_2d(n_target, porosity, pore, seed=seed)
+        periodic = {"Periodic_x": 1, "Periodic_y": 0}
+        mat = synthetic_isotropic_2d(**margs)
+        normalization = -1.0
+    path = write_msh2(cell, os.path.join(tmpdir, name))
+    geo = R.mesh.get_mesh(path[:-4])
+    t_mesh = time.time() - t0
+    rmat = R.objects.Material(*mat)
+    bcs = R.objects.BoundaryConditions(periodic=periodic, diffuse="Boundary")
+    ek = R.objects.EffectiveThermalConductivity(normalization=normalization, contact="Periodic_x")
+    d = {}
+    f = None
+    t_fourier = 0.0
+    if with_fourier:
+        out = io.StringIO()
+        t1 = time.time()
+        with contextlib.redirect_stdout(out):
+            f = R.fourier.Fourier(geo, rmat.thermal_conductivity, bcs, effective_thermal_conductivity=ek)
+        t_fourier = time.time() - t1
+        printed = [l for l in out.getvalue().splitlines() if l.startswith("Kappa (Fourier)")]
+        d.update(fourier_T=f.variables["Temperature_Fourier"]["data"], fourier_J=f.variables["Flux_Fourier"]["data"],
+                 fourier_kappa_printed=float(printed[-1].split(":")[1].split(",")[0]))
+    argv = sys.argv
+    sys.argv = [argv[0], "-np", str(n_process)]      # the reference's runner reads its worker count here
+    try:
+        t2 = time.time()
+        with contextlib.redirect_stdout(io.StringIO()):
+            b = R.bte.BTE_RTA(geo, rmat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-12,
+                              bte_max_iter=3000)
+        t_bte = time.time() - t2
+    finally:
+        sys.argv = argv
+    d.update(
+        nodes=cell.nodes, elems=cell.elems.astype(np.int32), size=cell.size, porosity=cell.porosity, pore=cell.pore,
+        seed=cell.seed, periodic_x=cell.periodic["x"], periodic_y=cell.periodic["y"],
+        **({"periodic_z": cell.periodic["z"]} if "z" in cell.periodic else {}),
+        mat_args=repr(margs), normalization=normalization, jumps=repr(periodic),
+        mfps=mat.mfps, vmfp=mat.vmfp, sigma=mat.sigma, t_coeff=mat.t_coeff, kappa_bulk=mat.thermal_conductivity,
+        bte_kappa=b.kappa_eff, bte_T=b.variables["Temperature_BTE"]["data"], bte_J=b.variables["Flux_BTE"]["data"],
+        bte_S=b.aux["suppression"], n_process=n_process, t_mesh=t_mesh, t_fourier=t_fourier, t_bte=t_bte,
+        fourier_guess=with_fourier,
+    )
+    for region, segs in cell.segments.items():
+        d["seg_" + region] = segs
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print(f"{name}: n={geo.n_elems} ordinates={mat.t_coeff.size} kappa_bte={b.kappa_eff:.12g} "
+          f"mesh {t_mesh:.1f}s fourier {t_fourier:.1f}s bte {t_bte:.1f}s on {n_process} processes", flush=True)
+
+
+def main():
+    args = sys.argv[1:]
+    n_process = os.cpu_count() or 1
+    if "-np" in args:
+        i = args.index("-np")
+        n_process = int(args[i + 1])
+        del args[i:i + 2]
+    names = args or list(CASES)
+    R = ref_loader.load(in_process=False)
+    with tempfile.TemporaryDirectory(dir=HERE) as tmp:   # scratch msh files beside the fixtures
+        for name in names:
+            run_case(R, name, n_process, tmp)
+
+
+if __name__ == "__main__":
+    main()

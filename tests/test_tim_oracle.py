@@ -47,8 +47,8 @@ def test_reference_inverse_golden_regenerates():
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
     import ref_loader
-    if not ref_loader.available():
-        pytest.skip("reference checkout absent")
+    if not ref_loader.available_inverse():
+        pytest.skip("reference inverse-design modules absent (a source checkout is needed: OBTE_REFERENCE)")
     import make_golden_inverse as M
     d = np.load(GOLD)
     name, n, kn, n_phi, seed = M.CASES[0]
