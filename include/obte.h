@@ -168,6 +168,14 @@ obte_status obte_bte_plan_set_transmission(obte_plan plan, const double* side_tr
  * separate streams.  One plan must not be used by two threads at the same time.
  */
 obte_status obte_bte_plan_set_stream(obte_plan plan, void* stream);
+/*
+ * Do a solve's set-up ahead of it: pack and upload the device tables of the sweep precisions that
+ * `precision` uses (OBTE_FP32_REFINE: FP32 and FP64) and allocate the solve scratch for GMRES
+ * restart length `restart` (<= 0: 30).  obte_bte_solve does the same on first use; a serving loop
+ * calls this on its host builder threads so that the GPU slot that later runs the solve only solves.
+ * No counterpart in the reference, which builds its operators inside BTE_RTA (openbte/bte.py:47-185).
+ */
+obte_status obte_bte_plan_prepare(obte_plan plan, int32_t precision, int32_t restart);
 /* Device bytes held by the plan (tables) and by one solve's scratch. */
 obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision, int32_t restart,
                                     int64_t* plan_bytes, int64_t* solve_bytes);

@@ -98,6 +98,7 @@ SIGNATURES = [
     ("obte_bte_plan_set_transmission", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
     ("obte_bte_plan_set_stream", C.c_int, [C.c_void_p, C.c_void_p]),
     ("obte_bte_plan_footprint", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, p_i64, p_i64]),
+    ("obte_bte_plan_prepare", C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     ("obte_bte_solve", C.c_int, [C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.POINTER(SolveInfo)]),
     ("obte_bte_sweep", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),

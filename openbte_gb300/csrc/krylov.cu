@@ -638,6 +638,8 @@ struct Solver {
       return gmres32(rhs, x, tol_rel, tol_abs, res_out, ok);
     const int64_t n = wk.nu;
     const int m = wk.restart;
+    // the FP64 basis is allocated on first use: FP32-refine solves at the usual tolerances never need it
+    if (!wk.V.p) OBTE_TRY(wk.V.alloc((size_t)n * sizeof(double) * (m + 1)));
     double* V = wk.V.as<double>();
     double* w = wk.w.as<double>();
     double* r = wk.r.as<double>();
@@ -781,7 +783,6 @@ static obte_status alloc_work(obte_plan plan, Work& wk, int restart) {
   OBTE_TRY(wk.w.alloc(vb));
   OBTE_TRY(wk.tmp.alloc(vb));
   OBTE_TRY(wk.delta.alloc(vb));
-  OBTE_TRY(wk.V.alloc(vb * (restart + 1)));
   OBTE_TRY(wk.partial.alloc((size_t)wk.nb * (restart + 1) * sizeof(double)));
   OBTE_TRY(wk.hdev.alloc((size_t)(restart + 2) * sizeof(double)));
   OBTE_TRY(wk.sdev.alloc(8 * sizeof(double)));
@@ -812,6 +813,39 @@ extern "C" obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const d
                         nullptr));
   OBTE_CUDA(cudaStreamSynchronize(plan->stream));
   return check_device_error(plan);
+}
+
+extern "C" obte_status obte_bte_plan_prepare(obte_plan plan, int32_t precision, int32_t restart) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  if (!plan->ctx) { set_error("host-only plan cannot be prepared"); return OBTE_ERR_BAD_ARG; }
+  if (precision != OBTE_FP64 && precision != OBTE_FP32 && precision != OBTE_FP32_REFINE) {
+    set_error("bad precision"); return OBTE_ERR_BAD_ARG;
+  }
+  const Schedule& s = plan->sched;
+  restart = restart > 0 ? std::min(restart, 200) : 30;
+  // tables of the sweep precisions the solve will use (FP32_REFINE: FP32 sweeps and one FP64 pass)
+  if (precision != OBTE_FP64) OBTE_TRY(ensure_tables(plan, true));
+  if (precision != OBTE_FP32) OBTE_TRY(ensure_tables(plan, false));
+  if (!plan->work || plan->work->restart != restart || plan->work->nu != plan->nu) {
+    plan->work.reset(new Work());
+    plan->has_solution = false;
+    obte_status ast = alloc_work(plan, *plan->work, restart);
+    if (ast != OBTE_OK) { plan->work.reset(); return ast; }
+  }
+  Work& wk = *plan->work;
+  if (precision != OBTE_FP64 && !wk.V32.p) {
+    const int64_t ld = (wk.nu + 3) & ~(int64_t)3;
+    OBTE_TRY(wk.V32.alloc((size_t)ld * (restart + 1) * sizeof(float)));
+    OBTE_TRY(wk.w32.alloc((size_t)ld * sizeof(float)));
+  }
+  if (precision == OBTE_FP32_REFINE && !wk.rc.p) {
+    OBTE_TRY(wk.rc.alloc((size_t)wk.nu * sizeof(double)));
+    OBTE_TRY(wk.Jraw2.alloc((size_t)s.n * s.ds * sizeof(double)));
+    OBTE_TRY(wk.Kraw2.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+    OBTE_TRY(wk.Sraw2.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+  }
+  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  return OBTE_OK;
 }
 
 extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opts, const double* dT0, double* dT,

@@ -30,7 +30,7 @@
 // openbte/bte.py:222-243 are register accumulations over the MFP loop followed
 // by one FP64 atomic per element (DeltaT', T_B', J) or per MFP (K, S).
 // Every mbarrier wait is bounded; on timeout the CTA raises the device error
-// word, stops using the buffers, waits (bounded) for its copy in flight and
+// word, stops using the buffers, waits (bounded) for its copies in flight and
 // leaves at the next block-wide barrier.
 #include <cuda_runtime.h>
 
@@ -502,7 +502,7 @@ __device__ __forceinline__ double quot(double num, double den) {
 }
 
 // Shared memory layout (bytes):
-//   [0,64) mbarriers  [64,72) abort flags
+//   [0,64) mbarriers  [64,128) unused
 //   [128, ...) nbuf x records | nbuf x values | nbuf x wall weights | nbuf x prefetch lists | sig | K S | ring
 // nbuf = TMA pipeline depth: unit u + nbuf - 1 is issued while unit u runs (at most kMaxBuf mbarriers)
 static constexpr int kMaxBuf = 8;
@@ -589,6 +589,12 @@ __device__ __forceinline__ T group_sum(T v, unsigned mask) {
 template <typename Real, int G, int KV>
 struct SweepMinBlocks { static constexpr int v = (sizeof(Real) == 4 && G == 1 && KV == 8) ? 5 : 1; };
 
+// The thread that issues the bulk copies: lane 0 of the last warp.  Its elements are the last of a unit,
+// which most units do not have (median 88 of 128 elements on the 60k-triangle cell), so the issue work stays
+// off the warps that every unit keeps busy.
+template <int G>
+struct Issuer { static constexpr int tid = kUnit * G - 32; };
+
 template <typename Real, int NF, int G, int KV, bool FINAL>
 __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte_sweep_kernel(const SweepParams<Real> p) {
   constexpr int RW = Rec<Real, NF>::W;           // record words
@@ -599,7 +605,6 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
   const int nbuf = p.nbuf;
   const SmemLayout<Real> L(NF, MC, rows, p.unit_wo, p.pf_pad, p.unit_sx, nbuf);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
-  int* s_abort = reinterpret_cast<int*>(smem + 64);
   Real* s_k = reinterpret_cast<Real*>(smem + L.kacc);
   Real* s_s = reinterpret_cast<Real*>(smem + L.sacc);
   Real* ring = reinterpret_cast<Real*>(smem + L.ring);    // [rows][MC]
@@ -672,8 +677,6 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
   }
   if (tid == 0) {
     for (int i = 0; i < nbuf; ++i) mbar_init(&bars[i], 1);
-    s_abort[0] = 0;
-    s_abort[1] = 0;
     fence_mbar_init();
   }
   __syncthreads();
@@ -702,27 +705,37 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
     if (pbytes) tma_load_1d(smem + L.pfl + bi * L.pf_stride, p.pf + f0, pbytes, bar);
     if (sbytes) tma_load_1d(smem + L.sxo + bi * L.sx_stride, p.sx + (int64_t)x0 * 4, sbytes, bar);
   };
-  if (tid == 0)
+  constexpr int kIssuer = Issuer<G>::tid;
+  if (tid == kIssuer)
     for (int u = 0; u < nbuf - 1 && u < nlev; ++u) issue(u, u);
 
+  // per-unit metadata, loaded one unit ahead so that its latency stays off the unit's critical path
+  int a = nlev > 0 ? lev[0] : 0, e = nlev > 0 ? lev[1] : 0;
+  int wu = kwo[0];
+  int kpf1 = nlev > 1 ? kpf[1] : 0, kpf2 = nlev > 1 ? kpf[2] : 0;
+  // the value window of a unit starts (q n + a) pairs into the array; FP32 pairs are 8 bytes, so the
+  // 16-byte aligned window starts one pair early when q n + a is odd (FP64 pairs are 16 bytes: never)
+  const int qn_odd = (int)(((int64_t)q * p.n) & 1);
   int bi = 0;            // buffer of unit u (u mod nbuf)
   unsigned phase = 0;    // parity of its mbarrier phase ((u / nbuf) & 1)
   for (int u = 0; u < nlev; ++u) {
-    const int cur = u & 1;
-    const int a = lev[u], e = lev[u + 1];
-    const int wu = kwo[u];
-    const int npf = u + 1 < nlev ? kpf[u + 2] - kpf[u + 1] : 0;   // padded length of unit u+1's list
+    const int e_next = u + 2 <= nlev ? lev[u + 2] : 0;
+    const int wu_next = kwo[u + 1];
+    const int kpf3 = u + 3 <= nlev ? kpf[u + 3] : 0;
+    const int npf = u + 1 < nlev ? kpf2 - kpf1 : 0;   // padded length of unit u+1's list
     const int prow_next = prow0 + ((u + 1) & 1) * p.emax;
     // buffer (u + nbuf - 1) mod nbuf was last read during unit u - 1, finished at the barrier below
-    if (tid == 0 && u + nbuf - 1 < nlev) issue(u + nbuf - 1, bi == 0 ? nbuf - 1 : bi - 1);
+    if (tid == kIssuer && u + nbuf - 1 < nlev) issue(u + nbuf - 1, bi == 0 ? nbuf - 1 : bi - 1);
     const bool ready = mbar_wait_bounded(&bars[bi], phase, p.wait_limit);
+    // the periodic prefetch runs on the high thread indices (list entry i on element kUnit - 1 - i), which
+    // most units leave without an element
+    const int pf_i = kUnit - 1 - el;
     if (!ready) {
-      s_abort[cur] = 1;
       atomicOr(p.err, 1);
     } else {
       // cut inflow values of unit u+1: loads issued now, stored into bank (u+1)&1 after the MFP loop
       const int32_t* s_pf = reinterpret_cast<const int32_t*>(smem + L.pfl + bi * L.pf_stride);
-      const int pk = el < npf ? s_pf[el] : -1;
+      const int pk = pf_i < npf ? s_pf[pf_i] : -1;
       double xv[KV];
       if (pk >= 0) {
         const double* xs = X + (xq + pk) * p.n_mfp + m0 + mo;
@@ -738,7 +751,7 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
           const int4 x = r4[i];
           r[4 * i] = x.x; r[4 * i + 1] = x.y; r[4 * i + 2] = x.z; r[4 * i + 3] = x.w;
         }
-        const int voff = (int)(((val_q0 + (int64_t)a * VB) & 15) / VB);
+        const int voff = sizeof(Real) == 4 ? ((qn_odd + a) & 1) : 0;
         const Real* v = reinterpret_cast<const Real*>(smem + L.val + bi * L.val_stride) + 2 * (voff + el);
         const Real b = v[0], pw = v[1];
         const int c = r[0];
@@ -757,10 +770,10 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
         const Real c3 = NF > 3 ? word_real<Real>(r, RR::COEF + 3 * RR::CSTEP) : Real(0);
         const Real D = word_real<Real>(r, RR::D);
         Real v0[KV], v1[KV], v2[KV], v3[KV];
-        vload(ring + (size_t)s0 * MC + mo, v0);
-        vload(ring + (size_t)s1 * MC + mo, v1);
-        vload(ring + (size_t)s2 * MC + mo, v2);
-        if (NF > 3) vload(ring + (size_t)s3 * MC + mo, v3);
+        vload(ring + s0 * MC + mo, v0);
+        vload(ring + s1 * MC + mo, v1);
+        vload(ring + s2 * MC + mo, v2);
+        if (NF > 3) vload(ring + s3 * MC + mo, v3);
         Real T[KV];
         Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
         if constexpr (sizeof(Real) == 4 && KV % 2 == 0) {
@@ -809,7 +822,7 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
             }
           }
         }
-        vstore(ring + (size_t)so * MC + mo, T);
+        vstore(ring + so * MC + mo, T);
         if (FINAL && p.Xs != nullptr) {
 #pragma unroll
           for (int j = 0; j < KV; ++j)
@@ -880,25 +893,29 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
         Real xr[KV];
 #pragma unroll
         for (int j = 0; j < KV; ++j) xr[j] = (Real)xv[j];
-        vstore(ring + (size_t)(prow_next + el) * MC + mo, xr);
+        vstore(ring + (prow_next + pf_i) * MC + mo, xr);
       }
-      for (int i = el + kUnit; i < npf; i += kUnit) {   // units with more than kUnit cut inflow faces
+      for (int i = pf_i + kUnit; i < npf; i += kUnit) {   // units with more than kUnit cut inflow faces
         const int k = s_pf[i];
         if (k < 0) continue;
         const double* xs = X + (xq + k) * p.n_mfp + m0 + mo;
         for (int j = 0; j < KV; ++j) ring[(size_t)(prow_next + i) * MC + mo + j] = mo + j < mc ? (Real)xs[j] : Real(0);
       }
     }
-    __syncthreads();
-    // a flag raised during unit u lives in word u&1; unit u+1 writes the other word
-    if (s_abort[cur]) {
+    // block barrier that also tells every thread whether any wait of this unit gave up
+    if (__syncthreads_or(ready ? 0 : 1)) {
       // let the copies this CTA still has in flight land before leaving (bounded)
-      if (tid == 0)
+      if (tid == kIssuer)
         for (int w = u + 1; w < nlev && w < u + nbuf; ++w) mbar_wait_bounded(&bars[w % nbuf], (unsigned)(w / nbuf) & 1u);
       __syncthreads();
       return;
     }
     if (++bi == nbuf) { bi = 0; phase ^= 1u; }
+    a = e;
+    e = e_next;
+    wu = wu_next;
+    kpf1 = kpf2;
+    kpf2 = kpf3;
   }
   if (FINAL) {
     for (int j = tid; j < mc; j += blockDim.x) {

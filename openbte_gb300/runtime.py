@@ -217,6 +217,10 @@ class Plan:
             _lib.check(self.lib.obte_bte_plan_set_stream(self.handle, C.c_void_p(stream)), "set_stream")
             self.stream = stream
 
+    def prepare(self, precision="fp32_refine", restart=30):
+        """Upload the device tables `precision` uses and allocate the solver scratch ahead of a solve."""
+        _lib.check(self.lib.obte_bte_plan_prepare(self.handle, _lib.PRECISION[precision], int(restart)), "prepare")
+
     def footprint(self, precision="fp64", restart=30):
         pb, sb = C.c_int64(), C.c_int64()
         _lib.check(self.lib.obte_bte_plan_footprint(self.handle, _lib.PRECISION[precision], restart, C.byref(pb),

@@ -1,21 +1,26 @@
 """Continuous-batching kappa_eff server on one GPU.
 
-Requests (mesh, material, boundary conditions, contact) arrive over time; each
-becomes a plan (sweep schedule and tables, built on host threads while the GPU
-works on earlier requests) and then a solve. Up to ``slots`` solves run at
-once, each on its own CUDA stream, so their sweeps and Krylov work overlap on
-the device; a request is admitted when a slot is free and its HBM footprint
-(plan tables + solver scratch) fits the budget. Plans are cached by content:
-a repeated geometry keeps its mesh, sweep orders, tables and converged state
-resident and can warm-start from it.
+Requests (mesh, material, boundary conditions, contact) arrive over time and go through four stages:
 
-Admission is first-fit in arrival order: the oldest queued request that fits
-the free memory starts first; a request whose footprint alone exceeds the
-budget is rejected (``status='rejected'``) instead of waiting forever.
+1. build (host threads): the plan's sweep schedule in C++ and its device footprint (tables + solver
+   scratch); a repeated geometry finds its plan in the cache instead;
+2. admission: first-fit in arrival order against the HBM budget.  The budget covers every byte the
+   server holds on the device: plans that are prepared (running, waiting for a slot, or idle in the
+   cache) and reservations of admitted plans not yet prepared.  Idle cached plans are evicted, least
+   recently used first, when a request does not fit otherwise.  A request whose footprint alone exceeds
+   the budget is rejected (``status='rejected'``) instead of waiting forever;
+3. prepare (host threads): device tables packed and uploaded, solver scratch allocated
+   (``obte_bte_plan_prepare``), so that GPU time goes to solves only;
+4. solve: up to ``slots`` solves run at once, each on its own CUDA stream, so their sweeps and Krylov work
+   overlap on the device.  At most ``slots`` prepared requests wait for a slot (``ahead``).
 
-The scheduling logic talks to a backend with three calls (``build``,
-``solve``, ``release``); :class:`GPUBackend` is the real one, tests can plug a
-fake one to exercise admission and ordering without a GPU.
+Plans are cached by content: a repeated geometry keeps its mesh, sweep orders, tables and converged
+state resident and can warm-start from it; it also builds the periodic-inflow preconditioner on its
+second solve, with the preconditioner's memory added to the plan's footprint.
+
+The scheduling logic talks to a backend with the calls ``build``, ``solve`` and ``release`` (and
+optionally ``prepare``, ``resident_bytes``, ``is_resident``, ``evict_idle``); :class:`GPUBackend` is the
+real one, tests plug a fake one to exercise admission and ordering without a GPU.
 """
 from __future__ import annotations
 
@@ -68,8 +73,16 @@ class Result:
         return self.t_start - self.t_built
 
 
+# sweep-table sets a solve of each precision reads (FP32+refine: FP32 sweeps and one FP64 pass)
+_TABLES = {"fp64": {"fp64"}, "fp32": {"fp32"}, "fp32_refine": {"fp32", "fp64"}}
+
+
 class GPUBackend:
-    """Plans and solves on one CUDA device through the C ABI."""
+    """Plans and solves on one CUDA device through the C ABI.
+
+    Every plan the backend holds is in ``_cache`` (least recently used first): busy ones (a request is
+    between build and release) and idle ones kept for repeated geometries.  ``resident_bytes`` is the
+    device memory of the prepared ones, which the server's admission counts."""
 
     def __init__(self, device=0, restart=30, max_sweeps=2000, cache_plans=8):
         import torch
@@ -95,7 +108,7 @@ class GPUBackend:
         return int(free * fraction)
 
     def build(self, req: Request):
-        """-> (plan, footprint bytes, reused?)"""
+        """Host part of a plan (the C++ schedule) or the cached plan -> (plan, footprint bytes, reused?)"""
         from .runtime import HostProblem, Plan
         hp = HostProblem(req.geo, req.mat, req.bcs, req.ek)
         key = hp.key()
@@ -109,6 +122,8 @@ class GPUBackend:
         with self.torch.cuda.stream(st):
             pl = Plan(hp, self.device, stream=st.cuda_stream)
         pl.key = key
+        pl.tables = set()        # table sets uploaded
+        pl.resident = 0          # device bytes once prepared
         with self._lock:
             self._cache[key] = pl
             self._busy[key] += 1
@@ -118,6 +133,27 @@ class GPUBackend:
         a, b = pl.footprint(req.precision, self.restart)
         return int(a + b)
 
+    def extra_bytes(self, pl, req) -> int:
+        """Device bytes that preparing `pl` for `req` adds (0 for a plan already prepared for it)."""
+        if _TABLES[req.precision] <= pl.tables:
+            return 0
+        return max(0, self._footprint(pl, req) - pl.resident)
+
+    def prepare(self, pl, req: Request):
+        """Upload the plan's device tables and allocate its solver scratch (host threads, before a slot)."""
+        if _TABLES[req.precision] <= pl.tables:
+            return
+        st = self._stream()
+        pl.set_stream(st.cuda_stream)
+        pl.prepare(req.precision, self.restart)
+        with self._lock:
+            pl.tables |= _TABLES[req.precision]
+            pl.resident = max(pl.resident, self._footprint(pl, req))
+
+    def resident_bytes(self) -> int:
+        with self._lock:
+            return sum(pl.resident for pl in self._cache.values())
+
     def solve(self, pl, req: Request, slot: int) -> dict:
         from .bte import solve_plan
         torch = self.torch
@@ -125,8 +161,8 @@ class GPUBackend:
         pl.set_stream(st.cuda_stream)
         with torch.cuda.stream(st):
             dT0 = torch.zeros(pl.n, dtype=torch.float64, device=f"cuda:{self.device}")
-            # the periodic-inflow preconditioner stays off: its blocks and set-up buffers are not part of the
-            # footprint a request is admitted by (and a request's plan is usually solved once)
+            # the periodic-inflow preconditioner stays off: its setup costs about as many sweeps as a solve
+            # saves, and a served request's plan is usually solved once
             info, *_ = solve_plan(pl, dT0, precision=req.precision, rtol=req.rtol, max_sweeps=self.max_sweeps,
                                   restart=self.restart, warm_start=req.warm_start, precond=-1)
         st.synchronize()
@@ -134,40 +170,61 @@ class GPUBackend:
                 "n_sweeps_fp64": info.n_sweeps_fp64}
 
     def release(self, pl):
-        """Solve finished: the plan stays cached (resident) unless the cache is over its size."""
+        """A request is done with the plan: it stays cached (resident) unless the cache is over its size."""
+        victims = []
         with self._lock:
             self._busy[pl.key] -= 1
-            while len(self._cache) > self.cache_plans:
-                victim = next((k for k in self._cache if self._busy[k] <= 0), None)
+            while len(self._cache) - len(victims) > self.cache_plans:
+                victim = next((k for k in self._cache if self._busy[k] <= 0 and k not in victims), None)
                 if victim is None:
                     break
-                self._cache.pop(victim)
+                victims.append(victim)
+            dropped = [self._cache.pop(k) for k in victims]
+        del dropped       # plans are destroyed here, outside the lock
 
-    def evict_idle(self) -> int:
-        """Drop every idle cached plan; returns how many were dropped."""
+    def evict_idle(self, need: Optional[int] = None) -> int:
+        """Drop idle cached plans, least recently used first, until `need` bytes are freed (None: all of them);
+        returns the bytes freed."""
+        freed = 0
         with self._lock:
-            idle = [k for k in self._cache if self._busy[k] <= 0]
-            for k in idle:
-                self._cache.pop(k)
-        return len(idle)
+            dropped = []
+            for k in list(self._cache):
+                if need is not None and freed >= need:
+                    break
+                if self._busy[k] <= 0:
+                    pl = self._cache.pop(k)
+                    freed += pl.resident
+                    dropped.append(pl)
+        del dropped
+        return freed
 
 
 class Server:
-    """Continuous batching: a host pool builds plans, `slots` GPU workers solve concurrently."""
+    """Continuous batching: host threads build and prepare plans, `slots` GPU workers solve concurrently."""
 
     def __init__(self, backend=None, slots: int = 4, builders: int = 4, hbm_budget: Optional[int] = None,
-                 hbm_fraction: float = 0.7):
+                 hbm_fraction: float = 0.7, ahead: Optional[int] = None):
         self.backend = backend if backend is not None else GPUBackend()
         self.slots = slots
+        self.ahead = slots if ahead is None else ahead
         self.budget = int(hbm_budget) if hbm_budget is not None else self.backend.budget(hbm_fraction)
         self._builders = cf.ThreadPoolExecutor(max_workers=builders, thread_name_prefix="obte-build")
+        self._preparers = cf.ThreadPoolExecutor(max_workers=max(1, min(2, builders)), thread_name_prefix="obte-prep")
         self._cv = threading.Condition()
-        self._queue: "collections.deque" = collections.deque()   # built, waiting for admission
+        self._waiting: "collections.deque" = collections.deque()   # built, waiting for admission
+        self._ready: "collections.deque" = collections.deque()     # prepared, waiting for a slot
+        # device memory: with a backend that reports resident bytes, held = resident + reserved (admitted,
+        # not yet prepared); otherwise held = the footprints of the admitted requests
+        self._resident = getattr(self.backend, "resident_bytes", None)
+        self._reserved = 0
         self._used = 0
+        self._admitted = 0          # admitted and not finished
+        self._preparing = 0
         self._running = 0
         self._closed = False
         self.results = []
         self.max_concurrent = 0
+        self.max_held = 0
         self._workers = [threading.Thread(target=self._slot_loop, args=(i,), daemon=True, name=f"obte-slot{i}")
                          for i in range(slots)]
         for w in self._workers:
@@ -181,12 +238,49 @@ class Server:
         return fut
 
     def close(self):
+        # every submitted request is built (and queued) before the slots may see the server closed
+        self._builders.shutdown(wait=True)
         with self._cv:
             self._closed = True
             self._cv.notify_all()
-        self._builders.shutdown(wait=True)
         for w in self._workers:
             w.join()
+        self._preparers.shutdown(wait=True)
+
+    # -- memory accounting (call with self._cv held) --------------------------------------
+    def _held(self) -> int:
+        return (self._resident() + self._reserved) if self._resident else self._used
+
+    def _need(self, item) -> int:
+        req, res, _, plan = item
+        extra = getattr(self.backend, "extra_bytes", None)
+        return extra(plan, req) if extra is not None else res.footprint
+
+    def _admit_locked(self):
+        """Admit waiting requests (first fit in arrival order) while slots plus look-ahead and memory allow."""
+        while self._waiting and self._admitted < self.slots + self.ahead:
+            held = self._held()
+            pick = None
+            for i, item in enumerate(self._waiting):
+                need = self._need(item)
+                if held + need <= self.budget:
+                    pick = (i, item, need)
+                    break
+            if pick is None:
+                evict = getattr(self.backend, "evict_idle", None)
+                if evict is not None and evict(held + self._need(self._waiting[0]) - self.budget) > 0:
+                    continue
+                return
+            i, item, need = pick
+            del self._waiting[i]
+            self._admitted += 1
+            if self._resident:
+                self._reserved += need
+            else:
+                self._used += need
+            self.max_held = max(self.max_held, self._held())
+            self._preparing += 1
+            self._preparers.submit(self._prepare, item, need)
 
     # -- stages -------------------------------------------------------------------------
     def _build(self, req, res, fut):
@@ -207,26 +301,42 @@ class Server:
             self._finish(res, fut)
             return
         with self._cv:
-            self._queue.append((req, res, fut, plan))
+            self._waiting.append((req, res, fut, plan))
+            self._admit_locked()
             self._cv.notify_all()
 
+    def _prepare(self, item, need):
+        req, res, fut, plan = item
+        err = None
+        try:
+            prep = getattr(self.backend, "prepare", None)
+            if prep is not None:
+                prep(plan, req)
+        except Exception as e:  # noqa: BLE001
+            err = f"{type(e).__name__}: {e}"
+        with self._cv:
+            self._preparing -= 1
+            if self._resident:
+                self._reserved -= need       # now counted in the backend's resident bytes
+            if err is None:
+                self._ready.append(item)
+                self._cv.notify_all()
+                return
+        res.status, res.error, res.t_done = "error", err, time.perf_counter()
+        self._done(plan, res, fut, need)
+
     def _take(self):
-        """First queued request (arrival order) that fits the free memory; None when closing."""
+        """Next prepared request (arrival order of admission); None when closed and nothing is left."""
         with self._cv:
             while True:
-                for i, item in enumerate(self._queue):
-                    if self._used + item[1].footprint <= self.budget:
-                        del self._queue[i]
-                        self._used += item[1].footprint
-                        self._running += 1
-                        self.max_concurrent = max(self.max_concurrent, self._running)
-                        return item
-                if self._closed and not self._queue:
+                if self._ready:
+                    item = self._ready.popleft()
+                    self._running += 1
+                    self.max_concurrent = max(self.max_concurrent, self._running)
+                    return item
+                if self._closed and not self._waiting and not self._preparing and self._admitted == self._running:
+                    self._cv.notify_all()
                     return None
-                if self._queue and self._running == 0 and hasattr(self.backend, "evict_idle"):
-                    # nothing runs but the head does not fit: cached idle plans hold the memory
-                    if self.backend.evict_idle():
-                        continue
                 self._cv.wait(timeout=0.05)
 
     def _slot_loop(self, slot):
@@ -246,12 +356,20 @@ class Server:
             except Exception as e:  # noqa: BLE001
                 res.status, res.error = "error", f"{type(e).__name__}: {e}"
             res.t_done = time.perf_counter()
-            self.backend.release(plan)
             with self._cv:
-                self._used -= res.footprint
                 self._running -= 1
-                self._cv.notify_all()
-            self._finish(res, fut)
+            self._done(plan, res, fut, res.footprint)
+
+    def _done(self, plan, res, fut, need):
+        """The request leaves the server: release its plan, free its admission, admit the next ones."""
+        self.backend.release(plan)
+        with self._cv:
+            self._admitted -= 1
+            if not self._resident:
+                self._used -= need
+            self._admit_locked()
+            self._cv.notify_all()
+        self._finish(res, fut)
 
     def _finish(self, res, fut):
         with self._cv:

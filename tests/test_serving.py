@@ -104,3 +104,77 @@ def test_plan_cache_key_separates_contents():
     assert fingerprint(a.T) == fingerprint(np.ascontiguousarray(a.T))
     assert fingerprint(np.zeros((3, 0))) != fingerprint(np.zeros((0, 3)))
     assert fingerprint(None) != fingerprint(0)
+
+
+class CachingBackend(FakeBackend):
+    """Fake device memory with a plan cache: a plan's bytes are held from prepare until eviction, and idle
+    cached plans keep them (the overcommit case: cached plans plus a new request exceed the budget)."""
+
+    def __init__(self):
+        super().__init__()
+        self.cache = {}            # key -> [bytes held, busy count]
+        self.held = 0
+        self.max_held = 0
+        self.evicted = []
+
+    def build(self, req):
+        key = req.tag["key"]
+        with self.lock:
+            ent = self.cache.setdefault(key, [0, 0])
+            ent[1] += 1
+        return key, req.tag["foot"], False
+
+    def extra_bytes(self, key, req):
+        return 0 if self.cache[key][0] else req.tag["foot"]
+
+    def prepare(self, key, req):
+        with self.lock:
+            ent = self.cache[key]
+            if not ent[0]:
+                ent[0] = req.tag["foot"]
+                self.held += ent[0]
+                self.max_held = max(self.max_held, self.held)
+
+    def resident_bytes(self):
+        with self.lock:
+            return sum(v[0] for v in self.cache.values())
+
+    def solve(self, plan, req, slot):
+        time.sleep(req.tag["t"])
+        with self.lock:
+            self.order.append(req.rid)
+        return {"kappa": req.tag["kappa"], "converged": True}
+
+    def release(self, key):
+        with self.lock:
+            self.cache[key][1] -= 1
+
+    def evict_idle(self, need=None):
+        freed = 0
+        with self.lock:
+            for k in list(self.cache):
+                if need is not None and freed >= need:
+                    break
+                if self.cache[k][1] <= 0:
+                    freed += self.cache[k][0]
+                    self.held -= self.cache[k][0]
+                    self.evicted.append(k)
+                    del self.cache[k]
+        return freed
+
+
+def test_cached_idle_plans_count_against_the_budget():
+    be = CachingBackend()
+    srv = Server(backend=be, slots=2, builders=1, hbm_budget=100)
+    # three plans of 40 stay cached after their solves (120 > 100 once the third is prepared unless the
+    # first is evicted); a repeat of plan "a" reuses its resident tables
+    reqs = [Request(None, None, None, None, rid=i, tag={"key": k, "foot": 40, "t": 0.01, "kappa": 1.0})
+            for i, k in enumerate(["a", "b", "c", "a", "d"])]
+    res = []
+    for r in reqs:            # one at a time, so that earlier plans are idle in the cache
+        res += replay(srv, [r])
+    srv.close()
+    assert all(r.status == "ok" for r in res)
+    assert be.max_held <= 100, be.max_held
+    assert srv.max_held <= 100
+    assert be.evicted, "idle cached plans must be evicted to admit new ones"
