@@ -1,16 +1,27 @@
-"""Benchmark: served FP32+refine kappa_eff solves/s vs plain FP64 on one GB300.
+"""Benchmark: served FP32+refine kappa_eff solves/s and p50/p99 latency vs plain FP64, on one GB300.
 
-Workload (default): 2D periodic 100 nm cell, centred square pore at porosity
-0.25, seeded 60,000-triangle Delaunay mesh, synthetic lognormal material with
-100 MFPs x 96 directions (9,600 ordinates, 5.8e8 unknowns per sweep).
+Default workload (``c3_serve_512x50``): the seeded serving stream of 512 2D requests arriving as a
+Poisson process at 50 requests/s.  Each request draws porosity U(0.05, 0.40), a circular or square
+pore (50/50), a seeded periodic Delaunay mesh of log-uniform 2k-60k triangles, 48 or 96 directions and
+30-100 MFPs of the synthetic lognormal material (bulk 150 W/mK).  Meshes are built before the timed
+region (the reference's ``BTE_RTA`` takes a built ``Mesh`` too); everything after that is timed:
+each request goes through ``serving.Server`` (host schedule build, HBM admission, table upload, solve
+on one of the GPU slots, kappa_eff back to the host).  The stream is timed as one run; a "step" is
+1/K of it (``config.requests_per_step``).  Also measured: FP64 solves of every request (the kappa
+error of each served result), plain FP64 one at a time on a seeded subset, the same requests the
+reference arm solves, and the resident 60k-triangle solve of the 2D scale-up config (``resident_c1``,
+which also carries the sweep kernel's roofline).
 
-One step = one kappa_eff solve (the full source iteration to the fixed point,
-plus the final output sweep) on inputs resident in HBM. ``e2e`` repeats the
-solve through the public ``BTE_RTA`` call with host arrays (host->device copy
-of the initial temperature, device->host copy of every output in the timed
-region). Under torchrun every rank is an independent replica.
+Other workloads (``--workload``): ``c1_60k_100x96`` (one kappa_eff solve per step on a resident plan),
+``c2_100k_30x16x32`` (3D), ``c4_inverse_128x50x64`` (inverse-design gradient).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+``--impl reference`` times the unmodified reference (``baseline/_ref``, imported through
+``oracle/ref_loader.py``) on the host cores: for the serving stream, one request per step (Fourier
+first guess, then ``BTE_RTA`` with its own process pool on all cores, bte_rtol 1e-6, which keeps its
+kappa within 1e-4 of its converged value) on a seeded sample of the same stream restricted to meshes
+of at most 4,000 triangles (full reference solves of the larger requests take minutes each).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload ...]
 """
 from __future__ import annotations
 
@@ -38,6 +49,13 @@ WORKLOADS = {
     # inverse design: pixels per side, n_mfp, n_dir, density-field seed
     "c4_inverse_128x50x64": (128, 50, 64, None, "pixels", 0),
 }
+# serving streams: name -> (requests, arrival rate per second)
+SERVE = {"c3_serve_512x50": (512, 50.0)}
+# largest mesh of the requests the reference arm solves in full (one step each)
+REF_MAX_TRI = 4000
+# the reference's tolerance for the served workload: with the Fourier first guess, bte_rtol 1e-6 keeps its
+# kappa within 3e-6 of its converged value on the 2k-triangle cell (1e-5: 1.5e-4; its default 1e-4: 1e-3)
+REF_BTE_RTOL = 1e-6
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) of one FP32 sweep launch, from one ncu capture of `bench.py --profile-sweeps 2`
 # (dram__bytes.sum.per_second x gpu__time_duration): 154.7 GB/s x 1.852 ms.  The iterate stays in shared
@@ -75,13 +93,10 @@ def _stream_mesh(args):
     return mesh_from_cell(porous_cell_2d(n_tri, phi, pore, seed=seed))
 
 
-def serving_stream(n_req, seed=0):
-    """Seeded request mix: porosity U(0.05, 0.40), circle/square pore 50/50, log-uniform 2k-60k triangles,
-    48 or 96 directions, 30-100 MFPs (meshes built in a spawn pool before the stream starts)."""
-    import multiprocessing as mp
-    from openbte_gb300 import objects as O
-    from openbte_gb300.material import synthetic_isotropic_2d
-    from openbte_gb300.serving import Request
+def stream_spec(n_req, seed=0):
+    """Seeded request mix: (triangles, porosity, pore, mesh seed, directions, MFPs) per request, in arrival order:
+    porosity U(0.05, 0.40), circle/square pore 50/50, log-uniform 2k-60k triangles, 48 or 96 directions,
+    30-100 MFPs."""
     rng = np.random.default_rng(seed)
     spec = []
     for i in range(n_req):
@@ -91,42 +106,153 @@ def serving_stream(n_req, seed=0):
         n_dir = int(rng.choice([48, 96]))
         n_mfp = int(rng.integers(30, 101))
         spec.append((n_tri, phi, pore, 1000 + i, n_dir, n_mfp))
+    return spec
+
+
+def reference_sample(k, seed=0, max_tri=REF_MAX_TRI):
+    """The first k requests of the seeded stream with at most max_tri triangles: [(request index, spec)]."""
+    out = []
+    for i, sp in enumerate(stream_spec(max(4096, 64 * k), seed)):
+        if sp[0] <= max_tri:
+            out.append((i, sp))
+            if len(out) == k:
+                break
+    return out
+
+
+def serving_stream(n_req, seed=0, only=None):
+    """Requests of the seeded stream (meshes built in a spawn pool, before any timing); `only`: request
+    indices to build (default: the first n_req)."""
+    import multiprocessing as mp
+    from openbte_gb300 import objects as O
+    from openbte_gb300.material import synthetic_isotropic_2d
+    from openbte_gb300.serving import Request
+    spec = stream_spec(max(n_req, 1 + max(only)) if only else n_req, seed)
+    idx = list(only) if only else list(range(n_req))
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
-        meshes = pool.map(_stream_mesh, [(a, b, c, d) for a, b, c, d, _, _ in spec])
+        meshes = pool.map(_stream_mesh, [spec[i][:4] for i in idx])
     bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
     ek = O.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
     reqs = []
-    for i, (geo, (n_tri, phi, pore, _, n_dir, n_mfp)) in enumerate(zip(meshes, spec)):
+    for i, geo in zip(idx, meshes):
+        n_tri, phi, pore, _, n_dir, n_mfp = spec[i]
         reqs.append(Request(geo, synthetic_isotropic_2d(n_mfp, n_dir), bcs, ek, rid=i,
                             tag={"n_elems": geo.n_elems, "phi": phi, "pore": pore, "n_dir": n_dir, "n_mfp": n_mfp}))
     return reqs
 
 
-def run_serving(n_req, rate, device, slots=4):
-    from openbte_gb300.serving import GPUBackend, Server, replay, summarize
+def serve_requests(reqs, precision, rtol, device, slots, builders, preparers, rate=None, seed=1):
+    """Replay `reqs` through a fresh server (Poisson arrivals at `rate`, None: all at once).
+    Returns (results, wall seconds, server, backend)."""
+    import torch
+    from openbte_gb300.serving import GPUBackend, Server, replay
+    for r in reqs:
+        r.precision = precision
+        r.rtol = rtol
+    be = GPUBackend(device=device)
+    srv = Server(backend=be, slots=slots, builders=builders, preparers=preparers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = replay(srv, reqs, rate=rate, seed=seed)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    srv.close()
+    return res, wall, srv, be
+
+
+def run_serve(args, dev, world, rank, local):
+    """The serving stream (configs[3]): served FP32+refine against plain FP64 on the same GPU."""
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.serving import summarize
+    lib = _lib.load()
+    n_req, rate = SERVE[args.workload]
+    os.environ["OBTE_HOST_THREADS"] = str(args.host_threads)
+    pool = dict(device=local, slots=args.slots, builders=args.builders, preparers=args.preparers)
+    t0 = time.time()
     reqs = serving_stream(n_req)
-    out = {"requests": n_req, "rate_per_s": rate,
-           "unknowns_per_sweep_mean": float(np.mean([r.tag["n_elems"] * r.tag["n_dir"] * r.tag["n_mfp"]
-                                                     for r in reqs]))}
-    for prec, nslots in (("fp32_refine", slots), ("fp64", 1)):
-        for r in reqs:
-            r.precision = prec
-            r.rtol = 1e-6 if prec == "fp32_refine" else 1e-8
-        srv = Server(backend=GPUBackend(device=device), slots=nslots, builders=4)
-        t0 = time.perf_counter()
-        res = replay(srv, reqs, rate=rate, seed=1)
-        wall = time.perf_counter() - t0
-        srv.close()
-        s = summarize(res, wall)
-        s["slots"] = nslots
-        s["max_concurrent"] = srv.max_concurrent
-        out[prec] = s
-        if prec == "fp32_refine":
-            k32 = {r.rid: r.kappa for r in res}
-        else:
-            errs = [abs(k32[r.rid] - r.kappa) / abs(r.kappa) for r in res if r.status == "ok"]
-            out["kappa_rel_err_fp32_refine_vs_fp64_max"] = float(max(errs)) if errs else None
-    return out
+    mesh_s = time.time() - t0
+    # warm-up: a few requests of the stream through a throwaway server in each precision
+    warm = reqs[:max(3, args.warmup)]
+    for prec in ("fp32_refine", "fp64"):
+        serve_requests(warm, prec, args.serve_rtol, **pool)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    l0 = lib.obte_launch_count()
+    with Clocks(local) as clk:
+        res, wall, srv, be = serve_requests(reqs, "fp32_refine", args.serve_rtol, rate=rate, seed=1, **pool)
+    launches = lib.obte_launch_count() - l0
+    barrier()
+    summ = summarize(res, wall)
+    t_job = max_over_ranks(wall, world, dev)
+    ok = [r for r in res if r.status == "ok"]
+    value = world * len(ok) / t_job
+    # FP64 solve of every request: the kappa error of each served FP32+refine result
+    res64, wall64, srv64, _ = serve_requests(reqs, "fp64", 1e-9, rate=None, **pool)
+    k64 = {r.rid: r.kappa for r in res64 if r.status == "ok"}
+    errs = [abs(r.kappa - k64[r.rid]) / abs(k64[r.rid]) for r in ok if r.rid in k64]
+    # plain FP64 one request at a time (one slot, back to back) on a seeded subset, same tolerance as the
+    # served FP32+refine form
+    sub = reqs[::args.fp64_subset_every]
+    res1, wall1, _, _ = serve_requests(sub, "fp64", args.serve_rtol, rate=None, **dict(pool, slots=1))
+    lat1 = np.array([r.t_done - r.t_start for r in res1 if r.status == "ok"])
+    fp64_rate = len(lat1) / wall1
+    # the requests the reference arm solves (its timed steps), served here the same two ways
+    ref_ids = [i for i, _ in reference_sample(args.warmup + args.steps)][args.warmup:]
+    same = serving_stream(0, only=ref_ids)
+    r_one, w_one, _, _ = serve_requests(same, "fp32_refine", args.serve_rtol, rate=None, **dict(pool, slots=1))
+    r_srv, w_srv, _, _ = serve_requests(same, "fp32_refine", args.serve_rtol, rate=None, **pool)
+    # bytes: plan tables uploaded per request (host -> device); per-ordinate kappa K read back per request
+    h2d = be.uploaded_bytes
+    d2h = sum(r.tag["n_dir"] * r.tag["n_mfp"] * 8 for r in reqs)
+    K = args.steps
+    line = {
+        "metric": "kappa_eff solves/s (served FP32+refine, <=1e-4 kappa error)",
+        "value": value, "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": t_job * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded request stream: meshes, materials, Poisson arrivals)",
+        "config": {"workload": args.workload, "requests": n_req, "rate_per_s": rate,
+                   "requests_per_step": n_req / K, "step": "1/K of the stream, timed as one run",
+                   "precision": "fp32_refine", "rtol": args.serve_rtol,
+                   "unknowns_per_sweep_mean": float(np.mean([r.tag["n_elems"] * r.tag["n_dir"] * r.tag["n_mfp"]
+                                                             for r in reqs])),
+                   "server": {"slots": args.slots, "builders": args.builders, "preparers": args.preparers,
+                              "host_threads_per_build": args.host_threads},
+                   "value_scope": "end to end: host meshes in, kappa_eff out (schedule build, table upload, "
+                                  "solve, read-back all inside the timed region)",
+                   "l2": "every request is a new mesh (plans, tables and Krylov vectors of 2k-60k-element "
+                         "problems; the stream's working set is far above L2)",
+                   "parallelism": f"replicas{world}" if world > 1 else "single"},
+        "latency_ms": {"p50": summ["p50_ms"], "p99": summ["p99_ms"]},
+        "served": {k: summ[k] for k in ("completed", "rejected", "errors", "error_messages", "mean_queue_ms", "wall_s")}
+                  | {"max_concurrent": srv.max_concurrent, "max_hbm_held_gb": srv.max_held / 1e9,
+                     "sweeps_per_request_mean": float(np.mean([r.n_sweeps for r in ok])) if ok else None,
+                     "mesh_build_s_untimed": mesh_s},
+        "kappa_rel_err_vs_fp64": {"max": float(max(errs)) if errs else None,
+                                  "median": float(np.median(errs)) if errs else None, "requests": len(errs),
+                                  "fp64_rtol": 1e-9},
+        "fp64_one_at_a_time": {"solves_per_s": fp64_rate, "requests": len(lat1),
+                               "subset": f"every {args.fp64_subset_every}th request of the stream",
+                               "rtol": args.serve_rtol,
+                               "latency_ms": {"p50": float(np.percentile(lat1, 50) * 1e3),
+                                              "p99": float(np.percentile(lat1, 99) * 1e3)} if len(lat1) else None},
+        "fp64_served_rtol1e-9": {"solves_per_s": len(k64) / wall64, "wall_s": wall64},
+        "speedup_vs_fp64_one_at_a_time": value / fp64_rate if fp64_rate else None,
+        "reference_sample": {"requests": ref_ids, "max_triangles": REF_MAX_TRI,
+                             "one_at_a_time_solves_per_s": len(r_one) / w_one,
+                             "served_solves_per_s": len(r_srv) / w_srv},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d / K),
+                "d2h_bytes_per_step": int(d2h / K)},
+        "gpu_launches": int(round(launches / K)),
+        "clocks": clk.summary(),
+    }
+    return line
 
 
 def algorithmic_sweep_bytes(geo, mat, b_T):
@@ -382,9 +508,83 @@ def max_over_ranks(x, world, device):
     return float(t.item())
 
 
+def reference_serve(args, steps, warmup, n_process=None):
+    """Unmodified reference solves, one request per step, on the seeded sample of the serving stream.
+
+    Each step is the reference's own pipeline for one request: ``Fourier`` (openbte/fourier.py:15-185)
+    for the first guess, then ``BTE_RTA`` (openbte/bte.py:19-271) at bte_rtol 1e-6 with its forking
+    process pool (openbte/utils.py:186-219) on every host core.  The request's mesh (this package's
+    seeded cell written as msh2 and read by the reference's own ``get_mesh``) and material are built
+    before the step, as the GPU arm's meshes are.  Returns (per-step seconds, kappas, request ids, cores)."""
+    import contextlib
+    import io
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_loader
+    from openbte_gb300.geometry import porous_cell_2d, write_msh2
+    from openbte_gb300.material import synthetic_isotropic_2d
+    if not ref_loader.available():
+        return None
+    R = ref_loader.load(in_process=False)
+    cores = n_process or (os.cpu_count() or 1)
+    sample = reference_sample(warmup + steps)
+    bcs = R.objects.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
+    ek = R.objects.EffectiveThermalConductivity(normalization=-1.0, contact="Periodic_x")
+    times, kappas, ids = [], [], []
+    argv = sys.argv
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, (rid, (n_tri, phi, pore, seed, n_dir, n_mfp)) in enumerate(sample):
+            path = write_msh2(porous_cell_2d(n_tri, phi, pore, seed=seed), os.path.join(tmp, f"r{rid}"))
+            with contextlib.redirect_stdout(io.StringIO()):
+                geo = R.mesh.get_mesh(path[:-4])
+            mat = R.objects.Material(*synthetic_isotropic_2d(n_mfp, n_dir))
+            sys.argv = [argv[0], "-np", str(cores)]      # the reference's runner reads its worker count here
+            try:
+                t0 = time.perf_counter()
+                with contextlib.redirect_stdout(io.StringIO()):
+                    f = R.fourier.Fourier(geo, mat.thermal_conductivity, bcs, effective_thermal_conductivity=ek)
+                    b = R.bte.BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek,
+                                      bte_rtol=REF_BTE_RTOL)
+                dt = time.perf_counter() - t0
+            finally:
+                sys.argv = argv
+            if k >= warmup:
+                times.append(dt)
+                kappas.append(float(b.kappa_eff))
+                ids.append(rid)
+    return times, kappas, ids, cores
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.workload in SERVE:
+        t0 = time.time()
+        out = reference_serve(args, args.steps, args.warmup)
+        if out is None:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference is not installed under baseline/_ref"}))
+            return
+        times, kappas, ids, cores = out
+        v = len(times) / sum(times)
+        sample = (f"{len(times)} requests of the seeded serving stream with at most {REF_MAX_TRI} triangles "
+                  f"(request ids {ids}), each a full unmodified reference solve (Fourier + BTE_RTA at bte_rtol "
+                  f"{REF_BTE_RTOL}, {cores} worker processes), after {args.warmup} warm-up requests; larger "
+                  f"requests of the stream are not run (minutes each), so this is the reference on the "
+                  f"stream's smallest requests")
+        print(json.dumps({"impl": "reference", "metric": "kappa_eff solves/s (served FP32+refine, <=1e-4 kappa error)",
+                          "value": v, "unit": "solves/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded request stream)",
+                          "config": {"workload": args.workload, "sample_max_triangles": REF_MAX_TRI,
+                                     "bte_rtol": REF_BTE_RTOL},
+                          "latency_ms": {"p50": float(np.percentile(times, 50) * 1e3),
+                                         "p99": float(np.percentile(times, 99) * 1e3)},
+                          "kappa_eff": kappas,
+                          "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "reference",
+                                           "sample": sample},
+                          "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                          "wall_s": time.time() - t0}))
         return
     if args.workload.startswith("c4_"):
         n, n_mfp, n_dir = WORKLOADS[args.workload][:3]
@@ -422,52 +622,11 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c1_60k_100x96", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp32_refine", choices=["fp32_refine", "fp32", "fp64"])
-    ap.add_argument("--rtol", type=float, default=1e-7)
-    ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve", type=int, default=0,
-                    help="also replay a seeded serving stream of this many requests (Poisson arrivals)")
-    ap.add_argument("--serve-rate", type=float, default=50.0)
-    ap.add_argument("--fd-pixels", type=int, default=0,
-                    help="config 4: also check dkappa/drho against central differences on this many pixels")
-    ap.add_argument("--profile-sweeps", type=int, default=0,
-                    help="only build the plan and run this many FP32 and FP64 sweeps (for ncu captures)")
-    ap.add_argument("--profile-fourier", type=int, default=0,
-                    help="only build the Fourier plan and run this many Fourier first-guess solves")
-    ap.add_argument("--profile-solves", type=int, default=0,
-                    help="only build the plan and run this many kappa_eff solves (for launch lists)")
-    ap.add_argument("--profile-gradients", type=int, default=0,
-                    help="config 4: only run this many gradient evaluations on new density fields (for launch lists)")
-    args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
-    if args.impl == "reference":
-        return reference_arm(args)
-
+def run_resident(args, dev, world, rank, local):
+    """One kappa_eff solve per step on a resident plan (c1 / c2 workloads); the profile options print
+    their own line and return None."""
     import torch
     import torch.distributed as dist
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    if args.workload.startswith("c4_"):
-        if rank == 0:
-            run_inverse(args, dev)
-        if world > 1:
-            dist.destroy_process_group()
-        return
-
     from openbte_gb300 import _lib
     from openbte_gb300.bte import BTE_RTA, solve_plan
     from openbte_gb300.fourier import Fourier, get_fourier_plan
@@ -670,12 +829,108 @@ def main():
         "preconditioner": {"blocks": pb.value, "setup_sweeps": ps.value, "setup_ms": pms.value},
         "wall_timed_s": t_total,
     }
-    if args.serve:
-        line["serving"] = run_serving(args.serve, args.serve_rate, local)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(geo, mat, bcs, ek)
         line["cpu_baseline"].pop("seconds_per_solve", None)
-    if rank == 0:
+    return line
+
+def _resident_args(args):
+    """The resident 60k-triangle solve of the 2D scale-up config, run beside the serving stream."""
+    a = argparse.Namespace(**vars(args))
+    a.workload = "c1_60k_100x96"
+    a.steps = max(3, min(args.steps, 10))
+    a.warmup = 3
+    a.precision = "fp32_refine"
+    a.rtol = 1e-7
+    a.fp64_steps = 1
+    a.no_cpu_baseline = True
+    return a
+
+
+def reference_cpu_sample(args, steps=3):
+    """cpu_baseline of the serving line: the reference arm on a bounded sample, in a child process (the
+    reference forks its workers, which must not happen in a process that holds a CUDA context)."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", args.workload,
+           "--steps", str(steps), "--warmup", "1", "--sample-only"]
+    try:
+        out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=dict(os.environ, RANK="0"))
+        for l in reversed(out.stdout.splitlines()):
+            if l.startswith("{"):
+                d = json.loads(l)
+                return d.get("cpu_baseline")
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c3_serve_512x50", choices=sorted(WORKLOADS) + sorted(SERVE))
+    ap.add_argument("--precision", default="fp32_refine", choices=["fp32_refine", "fp32", "fp64"])
+    ap.add_argument("--rtol", type=float, default=1e-7)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-rtol", type=float, default=1e-6,
+                    help="serving stream: residual tolerance of each request (FP32+refine and one-at-a-time FP64)")
+    ap.add_argument("--slots", type=int, default=8, help="serving stream: concurrent GPU solves")
+    ap.add_argument("--builders", type=int, default=8, help="serving stream: host threads building plans")
+    ap.add_argument("--preparers", type=int, default=6, help="serving stream: host threads uploading tables")
+    ap.add_argument("--host-threads", type=int, default=2, help="serving stream: host threads per plan build")
+    ap.add_argument("--fp64-subset-every", type=int, default=8,
+                    help="serving stream: plain FP64 one at a time on every n-th request")
+    ap.add_argument("--fd-pixels", type=int, default=0,
+                    help="config 4: also check dkappa/drho against central differences on this many pixels")
+    ap.add_argument("--profile-sweeps", type=int, default=0,
+                    help="only build the plan and run this many FP32 and FP64 sweeps (for ncu captures)")
+    ap.add_argument("--profile-fourier", type=int, default=0,
+                    help="only build the Fourier plan and run this many Fourier first-guess solves")
+    ap.add_argument("--profile-solves", type=int, default=0,
+                    help="only build the plan and run this many kappa_eff solves (for launch lists)")
+    ap.add_argument("--profile-gradients", type=int, default=0,
+                    help="config 4: only run this many gradient evaluations on new density fields (for launch lists)")
+    ap.add_argument("--sample-only", action="store_true",
+                    help="reference arm: a bounded cpu_baseline sample (the warm-up may be shorter than 3 steps)")
+    args = ap.parse_args()
+    if args.warmup < 3 and not args.sample_only:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if args.workload.startswith("c4_"):
+        if rank == 0:
+            run_inverse(args, dev)
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    if args.workload in SERVE:
+        line = run_serve(args, dev, world, rank, local)
+        if rank == 0:
+            res = run_resident(_resident_args(args), dev, 1, 0, local)
+            if res is not None:
+                line["roofline"] = dict(res["roofline"], workload="c1_60k_100x96 (resident plan)")
+                line["resident_c1"] = {k: res[k] for k in ("value", "ms_per_step", "latency_ms", "fp64",
+                                                          "speedup_vs_fp64", "kappa_rel_err_vs_fp64", "sweeps_per_solve",
+                                                          "fp64_sweeps_per_solve", "e2e", "pipeline", "preconditioner")}
+                line["resident_c1"]["config"] = res["config"]
+            if not args.no_cpu_baseline:
+                line["cpu_baseline"] = reference_cpu_sample(args)
+    else:
+        line = run_resident(args, dev, world, rank, local)
+    if rank == 0 and line is not None:
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

@@ -176,7 +176,8 @@ obte_status obte_bte_plan_set_stream(obte_plan plan, void* stream);
  * No counterpart in the reference, which builds its operators inside BTE_RTA (openbte/bte.py:47-185).
  */
 obte_status obte_bte_plan_prepare(obte_plan plan, int32_t precision, int32_t restart);
-/* Device bytes held by the plan (tables) and by one solve's scratch. */
+/* Device bytes held by the plan (tables: their actual size once uploaded, an upper estimate before) and by
+ * one solve's scratch (an upper estimate). */
 obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision, int32_t restart,
                                     int64_t* plan_bytes, int64_t* solve_bytes);
 

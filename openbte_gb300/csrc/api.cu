@@ -212,10 +212,13 @@ extern "C" obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision
     b += (s.lev_ptr.size() + s.in_idx.size()) * 8; // unit tables and periodic prefetch lists (bound)
     return (int64_t)b;
   };
+  // tables that are uploaded count with their actual size, the others with an upper estimate
+  const int64_t t64 = plan->d64.ready ? (int64_t)plan->d64.bytes() : tab(8);
+  const int64_t t32 = plan->d32.ready ? (int64_t)plan->d32.bytes() : tab(4);
   int64_t pb = (int64_t)plan->nu * 8 + (int64_t)s.x_cell.size() * 4 + (int64_t)s.kconst.size() * 24;
-  if (precision == OBTE_FP64) pb += tab(8);
-  else if (precision == OBTE_FP32) pb += tab(4);
-  else pb += tab(8) + tab(4);
+  if (precision == OBTE_FP64) pb += t64;
+  else if (precision == OBTE_FP32) pb += t32;
+  else pb += t64 + t32;
   if (plan_bytes) *plan_bytes = pb;
   if (solve_bytes) *solve_bytes = plan->ctx ? solve_scratch_bytes(plan, restart > 0 ? restart : 30) : 0;
   return OBTE_OK;

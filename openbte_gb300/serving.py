@@ -56,6 +56,8 @@ class Result:
     error: str = ""
     t_submit: float = 0.0
     t_built: float = 0.0
+    t_admitted: float = 0.0
+    t_prepared: float = 0.0
     t_start: float = 0.0
     t_done: float = 0.0
     footprint: int = 0
@@ -95,6 +97,7 @@ class GPUBackend:
         self._cache: "collections.OrderedDict[str, Any]" = collections.OrderedDict()
         self._busy = collections.Counter()
         self._lock = threading.Lock()
+        self.uploaded_bytes = 0      # device table bytes uploaded by prepare (host -> device)
 
     def _stream(self):
         s = getattr(self._tl, "stream", None)
@@ -147,6 +150,8 @@ class GPUBackend:
         pl.set_stream(st.cuda_stream)
         pl.prepare(req.precision, self.restart)
         with self._lock:
+            if not pl.tables:
+                self.uploaded_bytes += pl.footprint(req.precision, self.restart)[0]
             pl.tables |= _TABLES[req.precision]
             pl.resident = max(pl.resident, self._footprint(pl, req))
 
@@ -203,13 +208,13 @@ class Server:
     """Continuous batching: host threads build and prepare plans, `slots` GPU workers solve concurrently."""
 
     def __init__(self, backend=None, slots: int = 4, builders: int = 4, hbm_budget: Optional[int] = None,
-                 hbm_fraction: float = 0.7, ahead: Optional[int] = None):
+                 hbm_fraction: float = 0.7, ahead: Optional[int] = None, preparers: int = 2):
         self.backend = backend if backend is not None else GPUBackend()
         self.slots = slots
         self.ahead = slots if ahead is None else ahead
         self.budget = int(hbm_budget) if hbm_budget is not None else self.backend.budget(hbm_fraction)
         self._builders = cf.ThreadPoolExecutor(max_workers=builders, thread_name_prefix="obte-build")
-        self._preparers = cf.ThreadPoolExecutor(max_workers=max(1, min(2, builders)), thread_name_prefix="obte-prep")
+        self._preparers = cf.ThreadPoolExecutor(max_workers=max(1, preparers), thread_name_prefix="obte-prep")
         self._cv = threading.Condition()
         self._waiting: "collections.deque" = collections.deque()   # built, waiting for admission
         self._ready: "collections.deque" = collections.deque()     # prepared, waiting for a slot
@@ -273,6 +278,7 @@ class Server:
                 return
             i, item, need = pick
             del self._waiting[i]
+            item[1].t_admitted = time.perf_counter()
             self._admitted += 1
             if self._resident:
                 self._reserved += need
@@ -314,6 +320,7 @@ class Server:
                 prep(plan, req)
         except Exception as e:  # noqa: BLE001
             err = f"{type(e).__name__}: {e}"
+        res.t_prepared = time.perf_counter()
         with self._cv:
             self._preparing -= 1
             if self._resident:

@@ -6,13 +6,13 @@ tetrahedron spherical-pore cube with 30 x 16 x 32) are far beyond what the refer
 full: its per-ordinate SuperLU factorisation (openbte/bte.py:181-185) costs 0.5 s per ordinate on the
 2D mesh and ~290 s on the 3D one, on one core.  These cases keep the meshes and cut the ordinates, so the
 reference's own solver (``BTE_RTA``, openbte/bte.py:19-271, with its forking process pool,
-openbte/utils.py:186-219) runs them to bte_rtol=1e-12:
+openbte/utils.py:186-219) runs them to a tight bte_rtol:
 
 * ``c1scale``: the 60k-triangle mesh of the 2D benchmark (porous_cell_2d(60000, 0.25, 'square', seed=1)),
-  8 MFPs x 16 directions, Fourier first guess (openbte/fourier.py) then BTE;
+  8 MFPs x 16 directions, Fourier first guess (openbte/fourier.py) then BTE, bte_rtol=1e-12;
 * ``c2scale``: the 110k-tetrahedron mesh of the 3D benchmark (porous_cube_3d(100000, 0.10, seed=1)),
   2 MFPs (100 nm, 10 um) x 2 polar x 4 azimuthal directions, BTE from DeltaT = 0 (the reference's 3D
-  Fourier factorisation is skipped; the GPU test starts from zeros as well).
+  Fourier factorisation is skipped; the GPU test starts from zeros as well), bte_rtol=1e-10.
 
 Run where the reference is importable (``oracle/ref_loader.py``); writes ``tests/golden/<case>.npz`` with
 the cell (nodes, elements, boundary segments, periodic pairs), the material and the reference outputs:
@@ -40,15 +40,17 @@ from openbte_gb300.geometry import porous_cell_2d, porous_cube_3d, write_msh2  #
 from openbte_gb300.material import synthetic_isotropic_2d, synthetic_isotropic_3d  # noqa: E402
 
 CASES = {
-    # name: (dimension, n_elems target, porosity, pore, seed, material args, Fourier first guess)
-    "c1scale": (2, 60000, 0.25, "square", 1, dict(n_mfp=8, n_phi=16), True),
+    # name: (dimension, n_elems target, porosity, pore, seed, material args, Fourier first guess, bte_rtol)
+    "c1scale": (2, 60000, 0.25, "square", 1, dict(n_mfp=8, n_phi=16), True, 1e-12),
+    # the reference's stopping test (change of the norm of DeltaT between iterations) sits at round-off on
+    # the 110k-tetrahedron mesh before it reaches 1e-12; 1e-10 is four orders below the tests' 1e-6
     "c2scale": (3, 100000, 0.10, "sphere", 1, dict(n_mfp=2, n_theta=2, n_phi=4, mfp_min=100.0, mfp_max=1.0e4),
-                False),
+                False, 1e-10),
 }
 
 
 def run_case(R, name, n_process, tmpdir):
-    dim, n_target, porosity, pore, seed, margs, with_fourier = CASES[name]
+    dim, n_target, porosity, pore, seed, margs, with_fourier, rtol = CASES[name]
     t0 = time.time()
     if dim == 3:
         cell = porous_cube_3d(n_target, porosity, seed=seed)
@@ -82,9 +84,9 @@ def run_case(R, name, n_process, tmpdir):
     sys.argv = [argv[0], "-np", str(n_process)]      # the reference's runner reads its worker count here
     try:
         t2 = time.time()
-        with contextlib.redirect_stdout(io.StringIO()):
-            b = R.bte.BTE_RTA(geo, rmat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-12,
-                              bte_max_iter=3000)
+        # the reference prints one line per iteration (kept in the generator's output as a progress log)
+        b = R.bte.BTE_RTA(geo, rmat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=rtol,
+                          bte_max_iter=3000)
         t_bte = time.time() - t2
     finally:
         sys.argv = argv
@@ -95,7 +97,7 @@ def run_case(R, name, n_process, tmpdir):
         mat_args=repr(margs), normalization=normalization, jumps=repr(periodic),
         mfps=mat.mfps, vmfp=mat.vmfp, sigma=mat.sigma, t_coeff=mat.t_coeff, kappa_bulk=mat.thermal_conductivity,
         bte_kappa=b.kappa_eff, bte_T=b.variables["Temperature_BTE"]["data"], bte_J=b.variables["Flux_BTE"]["data"],
-        bte_S=b.aux["suppression"], n_process=n_process, t_mesh=t_mesh, t_fourier=t_fourier, t_bte=t_bte,
+        bte_S=b.aux["suppression"], bte_rtol=rtol, n_process=n_process, t_mesh=t_mesh, t_fourier=t_fourier, t_bte=t_bte,
         fourier_guess=with_fourier,
     )
     for region, segs in cell.segments.items():
