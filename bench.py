@@ -46,6 +46,8 @@ WORKLOADS = {
     "c1_60k_100x96": (60000, 100, 96, 0.25, "square", 1),
     "c0_2k_30x48": (2000, 30, 48, 0.25, "square", 1),
     "c2_100k_30x16x32": (100000, 30, (16, 32), 0.10, "sphere", 1),
+    # the 3D benchmark mesh with 4 x 8 directions: device tables of ~0.5 GB, for profiler captures
+    "c2_100k_30x4x8": (100000, 30, (4, 8), 0.10, "sphere", 1),
     # inverse design: pixels per side, n_mfp, n_dir, density-field seed
     "c4_inverse_128x50x64": (128, 50, 64, None, "pixels", 0),
 }
@@ -57,10 +59,14 @@ REF_MAX_TRI = 4000
 # kappa within 3e-6 of its converged value on the 2k-triangle cell (1e-5: 1.5e-4; its default 1e-4: 1e-3)
 REF_BTE_RTOL = 1e-6
 L2_BYTES = 129 * 1024 * 1024
-# DRAM bytes (read + write) of one FP32 sweep launch, from one ncu capture of `bench.py --profile-sweeps 2`
-# (dram__bytes.sum.per_second x gpu__time_duration): 154.7 GB/s x 1.852 ms.  The iterate stays in shared
-# memory, so this is about an eighth of the algorithmic bytes.
-SWEEP_DRAM_BYTES = {"c1_60k_100x96": 2.866e8}
+# DRAM bytes of one sweep launch (dram__bytes.sum.per_second x gpu__time_duration of one ncu capture of
+# `bench.py --workload <w> --profile-sweeps 2` with the current kernel; profiles/bte_sweep_*.md); the
+# iterate stays in shared memory, so this is about an eighth of the algorithmic bytes
+SWEEP_DRAM_BYTES = {("c1_60k_100x96", "fp32"): 2.873e8, ("c1_60k_100x96", "fp64"): 4.299e8,
+                    ("c2_100k_30x4x8", "fp32"): 2.501e8}
+SWEEP_DRAM_SOURCE = {("c1_60k_100x96", "fp32"): "profiles/bte_sweep_fp32_c1_60k_100x96.md",
+                     ("c1_60k_100x96", "fp64"): "profiles/bte_sweep_fp64_c1_60k_100x96.md",
+                     ("c2_100k_30x4x8", "fp32"): "profiles/bte_sweep_fp32_c2_110k_30x4x8.md"}
 
 
 def problem(workload):
@@ -818,9 +824,8 @@ def run_resident(args, dev, world, rank, local):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(round(launches)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": SWEEP_DRAM_BYTES.get(args.workload) if fp32 else None,
-                     "traffic_source": "ncu dram__bytes of one FP32 sweep launch (profiles/bte_sweep_fp32_c1_60k_100x96.md)"
-                     if fp32 and args.workload in SWEEP_DRAM_BYTES else None,
+                     "traffic": SWEEP_DRAM_BYTES.get((args.workload, "fp32" if fp32 else "fp64")),
+                     "traffic_source": SWEEP_DRAM_SOURCE.get((args.workload, "fp32" if fp32 else "fp64")),
                      "kernel": "bte_sweep_kernel", "ms_per_launch": t_sweep * 1e3,
                      "algorithmic_bytes": int(bytes_sweep), "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "clocks": clk.summary(),
