@@ -879,7 +879,7 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-7)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-rtol", type=float, default=1e-6,
+    ap.add_argument("--serve-rtol", type=float, default=1e-5,
                     help="serving stream: residual tolerance of each request (FP32+refine and one-at-a-time FP64)")
     ap.add_argument("--slots", type=int, default=8, help="serving stream: concurrent GPU solves")
     ap.add_argument("--builders", type=int, default=8, help="serving stream: host threads building plans")

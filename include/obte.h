@@ -132,6 +132,16 @@ obte_status obte_context_create(int device, void* stream, obte_context* out);
 obte_status obte_context_destroy(obte_context ctx);
 obte_status obte_context_set_stream(obte_context ctx, void* stream);
 const char* obte_status_string(int status);
+/*
+ * Device memory of destroyed plans is kept in a library-wide cache and reused by later plans instead of
+ * being returned with cudaFree, which synchronises the whole device and stalls every solve running
+ * on other streams (a serving loop drops a plan after every request).  The cache keeps at most
+ * OBTE_DEVICE_CACHE_MB megabytes (default 16 GiB; older blocks beyond it are freed) and is trimmed by
+ * itself when an allocation fails.  obte_device_cache_trim frees all of it (freed_bytes may be NULL);
+ * obte_device_cache_bytes reports its size.  No counterpart in the reference (it has no device code).
+ */
+obte_status obte_device_cache_trim(int64_t* freed_bytes);
+obte_status obte_device_cache_bytes(int64_t* cached_bytes);
 /* Last error text recorded on this thread (CUDA error names, argument checks). */
 const char* obte_last_error(void);
 /* Number of kernel launches this library issued in the calling process (instrumentation). */

@@ -3,6 +3,7 @@
 
 #include <atomic>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "internal.h"
@@ -23,21 +24,151 @@ obte_status cuda_fail(cudaError_t e, const char* what, const char* file, int lin
 
 void count_launch(int n) { g_launches += n; }
 
+// ---- recycled device blocks ---------------------------------------------------------------
+namespace {
+struct CachedBlock {
+  void* p;
+  size_t bytes;
+  int dev;
+};
+std::mutex g_cache_mu;
+std::vector<CachedBlock> g_cache;     // idle blocks, oldest first
+size_t g_cached = 0;
+thread_local int g_recycle = 0;
+
+// Most bytes the cache keeps (OBTE_DEVICE_CACHE_MB, default 16 GiB); older blocks beyond it are freed.
+size_t cache_cap() {
+  static const size_t cap = [] {
+    const char* e = std::getenv("OBTE_DEVICE_CACHE_MB");
+    return e ? (size_t)std::max(0L, std::atol(e)) << 20 : (size_t)16 << 30;
+  }();
+  return cap;
+}
+
+// Allocation sizes: powers of two up to 1 MiB, multiples of 2 MiB above, so blocks of similar plans fit.
+size_t size_class(size_t n) {
+  if (n <= ((size_t)1 << 20)) {
+    size_t c = 512;
+    while (c < n) c <<= 1;
+    return c;
+  }
+  const size_t g = (size_t)2 << 20;
+  return (n + g - 1) / g * g;
+}
+
+// Free every cached block of `dev` (all devices: -1); returns the bytes freed.
+size_t cache_trim(int dev) {
+  std::vector<CachedBlock> drop;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    std::vector<CachedBlock> keep;
+    for (const auto& b : g_cache) (dev < 0 || b.dev == dev ? drop : keep).push_back(b);
+    g_cache.swap(keep);
+    for (const auto& b : drop) g_cached -= b.bytes;
+  }
+  size_t freed = 0;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (const auto& b : drop) {
+    if (b.dev != cur) cudaSetDevice(b.dev);
+    cudaFree(b.p);
+    if (b.dev != cur) cudaSetDevice(cur);
+    freed += b.bytes;
+  }
+  return freed;
+}
+}  // namespace
+
+RecycleScope::RecycleScope() { ++g_recycle; }
+RecycleScope::~RecycleScope() { --g_recycle; }
+
+void device_release(void* p, size_t bytes, int dev) {
+  if (!g_recycle) {
+    cudaFree(p);
+    return;
+  }
+  std::vector<CachedBlock> drop;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    g_cache.push_back({p, bytes, dev});
+    g_cached += bytes;
+    while (g_cached > cache_cap() && !g_cache.empty()) {   // the oldest blocks go first
+      drop.push_back(g_cache.front());
+      g_cached -= g_cache.front().bytes;
+      g_cache.erase(g_cache.begin());
+    }
+  }
+  for (const auto& b : drop) cudaFree(b.p);   // blocks of this device: the caller's device is current
+}
+
 obte_status DevBuf::alloc(size_t n) {
   release();
   if (n == 0) n = 16;
-  cudaError_t e = cudaMalloc(&p, n);
+  const size_t want = size_class(n);
+  int d = 0;
+  OBTE_CUDA(cudaGetDevice(&d));
+  {
+    // best fit among the cached blocks of this device, at most 1/8 (or one 2 MiB step) larger
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    const size_t slack = std::max(want / 8, want > ((size_t)1 << 20) ? ((size_t)2 << 20) : (size_t)0);
+    int best = -1;
+    for (int i = 0; i < (int)g_cache.size(); ++i) {
+      const CachedBlock& b = g_cache[i];
+      if (b.dev == d && b.bytes >= want && b.bytes <= want + slack && (best < 0 || b.bytes < g_cache[best].bytes))
+        best = i;
+    }
+    if (best >= 0) {
+      p = g_cache[best].p;
+      bytes = g_cache[best].bytes;
+      dev = d;
+      g_cached -= bytes;
+      g_cache.erase(g_cache.begin() + best);
+      return OBTE_OK;
+    }
+  }
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e == cudaErrorMemoryAllocation && cache_trim(d) > 0) {
+    (void)cudaGetLastError();
+    e = cudaMalloc(&p, want);
+  }
   if (e != cudaSuccess) {
     p = nullptr;
     return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
   }
-  bytes = n;
+  bytes = want;
+  dev = d;
   return OBTE_OK;
+}
+
+namespace {
+std::vector<std::pair<void*, size_t>> g_host_cache;   // idle pinned blocks (guarded by g_cache_mu)
+constexpr size_t kHostCacheBlocks = 256;
+}  // namespace
+
+void host_release(void* p, size_t bytes) {
+  if (g_recycle) {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    if (g_host_cache.size() < kHostCacheBlocks) {
+      g_host_cache.emplace_back(p, bytes);
+      return;
+    }
+  }
+  cudaFreeHost(p);
 }
 
 obte_status HostBuf::alloc(size_t n) {
   release();
   if (n == 0) n = 16;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    for (size_t i = 0; i < g_host_cache.size(); ++i)
+      if (g_host_cache[i].second >= n && g_host_cache[i].second <= 4 * n + 4096) {
+        p = g_host_cache[i].first;
+        bytes = g_host_cache[i].second;
+        g_host_cache.erase(g_host_cache.begin() + i);
+        return OBTE_OK;
+      }
+  }
   cudaError_t e = cudaMallocHost(&p, n);
   if (e != cudaSuccess) {
     p = nullptr;
@@ -185,8 +316,28 @@ extern "C" obte_status obte_bte_plan_set_transmission(obte_plan plan, const doub
 }
 
 extern "C" obte_status obte_bte_plan_destroy(obte_plan plan) {
-  if (plan && plan->stream) cudaStreamSynchronize(plan->stream);
-  delete plan;
+  if (!plan) return OBTE_OK;
+  // every use of the plan's device buffers was on its stream: once it is idle they can be recycled
+  const bool idle = plan->ctx && cudaStreamSynchronize(plan->stream) == cudaSuccess;
+  if (idle) {
+    RecycleScope recycle;
+    delete plan;
+  } else {
+    delete plan;
+  }
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_device_cache_trim(int64_t* freed_bytes) {
+  const size_t f = cache_trim(-1);
+  if (freed_bytes) *freed_bytes = (int64_t)f;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_device_cache_bytes(int64_t* cached_bytes) {
+  if (!cached_bytes) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  *cached_bytes = (int64_t)g_cached;
   return OBTE_OK;
 }
 

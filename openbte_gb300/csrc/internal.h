@@ -95,15 +95,26 @@ struct PhaseTimer {
 };
 
 // ---- device buffer ------------------------------------------------------------
+// Device memory is taken from a library-wide cache of recycled blocks when one fits, else from cudaMalloc.
+// Blocks return to the cache only where the caller guarantees that no work still uses them (a plan being
+// destroyed after its stream was synchronised: RecycleScope); elsewhere release() calls cudaFree.  cudaFree
+// synchronises the whole device, which stalled every concurrent solve of a serving loop each time a
+// finished request's plan was dropped.
+void device_release(void* p, size_t bytes, int dev);
+struct RecycleScope {      // while alive on this thread, released device buffers go to the cache
+  RecycleScope();
+  ~RecycleScope();
+};
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  int dev = 0;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) device_release(p, bytes, dev);
     p = nullptr;
     bytes = 0;
   }
@@ -112,7 +123,9 @@ struct DevBuf {
   T* as() const { return static_cast<T*>(p); }
 };
 
-// Page-locked host buffer (the solver's small per-iteration device -> host reads).
+// Page-locked host buffer (the solver's small per-iteration device -> host reads).  Recycled like DevBuf
+// (cudaFreeHost synchronises the device as cudaFree does).
+void host_release(void* p, size_t bytes);
 struct HostBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -121,7 +134,7 @@ struct HostBuf {
   HostBuf& operator=(const HostBuf&) = delete;
   ~HostBuf() { release(); }
   void release() {
-    if (p) cudaFreeHost(p);
+    if (p) host_release(p, bytes);
     p = nullptr;
     bytes = 0;
   }

@@ -123,3 +123,34 @@ def test_concurrent_sweeps_with_different_footprints():
     for t in threads:
         t.join()
     assert not errors, errors
+
+
+def test_destroyed_plan_memory_is_recycled():
+    """A destroyed plan's device buffers go to the library's cache (no cudaFree, which would synchronise
+    the device under concurrent solves) and serve the next plan; trimming frees them."""
+    import ctypes as C
+    import gc
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.bte import solve_plan
+    from openbte_gb300.runtime import HostProblem, Plan
+    lib = _lib.load()
+    reqs = _requests()
+    cached = C.c_int64()
+    plan = Plan(HostProblem(reqs[1].geo, reqs[1].mat, reqs[1].bcs, reqs[1].ek))
+    dT0 = torch.zeros(plan.n, dtype=torch.float64, device="cuda")
+    k0 = solve_plan(plan, dT0, precision="fp32_refine", rtol=1e-8)[0].kappa_eff
+    del plan
+    gc.collect()
+    _lib.check(lib.obte_device_cache_bytes(C.byref(cached)), "cache bytes")
+    assert cached.value > 0
+    # the same problem again, on recycled memory: same kappa
+    plan = Plan(HostProblem(reqs[1].geo, reqs[1].mat, reqs[1].bcs, reqs[1].ek))
+    k1 = solve_plan(plan, dT0, precision="fp32_refine", rtol=1e-8)[0].kappa_eff
+    assert abs(k1 - k0) <= 1e-9 * abs(k0)
+    del plan
+    gc.collect()
+    freed = C.c_int64()
+    _lib.check(lib.obte_device_cache_trim(C.byref(freed)), "trim")
+    _lib.check(lib.obte_device_cache_bytes(C.byref(cached)), "cache bytes")
+    assert freed.value > 0 and cached.value == 0
