@@ -174,6 +174,9 @@ def run_serve(args, dev, world, rank, local):
     lib = _lib.load()
     n_req, rate = SERVE[args.workload]
     os.environ["OBTE_HOST_THREADS"] = str(args.host_threads)
+    # GPU-slot threads sleep while their solve runs instead of spinning on a core: the cores go to the
+    # threads that build and upload the next requests' plans
+    os.environ["OBTE_BLOCKING_SYNC"] = "1"
     pool = dict(device=local, slots=args.slots, builders=args.builders, preparers=args.preparers)
     t0 = time.time()
     reqs = serving_stream(n_req)
@@ -881,9 +884,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-rtol", type=float, default=1e-5,
                     help="serving stream: residual tolerance of each request (FP32+refine and one-at-a-time FP64)")
-    ap.add_argument("--slots", type=int, default=8, help="serving stream: concurrent GPU solves")
+    ap.add_argument("--slots", type=int, default=12, help="serving stream: concurrent GPU solves")
     ap.add_argument("--builders", type=int, default=8, help="serving stream: host threads building plans")
-    ap.add_argument("--preparers", type=int, default=6, help="serving stream: host threads uploading tables")
+    ap.add_argument("--preparers", type=int, default=8, help="serving stream: host threads uploading tables")
     ap.add_argument("--host-threads", type=int, default=2, help="serving stream: host threads per plan build")
     ap.add_argument("--fp64-subset-every", type=int, default=8,
                     help="serving stream: plain FP64 one at a time on every n-th request")
@@ -924,7 +927,8 @@ def main():
     if args.workload in SERVE:
         line = run_serve(args, dev, world, rank, local)
         if rank == 0:
-            res = run_resident(_resident_args(args), dev, 1, 0, local)
+            os.environ.pop("OBTE_BLOCKING_SYNC", None)
+        res = run_resident(_resident_args(args), dev, 1, 0, local)
             if res is not None:
                 line["roofline"] = dict(res["roofline"], workload="c1_60k_100x96 (resident plan)")
                 line["resident_c1"] = {k: res[k] for k in ("value", "ms_per_step", "latency_ms", "fp64",

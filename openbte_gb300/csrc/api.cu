@@ -24,6 +24,28 @@ obte_status cuda_fail(cudaError_t e, const char* what, const char* file, int lin
 
 void count_launch(int n) { g_launches += n; }
 
+cudaError_t wait_stream(cudaStream_t stream) {
+  const char* env = std::getenv("OBTE_BLOCKING_SYNC");   // read per call: a caller may switch modes between phases
+  const bool blocking = env && std::atoi(env) != 0;
+  if (!blocking) return cudaStreamSynchronize(stream);
+  // one blocking-sync event per thread and device, created on first use
+  thread_local std::vector<std::pair<int, cudaEvent_t>> events;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t ev = nullptr;
+  for (auto& de : events)
+    if (de.first == dev) ev = de.second;
+  if (!ev) {
+    e = cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
+    events.emplace_back(dev, ev);
+  }
+  e = cudaEventRecord(ev, stream);
+  if (e != cudaSuccess) return e;
+  return cudaEventSynchronize(ev);
+}
+
 // ---- recycled device blocks ---------------------------------------------------------------
 namespace {
 struct CachedBlock {
@@ -183,7 +205,7 @@ obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
   OBTE_TRY(b.alloc(std::max<size_t>(v.size(), 1) * sizeof(T)));
   if (!v.empty()) {
     OBTE_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
-    OBTE_CUDA(cudaStreamSynchronize(stream));
+    OBTE_CUDA(wait_stream(stream));
   }
   return OBTE_OK;
 }
@@ -191,7 +213,7 @@ obte_status upload_bytes(DevBuf& b, const void* p, size_t bytes, cudaStream_t st
   OBTE_TRY(b.alloc(std::max<size_t>(bytes, 1)));
   if (bytes) {
     OBTE_CUDA(cudaMemcpyAsync(b.p, p, bytes, cudaMemcpyHostToDevice, stream));
-    OBTE_CUDA(cudaStreamSynchronize(stream));
+    OBTE_CUDA(wait_stream(stream));
   }
   return OBTE_OK;
 }
@@ -318,7 +340,7 @@ extern "C" obte_status obte_bte_plan_set_transmission(obte_plan plan, const doub
 extern "C" obte_status obte_bte_plan_destroy(obte_plan plan) {
   if (!plan) return OBTE_OK;
   // every use of the plan's device buffers was on its stream: once it is idle they can be recycled
-  const bool idle = plan->ctx && cudaStreamSynchronize(plan->stream) == cudaSuccess;
+  const bool idle = plan->ctx && wait_stream(plan->stream) == cudaSuccess;
   if (idle) {
     RecycleScope recycle;
     delete plan;
@@ -344,7 +366,7 @@ extern "C" obte_status obte_device_cache_bytes(int64_t* cached_bytes) {
 extern "C" obte_status obte_bte_plan_set_stream(obte_plan plan, void* stream) {
   if (!plan || !plan->ctx) { set_error("null or host-only plan"); return OBTE_ERR_BAD_ARG; }
   // finish work issued on the previous stream before switching
-  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  OBTE_CUDA(wait_stream(plan->stream));
   plan->stream = static_cast<cudaStream_t>(stream);
   return OBTE_OK;
 }

@@ -39,6 +39,12 @@ obte_status cuda_fail(cudaError_t e, const char* what, const char* file, int lin
 // Count of kernel launches issued by this library (instrumentation for the bench).
 void count_launch(int n = 1);
 
+// Wait until `stream` has finished its work.  By default this is cudaStreamSynchronize, which spins on a
+// core while it waits; with OBTE_BLOCKING_SYNC=1 the calling thread sleeps on a blocking-sync event
+// instead (a serving loop with many GPU slots would otherwise keep one host core spinning per slot, taken
+// from the threads that build and upload the next requests' plans).
+cudaError_t wait_stream(cudaStream_t stream);
+
 // Host worker count: OBTE_HOST_THREADS, else the hardware concurrency (at most 32).
 inline int host_threads() {
   int t = (int)std::thread::hardware_concurrency();

@@ -429,7 +429,7 @@ struct Solver {
     OBTE_CUDA(cudaGetLastError());
     h.resize(kk);
     OBTE_CUDA(cudaMemcpyAsync(h.data(), wk.hdev.p, kk * sizeof(double), cudaMemcpyDeviceToHost, st));
-    OBTE_CUDA(cudaStreamSynchronize(st));
+    OBTE_CUDA(wait_stream(st));
     return OBTE_OK;
   }
   obte_status norm(const double* x, double& out) {
@@ -563,7 +563,7 @@ struct Solver {
         count_launch(11);
         OBTE_CUDA(cudaGetLastError());
         OBTE_CUDA(cudaMemcpyAsync(wk.hcol.p, cold, (size_t)(k + 2) * sizeof(double), cudaMemcpyDeviceToHost, st));
-        OBTE_CUDA(cudaStreamSynchronize(st));
+        OBTE_CUDA(wait_stream(st));
         const double hn = hc[k];
         for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hc[i];
         H[(size_t)(j + 1) * m + j] = hn;
@@ -699,7 +699,7 @@ struct Solver {
         count_launch(11);
         OBTE_CUDA(cudaGetLastError());
         OBTE_CUDA(cudaMemcpyAsync(wk.hcol.p, gsd.col, (size_t)(k + 2) * sizeof(double), cudaMemcpyDeviceToHost, st));
-        OBTE_CUDA(cudaStreamSynchronize(st));
+        OBTE_CUDA(wait_stream(st));
         const double hn = hc[k];
         // Hessenberg column j
         for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hc[i];
@@ -811,7 +811,7 @@ extern "C" obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const d
   // scratch for the final-pass outputs is not needed for a plain sweep
   OBTE_TRY(launch_sweep(plan, precision != OBTE_FP64, u_in, u_out, with_source != 0, false, nullptr, nullptr,
                         nullptr));
-  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  OBTE_CUDA(wait_stream(plan->stream));
   return check_device_error(plan);
 }
 
@@ -844,7 +844,7 @@ extern "C" obte_status obte_bte_plan_prepare(obte_plan plan, int32_t precision, 
     OBTE_TRY(wk.Kraw2.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
     OBTE_TRY(wk.Sraw2.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
   }
-  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  OBTE_CUDA(wait_stream(plan->stream));
   return OBTE_OK;
 }
 
@@ -997,10 +997,10 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   if (K) {
     std::vector<double> kh((size_t)s.n_mfp * s.n_dir);
     OBTE_CUDA(cudaMemcpyAsync(kh.data(), K, kh.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    OBTE_CUDA(cudaStreamSynchronize(st));
+    OBTE_CUDA(wait_stream(st));
     for (double v : kh) kappa += v;
   }
-  OBTE_CUDA(cudaStreamSynchronize(st));
+  OBTE_CUDA(wait_stream(st));
   OBTE_TRY(check_device_error(plan));
   plan->has_solution = true;
   if (info) {

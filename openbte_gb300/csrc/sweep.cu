@@ -1117,7 +1117,7 @@ static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) 
     }
   });
   OBTE_CUDA(cudaMemcpyAsync(d.rec.p, rec, d.h_rec.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-  OBTE_CUDA(cudaStreamSynchronize(st));
+  OBTE_CUDA(wait_stream(st));
   OBTE_TRY(upload_real<Real>(d.sr, sr, st));
   OBTE_CUDA(cudaMemcpy(d.Pq.p, s.P.data(), s.P.size() * sizeof(double), cudaMemcpyHostToDevice));
   OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
@@ -1282,7 +1282,7 @@ obte_status check_device_error(obte_plan plan) {
   if (!plan->err.p) return OBTE_OK;
   int h = 0;
   OBTE_CUDA(cudaMemcpyAsync(&h, plan->err.p, sizeof(int), cudaMemcpyDeviceToHost, plan->stream));
-  OBTE_CUDA(cudaStreamSynchronize(plan->stream));
+  OBTE_CUDA(wait_stream(plan->stream));
   if (h) {
     OBTE_CUDA(cudaMemsetAsync(plan->err.p, 0, sizeof(int), plan->stream));
     set_error("a device-side wait timed out in the sweep kernel");

@@ -250,7 +250,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   OBTE_CUDA(cudaGetLastError());
   std::vector<double> hn((size_t)nord * 2);
   OBTE_CUDA(cudaMemcpyAsync(hn.data(), nrm.p, hn.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-  OBTE_CUDA(cudaStreamSynchronize(st));
+  OBTE_CUDA(wait_stream(st));
   P.detect_sweeps = n_detect;
   struct Cand { int q, m; double ratio; std::vector<int32_t> slots; };
   std::vector<Cand> cand;
@@ -272,7 +272,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
     hx.resize((size_t)nsl * s.n_mfp);
     OBTE_CUDA(cudaMemcpyAsync(hx.data(), x + xoff + s.x_base[q] * s.n_mfp, hx.size() * sizeof(double),
                               cudaMemcpyDeviceToHost, st));
-    OBTE_CUDA(cudaStreamSynchronize(st));
+    OBTE_CUDA(wait_stream(st));
     for (int m : ms) {
       double vmax = 0;
       for (int64_t i = 0; i < nsl; ++i) vmax = std::max(vmax, hx[(size_t)i * s.n_mfp + m]);
@@ -374,7 +374,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   xprec_invert_kernel<<<nblk, 1024, 0, st>>>(P.bs.as<int32_t>(), P.bwoff.as<int64_t>(), P.W.as<float>(), bad.as<int>());
   count_launch();
   OBTE_CUDA(cudaGetLastError());
-  OBTE_CUDA(cudaStreamSynchronize(st));
+  OBTE_CUDA(wait_stream(st));
   OBTE_TRY(check_device_error(plan));
   P.nblk = nblk;
   P.smax = smax;
