@@ -684,7 +684,7 @@ def run_resident(args, dev, world, rank, local):
         u = torch.zeros(plan.nu, dtype=torch.float64, device=dev)
         uo = torch.zeros_like(u)
         ms = {}
-        for prec in ("fp32", "fp64"):
+        for prec in ("fp32", "fp64", "df"):
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
             for i in range(args.profile_sweeps):
                 if i == args.profile_sweeps // 2:
@@ -928,7 +928,7 @@ def main():
         line = run_serve(args, dev, world, rank, local)
         if rank == 0:
             os.environ.pop("OBTE_BLOCKING_SYNC", None)
-        res = run_resident(_resident_args(args), dev, 1, 0, local)
+            res = run_resident(_resident_args(args), dev, 1, 0, local)
             if res is not None:
                 line["roofline"] = dict(res["roofline"], workload="c1_60k_100x96 (resident plan)")
                 line["resident_c1"] = {k: res[k] for k in ("value", "ms_per_step", "latency_ms", "fp64",

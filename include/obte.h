@@ -43,8 +43,10 @@ typedef struct obte_context_s* obte_context;
 typedef struct obte_plan_s* obte_plan;
 typedef struct obte_fourier_plan_s* obte_fourier_plan;
 
-/* Sweep precision. */
-enum { OBTE_FP64 = 0, OBTE_FP32_REFINE = 1, OBTE_FP32 = 2 };
+/* Sweep precision.  OBTE_DOUBLE_FLOAT (sweeps only: obte_bte_sweep, obte_bte_sweep_fields) sweeps the FP64
+ * tables in double-float arithmetic, pairs of FP32 numbers with ~44 significant bits computed on the FP32
+ * pipe; it is the output pass of OBTE_FP32_REFINE solves. */
+enum { OBTE_FP64 = 0, OBTE_FP32_REFINE = 1, OBTE_FP32 = 2, OBTE_DOUBLE_FLOAT = 3 };
 
 /* Contact kinds for kappa_eff (openbte/bte.py:132-158). */
 enum { OBTE_CONTACT_NONE = 0, OBTE_CONTACT_PERIODIC = 1, OBTE_CONTACT_MIXED = 2, OBTE_CONTACT_NANOWIRE = 3 };
@@ -124,6 +126,7 @@ typedef struct {
   double residual;                /* final ‖F(u)-u‖/‖u‖ (FP64)                   */
   double offset;                  /* constant shift applied to match the reference's conserved offset */
   int32_t converged;
+  int32_t n_sweeps_df;            /* of which double-float output passes (FP32_REFINE, OBTE_REFINE_DF=1) */
 } obte_solve_info;
 
 /* ---- context ------------------------------------------------------------ */
@@ -202,7 +205,8 @@ obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opts, const do
                            double* dT, double* J, double* K, double* S, obte_solve_info* info);
 
 /*
- * One transport sweep of every ordinate — the per-ordinate solves
+ * One transport sweep of every ordinate (precision: OBTE_FP64, OBTE_FP32 / OBTE_FP32_REFINE or
+ * OBTE_DOUBLE_FLOAT) — the per-ordinate solves
  * A_mq T = B of openbte/bte.py:208-243 followed by the reduction of
  * openbte/objects.py:86-101 — at a given state.
  *   u_in   device [n_elems + n_diffuse + n_x]  (DeltaT, T_B, periodic inflow)
@@ -240,7 +244,8 @@ obte_status obte_bte_sweep_static(obte_plan plan, int32_t precision, const doubl
  * T_mq = A_mq^-1 B_mq of openbte/bte.py:217-218, which the reference keeps inside its worker processes
  * and returns only reduced (ΔT, J, K, S).  For checks of single ordinates against exact solves, or for
  * callers that want the phonon temperatures themselves.
- *   T  device [n_dir, n_elems, n_mfp]: float for OBTE_FP32 / OBTE_FP32_REFINE, double for OBTE_FP64
+ *   T  device [n_dir, n_elems, n_mfp]: float for OBTE_FP32 / OBTE_FP32_REFINE, double for OBTE_FP64 and
+ *      OBTE_DOUBLE_FLOAT
  * u_in, u_out and with_source as for obte_bte_sweep.
  */
 obte_status obte_bte_sweep_fields(obte_plan plan, int32_t precision, const double* u_in, double* u_out,

@@ -22,7 +22,7 @@ OBTE_ERR_NOT_CONVERGED = 4
 OBTE_ERR_UNSUPPORTED = 7
 OBTE_ERR_DEVICE_TIMEOUT = 8
 
-PRECISION = {"fp64": 0, "fp32_refine": 1, "fp32": 2}
+PRECISION = {"fp64": 0, "fp32_refine": 1, "fp32": 2, "df": 3}
 CONTACT_NONE, CONTACT_PERIODIC, CONTACT_MIXED, CONTACT_NANOWIRE = 0, 1, 2, 3
 
 p_i64 = C.POINTER(C.c_int64)
@@ -59,7 +59,8 @@ class SolveOpts(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("kappa_eff", C.c_double), ("n_sweeps", C.c_int32), ("n_sweeps_fp64", C.c_int32),
-                ("residual", C.c_double), ("offset", C.c_double), ("converged", C.c_int32)]
+                ("residual", C.c_double), ("offset", C.c_double), ("converged", C.c_int32),
+                ("n_sweeps_df", C.c_int32)]
 
 
 class FourierProblem(C.Structure):

@@ -97,6 +97,7 @@ def BTE_RTA(geo, mat, bcs, fourier=None, effective_thermal_conductivity=None, he
     variables = {"Temperature_BTE": {"data": dT.cpu().numpy(), "units": "K"},
                  "Flux_BTE": {"data": J.cpu().numpy() * 1e9, "units": "W/m/m"}}
     aux = {"suppression": S.cpu().numpy(), "kappa_eff": kappa_eff, "kappa_mode": K_h,
-           "n_sweeps": info.n_sweeps, "n_sweeps_fp64": info.n_sweeps_fp64, "residual": info.residual,
+           "n_sweeps": info.n_sweeps, "n_sweeps_fp64": info.n_sweeps_fp64, "n_sweeps_df": info.n_sweeps_df,
+           "residual": info.residual,
            "converged": bool(info.converged), "precision": precision}
     return SolverResults(kappa_eff=kappa_eff, variables=variables, aux=aux)

@@ -447,26 +447,37 @@ extern "C" obte_status obte_bte_schedule_coefficients(obte_plan plan, int32_t q,
   return OBTE_OK;
 }
 
+namespace obte {
+obte_status ensure_fields_scratch(obte_plan plan) {
+  if (plan->fields_J.p) return OBTE_OK;
+  const Schedule& s = plan->sched;
+  OBTE_TRY(plan->fields_J.alloc((size_t)s.n * s.ds * sizeof(double)));
+  OBTE_TRY(plan->fields_K.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+  OBTE_TRY(plan->fields_S.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
+  return OBTE_OK;
+}
+}  // namespace obte
+
 extern "C" obte_status obte_bte_sweep_fields(obte_plan plan, int32_t precision, const double* u_in, double* u_out,
                                              int32_t with_source, void* T) {
   if (!plan || !u_in || !u_out || !T) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
   if (!plan->ctx) { set_error("host-only plan cannot sweep"); return OBTE_ERR_BAD_ARG; }
-  if (precision != OBTE_FP64 && precision != OBTE_FP32 && precision != OBTE_FP32_REFINE) {
+  if (precision != OBTE_FP64 && precision != OBTE_FP32 && precision != OBTE_FP32_REFINE &&
+      precision != OBTE_DOUBLE_FLOAT) {
     set_error("bad precision"); return OBTE_ERR_BAD_ARG;
   }
   if (plan->xstore) { set_error("a gradient solve is using the per-ordinate store"); return OBTE_ERR_BAD_ARG; }
-  const Schedule& s = plan->sched;
-  const bool fp32 = precision != OBTE_FP64;
+  const bool fp32 = precision == OBTE_FP32 || precision == OBTE_FP32_REFINE;
   // the final-pass kernel also accumulates J, K and S; they go to plan-owned buffers and are discarded
-  if (!plan->fields_J.p) {
-    OBTE_TRY(plan->fields_J.alloc((size_t)s.n * s.ds * sizeof(double)));
-    OBTE_TRY(plan->fields_K.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
-    OBTE_TRY(plan->fields_S.alloc((size_t)s.n_mfp * s.n_dir * sizeof(double)));
-  }
+  OBTE_TRY(ensure_fields_scratch(plan));
   if (fp32) plan->xstore = static_cast<float*>(T);
   else plan->xstore64 = static_cast<double*>(T);
-  const obte_status st = launch_sweep(plan, fp32, u_in, u_out, with_source != 0, true, plan->fields_J.as<double>(),
-                                      plan->fields_K.as<double>(), plan->fields_S.as<double>());
+  const obte_status st =
+      precision == OBTE_DOUBLE_FLOAT
+          ? launch_sweep_df(plan, u_in, u_out, with_source != 0, plan->fields_J.as<double>(), plan->fields_K.as<double>(),
+                            plan->fields_S.as<double>())
+          : launch_sweep(plan, fp32, u_in, u_out, with_source != 0, true, plan->fields_J.as<double>(),
+                         plan->fields_K.as<double>(), plan->fields_S.as<double>());
   plan->xstore = nullptr;
   plan->xstore64 = nullptr;
   OBTE_TRY(st);

@@ -387,6 +387,9 @@ namespace obte {
 obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* u_out, bool with_src,
                          bool final_pass, double* Jraw, double* K, double* S);
 obte_status ensure_tables(obte_plan plan, bool fp32);
+// The output pass (J, K, S accumulated) in double-float arithmetic on the FP64 tables (sweep.cu).
+obte_status launch_sweep_df(obte_plan plan, const double* u_in, double* u_out, bool with_src, double* Jraw,
+                            double* K, double* S);
 // After set_transmission: the coefficient words of the device tables that exist (bytes uploaded added to *bytes).
 obte_status refresh_tables(obte_plan plan, int64_t* bytes);
 // Digest of the packed sweep tables of one precision, built on the host.
@@ -396,5 +399,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk);
 // out[X blocks] += W in[X blocks] (fp32: FP32 accumulation, for stages with an FP32 Krylov basis)
 void xprec_add(obte_plan plan, const double* in, double* out, bool fp32);
 obte_status check_device_error(obte_plan plan);
+// Plan-owned J, K, S buffers for sweeps whose final-pass accumulations are discarded (api.cu).
+obte_status ensure_fields_scratch(obte_plan plan);
 int64_t solve_scratch_bytes(obte_plan plan, int restart);
 }  // namespace obte

@@ -375,7 +375,7 @@ using Work = SolveWork;
 struct Solver {
   obte_plan plan;
   Work& wk;
-  int sweeps = 0, sweeps64 = 0;
+  int sweeps = 0, sweeps64 = 0, sweeps_df = 0;
   int max_sweeps;
   cudaStream_t st;
 
@@ -418,6 +418,12 @@ struct Solver {
     if (!fp32) ++sweeps64;
     return launch_sweep(plan, fp32, in, out, src, fin, wk.Jraw.as<double>(), wk.Kraw.as<double>(),
                         wk.Sraw.as<double>());
+  }
+  // the output pass in double-float arithmetic (with source, J, K, S accumulated)
+  obte_status sweep_df(const double* in, double* out) {
+    ++sweeps;
+    ++sweeps_df;
+    return launch_sweep_df(plan, in, out, true, wk.Jraw.as<double>(), wk.Kraw.as<double>(), wk.Sraw.as<double>());
   }
   // h[0..k) = V[0..k)^T w (and h[k] = w.w when self), copied to host
   obte_status multidot(const double* V, int k, const double* w, std::vector<double>& h, bool self = false) {
@@ -808,9 +814,20 @@ extern "C" obte_status obte_bte_sweep(obte_plan plan, int32_t precision, const d
                                       int32_t with_source) {
   if (!plan || !u_in || !u_out) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
   if (!plan->ctx) { set_error("host-only plan cannot sweep"); return OBTE_ERR_BAD_ARG; }
-  // scratch for the final-pass outputs is not needed for a plain sweep
-  OBTE_TRY(launch_sweep(plan, precision != OBTE_FP64, u_in, u_out, with_source != 0, false, nullptr, nullptr,
-                        nullptr));
+  if (precision != OBTE_FP64 && precision != OBTE_FP32 && precision != OBTE_FP32_REFINE &&
+      precision != OBTE_DOUBLE_FLOAT) {
+    set_error("bad precision"); return OBTE_ERR_BAD_ARG;
+  }
+  if (precision == OBTE_DOUBLE_FLOAT) {
+    // the double-float kernel is an output pass: its J, K, S accumulations go to discarded plan scratch
+    OBTE_TRY(ensure_fields_scratch(plan));
+    OBTE_TRY(launch_sweep_df(plan, u_in, u_out, with_source != 0, plan->fields_J.as<double>(),
+                             plan->fields_K.as<double>(), plan->fields_S.as<double>()));
+  } else {
+    // scratch for the final-pass outputs is not needed for a plain sweep
+    OBTE_TRY(launch_sweep(plan, precision != OBTE_FP64, u_in, u_out, with_source != 0, false, nullptr, nullptr,
+                          nullptr));
+  }
   OBTE_CUDA(wait_stream(plan->stream));
   return check_device_error(plan);
 }
@@ -946,8 +963,20 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   }
   const int64_t nks = (int64_t)s.n_mfp * s.n_dir;
   bool full_pass = true;
+  // With OBTE_REFINE_DF=1, FP32_REFINE runs its full output passes in double-float arithmetic on the FP32 pipe
+  // (~44 significant bits: rounding about 1e-13 of the state, below the tolerances down to 1e-11 it
+  // certifies; a tighter tolerance and gradient solves keep the FP64 pass).  It is off by default: on GB300
+  // the double-float sweep measured slower than the FP64 one (60k triangles x 9,600 ordinates: 23.7 against
+  // 16.3 ms; 110k tetrahedra x 15,360: 153 against 62 ms): its chains of dependent FP32 operations cost the
+  // latency-bound sweep more than the FP64 pipe does.
+  const char* rdf = std::getenv("OBTE_REFINE_DF");
+  const bool df_pass = prec == OBTE_FP32_REFINE && plan->xstore == nullptr && rtol >= 1e-11 &&
+                       rdf && std::atoi(rdf) != 0;
   for (int k = 0;; ++k) {
-    if (full_pass) OBTE_TRY(sv.sweep(fin32, u, Fu, true, true));
+    if (full_pass) {
+      if (df_pass) OBTE_TRY(sv.sweep_df(u, Fu));
+      else OBTE_TRY(sv.sweep(fin32, u, Fu, true, true));
+    }
     OBTE_TRY(sv.lincomb(1.0, Fu, -1.0, u, r));
     double rn;
     OBTE_TRY(sv.norm(r, rn));
@@ -1007,6 +1036,7 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
     info->kappa_eff = kappa;
     info->n_sweeps = sv.sweeps;
     info->n_sweeps_fp64 = sv.sweeps64;
+    info->n_sweeps_df = sv.sweeps_df;
     info->residual = res;
     info->offset = c;
     info->converged = ok ? 1 : 0;

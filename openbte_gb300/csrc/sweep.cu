@@ -501,6 +501,65 @@ __device__ __forceinline__ double quot(double num, double den) {
   return fma(fma(-den, t, num), r, t);
 }
 
+// ---- double-float arithmetic (the output pass of the FP32+refine solve) ----------------------------
+// A value is an unevaluated pair hi + lo of FP32 numbers (~44 significant bits), computed on the FP32 pipe
+// with error-free transformations: Knuth's two-sum, the FMA two-product (Dekker 1971; Ogita, Rump and
+// Oishi 2005), here on two MFPs at once with Blackwell's packed FP32x2 instructions.  The intrinsics round
+// every operation and are never contracted, which these transformations rely on.  In the ring and the
+// per-thread registers a pair lives in the 8 bytes of a double: low word hi, high word lo.
+struct df2 {
+  float2 h, l;   // hi and lo parts of two MFPs' values
+};
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __fadd2_rn(a, f2neg(b)); }
+__device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
+  const float2 s = __fadd2_rn(a, b);
+  const float2 bb = f2sub(s, a);
+  return {s, __fadd2_rn(f2sub(a, f2sub(s, bb)), f2sub(b, bb))};
+}
+__device__ __forceinline__ df2 fast_two_sum2(float2 a, float2 b) {   // |a| >= |b| (or a exact)
+  const float2 s = __fadd2_rn(a, b);
+  return {s, f2sub(b, f2sub(s, a))};
+}
+__device__ __forceinline__ df2 dadd2(df2 a, df2 b) {
+  const df2 s = two_sum2(a.h, b.h);
+  return fast_two_sum2(s.h, __fadd2_rn(s.l, __fadd2_rn(a.l, b.l)));
+}
+__device__ __forceinline__ df2 dneg2(df2 a) { return {f2neg(a.h), f2neg(a.l)}; }
+__device__ __forceinline__ df2 dmul2(df2 a, df2 b) {
+  const float2 p = __fmul2_rn(a.h, b.h);
+  float2 e = __ffma2_rn(a.h, b.h, f2neg(p));
+  e = __ffma2_rn(a.h, b.l, e);
+  e = __ffma2_rn(a.l, b.h, e);
+  return fast_two_sum2(p, e);
+}
+// a / b: an FP32 reciprocal seed y, the quotient q = a y and one correction by the residual a - q b
+__device__ __forceinline__ df2 ddiv2(df2 a, df2 b) {
+  const float2 y = make_float2(__fdividef(1.0f, b.h.x), __fdividef(1.0f, b.h.y));
+  const float2 q = __fmul2_rn(a.h, y);
+  float2 r = __ffma2_rn(f2neg(q), b.h, a.h);
+  r = __fadd2_rn(r, a.l);
+  r = __ffma2_rn(f2neg(q), b.l, r);
+  return fast_two_sum2(q, __fmul2_rn(r, y));
+}
+// split a double into hi + lo (FP64 pipe: two conversions and a subtraction)
+__device__ __forceinline__ float2 dsplit(double d) {
+  const float h = __double2float_rn(d);
+  return make_float2(h, __double2float_rn(d - (double)h));
+}
+__device__ __forceinline__ df2 dbcast(double d) {   // the same value in both lanes
+  const float2 s = dsplit(d);
+  return {make_float2(s.x, s.x), make_float2(s.y, s.y)};
+}
+__device__ __forceinline__ double dpack(float h, float l) { return __hiloint2double(__float_as_int(l), __float_as_int(h)); }
+__device__ __forceinline__ double dpack_split(double d) { const float2 s = dsplit(d); return dpack(s.x, s.y); }
+__device__ __forceinline__ float dpack_hi(double x) { return __int_as_float(__double2loint(x)); }
+__device__ __forceinline__ float dpack_lo(double x) { return __int_as_float(__double2hiint(x)); }
+__device__ __forceinline__ double dpack_value(double x) { return (double)dpack_hi(x) + (double)dpack_lo(x); }
+__device__ __forceinline__ df2 dunpack2(double a, double b) {   // two packed pairs -> lanes x, y
+  return {make_float2(dpack_hi(a), dpack_hi(b)), make_float2(dpack_lo(a), dpack_lo(b))};
+}
+
 // Shared memory layout (bytes):
 //   [0,64) mbarriers  [64,128) unused
 //   [128, ...) nbuf x records | nbuf x values | nbuf x wall weights | nbuf x prefetch lists | sig | K S | ring
@@ -595,8 +654,10 @@ struct SweepMinBlocks { static constexpr int v = (sizeof(Real) == 4 && G == 1 &&
 template <int G>
 struct Issuer { static constexpr int tid = kUnit * G - 32; };
 
-template <typename Real, int NF, int G, int KV, bool FINAL>
+// DF (Real = double, FINAL only): the FP64 tables swept in double-float arithmetic (see df2).
+template <typename Real, int NF, int G, int KV, bool FINAL, bool DF = false>
 __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte_sweep_kernel(const SweepParams<Real> p) {
+  static_assert(!DF || (sizeof(Real) == 8 && FINAL && KV % 2 == 0), "double-float sweeps: FP64 tables, output pass");
   constexpr int RW = Rec<Real, NF>::W;           // record words
   constexpr int MC = G * KV;                     // MFPs per CTA
   constexpr int VB = 2 * sizeof(Real);           // bytes of one (b, p) pair
@@ -659,7 +720,24 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
   Real* s_sig = reinterpret_cast<Real*>(smem + L.sig);
   for (int i = tid; i < MC * 3; i += blockDim.x) {
     const int jj = i / 3, d = i - 3 * jj;
-    s_sig[i] = (jj < mc && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m0 + jj) * p.ds + d] : Real(0);
+    const Real sv = (jj < mc && d < p.ds) ? p.sig[((int64_t)q * p.m_pad + m0 + jj) * p.ds + d] : Real(0);
+    if constexpr (DF) s_sig[i] = dpack_split(sv);   // packed hi / lo pairs
+    else s_sig[i] = sv;
+  }
+  // real value of a shared sigma entry (DF keeps them as packed pairs)
+  auto sigv = [&](Real x) -> Real {
+    if constexpr (DF) return dpack_value(x);
+    else return x;
+  };
+  // DF: this lane's MFPs and weights as pairs (lanes x, y = MFPs j, j + 1)
+  df2 lam2[DF ? KV / 2 : 1], tt2[DF ? KV / 2 : 1];
+  if constexpr (DF) {
+#pragma unroll
+    for (int j = 0; j < KV; j += 2) {
+      const float2 l0 = dsplit(lam[j]), l1 = dsplit(lam[j + 1]), t0 = dsplit(tt[j]), t1 = dsplit(tt[j + 1]);
+      lam2[j / 2] = {make_float2(l0.x, l1.x), make_float2(l0.y, l1.y)};
+      tt2[j / 2] = {make_float2(t0.x, t1.x), make_float2(t0.y, t1.y)};
+    }
   }
   if (FINAL)
     for (int j = tid; j < MC; j += blockDim.x) { s_k[j] = 0; s_s[j] = 0; }
@@ -673,7 +751,8 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
       const int k = p.pf[kpf[0] + j];
       if (k >= 0) v = (Real)X[(xq + k) * p.n_mfp + m0 + col];
     }
-    ring[i] = v;
+    if constexpr (DF) ring[i] = dpack_split(v);
+    else ring[i] = v;
   }
   if (tid == 0) {
     for (int i = 0; i < nbuf; ++i) mbar_init(&bars[i], 1);
@@ -776,7 +855,41 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
         if (NF > 3) vload(ring + s3 * MC + mo, v3);
         Real T[KV];
         Real dacc = 0, j0 = 0, j1 = 0, j2 = 0;
-        if constexpr (sizeof(Real) == 4 && KV % 2 == 0) {
+        if constexpr (DF) {
+          // output pass in double-float: the ring holds packed pairs, every product and sum is a pair
+          const df2 C0 = dbcast(c0), C1 = dbcast(c1), C2 = dbcast(c2), C3 = dbcast(c3), DD = dbcast(D);
+          const df2 BB = dbcast(b), PW = dbcast(pw);
+          const df2 ONE = {make_float2(1.0f, 1.0f), make_float2(0.0f, 0.0f)};
+          df2 da = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)}, ja = da, jb = da, jc = da;
+          Real Tp[KV];
+#pragma unroll
+          for (int j = 0; j < KV; j += 2) {
+            df2 sm = dmul2(C0, dunpack2(v0[j], v0[j + 1]));
+            sm = dadd2(sm, dmul2(C1, dunpack2(v1[j], v1[j + 1])));
+            sm = dadd2(sm, dmul2(C2, dunpack2(v2[j], v2[j + 1])));
+            if (NF > 3) sm = dadd2(sm, dmul2(C3, dunpack2(v3[j], v3[j + 1])));
+            const df2 LM = lam2[j / 2];
+            const df2 num = dadd2(BB, dmul2(LM, dadd2(PW, dneg2(sm))));   // b + L (pw - sm)
+            const df2 den = dadd2(ONE, dmul2(LM, DD));                    // 1 + L D
+            const df2 t2 = ddiv2(num, den);
+            Tp[j] = dpack(t2.h.x, t2.l.x);
+            Tp[j + 1] = dpack(t2.h.y, t2.l.y);
+            da = dadd2(da, dmul2(tt2[j / 2], t2));
+            const Real* sj = s_sig + (mo + j) * 3;   // packed sigma of MFPs j (sj[0..2]) and j + 1 (sj[3..5])
+            ja = dadd2(ja, dmul2(dunpack2(sj[0], sj[3]), t2));
+            jb = dadd2(jb, dmul2(dunpack2(sj[1], sj[4]), t2));
+            if (p.ds > 2) jc = dadd2(jc, dmul2(dunpack2(sj[2], sj[5]), t2));
+          }
+          dacc = ((double)da.h.x + (double)da.h.y) + ((double)da.l.x + (double)da.l.y);
+          j0 = ((double)ja.h.x + (double)ja.h.y) + ((double)ja.l.x + (double)ja.l.y);
+          j1 = ((double)jb.h.x + (double)jb.h.y) + ((double)jb.l.x + (double)jb.l.y);
+          j2 = ((double)jc.h.x + (double)jc.h.y) + ((double)jc.l.x + (double)jc.l.y);
+          vstore(ring + so * MC + mo, Tp);
+          // real values for the per-MFP outputs below (periodic outflow, walls, contact, stored fields)
+          const bool need = sp != 0 || p.Xs != nullptr || p.Xd != nullptr;
+#pragma unroll
+          for (int j = 0; j < KV; ++j) T[j] = need ? dpack_value(Tp[j]) : Real(0);
+        } else if constexpr (sizeof(Real) == 4 && KV % 2 == 0) {
           // FP32: the MFPs in pairs with Blackwell's packed FP32x2 arithmetic (one instruction per two MFPs;
           // each lane of a packed operation rounds like the scalar one)
           const float2 C0 = make_float2(c0, c0), C1 = make_float2(c1, c1), C2 = make_float2(c2, c2);
@@ -822,7 +935,7 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
             }
           }
         }
-        vstore(ring + so * MC + mo, T);
+        if constexpr (!DF) vstore(ring + so * MC + mo, T);
         if (FINAL && p.Xs != nullptr) {
 #pragma unroll
           for (int j = 0; j < KV; ++j)
@@ -862,9 +975,10 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
 #pragma unroll
           for (int j = 0; j < KV; ++j) {
             const Real* sj = s_sig + (mo + j) * 3;
-            const Real a0 = sj[0] * gw[0] + sj[1] * gw[1] + sj[2] * gw[2];
-            const Real a1 = sj[0] * gw1[0] + sj[1] * gw1[1] + sj[2] * gw1[2];
-            const Real a2 = sj[0] * gw2[0] + sj[1] * gw2[1] + sj[2] * gw2[2];
+            const Real s0r = sigv(sj[0]), s1r = sigv(sj[1]), s2r = sigv(sj[2]);
+            const Real a0 = s0r * gw[0] + s1r * gw[1] + s2r * gw[2];
+            const Real a1 = s0r * gw1[0] + s1r * gw1[1] + s2r * gw1[2];
+            const Real a2 = s0r * gw2[0] + s1r * gw2[1] + s2r * gw2[2];
             w0 += (a0 > Real(0) ? a0 * gw[3] : Real(0)) * T[j];
             w1 += (a1 > Real(0) ? a1 * gw1[3] : Real(0)) * T[j];
             w2 += (a2 > Real(0) ? a2 * gw2[3] : Real(0)) * T[j];
@@ -892,14 +1006,21 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
       if (pk >= 0) {
         Real xr[KV];
 #pragma unroll
-        for (int j = 0; j < KV; ++j) xr[j] = (Real)xv[j];
+        for (int j = 0; j < KV; ++j) {
+          if constexpr (DF) xr[j] = dpack_split(xv[j]);
+          else xr[j] = (Real)xv[j];
+        }
         vstore(ring + (prow_next + pf_i) * MC + mo, xr);
       }
       for (int i = pf_i + kUnit; i < npf; i += kUnit) {   // units with more than kUnit cut inflow faces
         const int k = s_pf[i];
         if (k < 0) continue;
         const double* xs = X + (xq + k) * p.n_mfp + m0 + mo;
-        for (int j = 0; j < KV; ++j) ring[(size_t)(prow_next + i) * MC + mo + j] = mo + j < mc ? (Real)xs[j] : Real(0);
+        for (int j = 0; j < KV; ++j) {
+          const Real xval = mo + j < mc ? (Real)xs[j] : Real(0);
+          if constexpr (DF) ring[(size_t)(prow_next + i) * MC + mo + j] = dpack_split(xval);
+          else ring[(size_t)(prow_next + i) * MC + mo + j] = xval;
+        }
       }
     }
     // block barrier that also tells every thread whether any wait of this unit gave up
@@ -1195,11 +1316,22 @@ obte_status ensure_tables(obte_plan plan, bool fp32) {
 
 // ---- launch -----------------------------------------------------------------------
 
-template <typename Real, int NF, int G, int KV, bool FINAL>
+template <typename Real, int NF, int G, int KV, bool FINAL, bool DF = false>
 static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                bool with_src, double* Jraw, double* K, double* S) {
   const Schedule& s = plan->sched;
   cudaStream_t st = plan->stream;
+  // the double-float pass chunks the MFPs by its own thread shape (G KV per CTA), not by the tables'
+  int n_chunks = d.n_chunks;
+  size_t smem = d.smem;
+  if (DF) {
+    n_chunks = (s.n_mfp + G * KV - 1) / (G * KV);
+    smem = SmemLayout<Real>(s.nf, G * KV, d.rows, d.unit_wo, d.pf_pad, d.unit_sx, d.nbuf).total;
+    if (smem > plan->ctx->smem_optin) {
+      set_error("the double-float sweep front needs more shared memory than one CTA can have");
+      return OBTE_ERR_UNSUPPORTED;
+    }
+  }
   const int64_t total = (int64_t)s.n_dir * s.n;
   const int vblocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)plan->ctx->num_sms * 8);
   sweep_values_kernel<Real><<<vblocks, 256, 0, st>>>(
@@ -1208,13 +1340,13 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
       d.vals.as<Real>());
   count_launch();
   OBTE_CUDA(cudaGetLastError());
-  auto kern = bte_sweep_kernel<Real, NF, G, KV, FINAL>;
+  auto kern = bte_sweep_kernel<Real, NF, G, KV, FINAL, DF>;
   // the limit is per kernel, shared by every plan and thread: always the device maximum, so concurrent
   // plans with different footprints cannot lower it under each other's launches
   OBTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan->ctx->smem_optin));
   SweepParams<Real> p;
   p.n = s.n; p.nd = s.nd; p.n_mfp = s.n_mfp; p.n_dir = s.n_dir; p.ds = s.ds; p.m_pad = s.m_pad;
-  p.n_chunks = d.n_chunks; p.rows = d.rows; p.S = s.max_slots;
+  p.n_chunks = n_chunks; p.rows = d.rows; p.S = s.max_slots;
   p.emax = d.emax; p.unit_wo = d.unit_wo; p.pf_pad = d.pf_pad; p.nbuf = d.nbuf;
   p.rec = d.rec.as<int32_t>(); p.vals = d.vals.as<Real>();
   p.lev_ptr = d.klev_ptr.as<int32_t>(); p.lev_off = d.klev_off.as<int64_t>(); p.nlev = d.knlev.as<int32_t>();
@@ -1233,12 +1365,13 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.wait_limit = plan->test_wait_limit > 0 ? plan->test_wait_limit : kWaitPolls;
   const bool subset = !FINAL && plan->sweep_cta_map != nullptr;
   static const bool index_order = std::getenv("OBTE_SWEEP_NO_LPT") != nullptr;   // plain index order
-  p.cta_map = subset ? plan->sweep_cta_map : (index_order ? nullptr : d.lpt.as<int32_t>());
+  // (the double-float pass runs in index order: the launch order table belongs to the tables' chunking)
+  p.cta_map = subset ? plan->sweep_cta_map : (index_order || DF ? nullptr : d.lpt.as<int32_t>());
   const int batch = subset && plan->sweep_batch > 1 ? plan->sweep_batch : 1;
   p.n_cta_batch = subset ? plan->sweep_n_cta : 0;
   p.batch_stride = batch > 1 ? plan->sweep_batch_stride : 0;
-  const int grid = subset ? plan->sweep_n_cta * batch : s.n_dir * d.n_chunks;
-  kern<<<grid, kUnit * G, d.smem, st>>>(p);
+  const int grid = subset ? plan->sweep_n_cta * batch : s.n_dir * n_chunks;
+  kern<<<grid, kUnit * G, smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
   return OBTE_OK;
@@ -1275,6 +1408,21 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
 #undef OBTE_W
   set_error("no compiled sweep kernel for this thread shape");
   return OBTE_ERR_UNSUPPORTED;
+}
+
+// The output pass in double-float arithmetic on the FP64 tables (J, K and S accumulated like a final pass).
+obte_status launch_sweep_df(obte_plan plan, const double* u_in, double* u_out, bool with_src, double* Jraw, double* K,
+                            double* S) {
+  OBTE_TRY(ensure_tables(plan, false));
+  const Schedule& s = plan->sched;
+  cudaStream_t st = plan->stream;
+  if (s.ds > 3) { set_error("sigma with more than 3 components"); return OBTE_ERR_UNSUPPORTED; }
+  if (s.nf > 4) { set_error("elements with more than 4 sides are not supported"); return OBTE_ERR_UNSUPPORTED; }
+  OBTE_CUDA(cudaMemsetAsync(u_out, 0, (size_t)(s.n + s.nd) * sizeof(double), st));
+  OBTE_CUDA(cudaMemsetAsync(Jraw, 0, (size_t)s.n * s.ds * sizeof(double), st));
+  const DevSchedule& d = plan->d64;
+  if (s.nf == 3) return launch_impl<double, 3, 1, 4, true, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
+  return launch_impl<double, 4, 1, 4, true, true>(plan, d, u_in, u_out, with_src, Jraw, K, S);
 }
 
 // Device error word: nonzero after a bounded wait gave up (cleared on read).

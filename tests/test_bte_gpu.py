@@ -34,7 +34,7 @@ def _state_from_exact(geo, mat, bcs, dT, TB):
     return out_T, out_B, np.concatenate(xs)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("fp32", 2e-5)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("df", 1e-11), ("fp32", 2e-5)])
 def test_sweep_equals_exact_ordinate_solves(case, precision, tol):
     import torch
     from openbte_gb300 import _lib
@@ -85,3 +85,45 @@ def test_bte_reduced_precision(case, precision, tol):
     assert err < tol, (precision, err, r.aux)
     T = r.variables["Temperature_BTE"]["data"]
     np.testing.assert_allclose(T, d["bte_T"], rtol=0, atol=10 * tol * np.abs(d["bte_T"]).max())
+
+
+@pytest.mark.parametrize("name", ["a600", "cube1k5", "gray600"])
+def test_double_float_sweep_equals_fp64_sweep(case, name):
+    """The double-float output pass (pairs of FP32 on the FP32 pipe) against the FP64 sweep on the same state:
+    every output within 1e-12 of the largest, on random states with and without the source."""
+    import ctypes as C
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.runtime import HostProblem, Plan
+    geo, mat, bcs, ek, d = case(name)
+    plan = Plan(HostProblem(geo, mat, bcs, ek))
+    rng = np.random.default_rng(4)
+    for src in (1, 0):
+        u = torch.tensor(rng.standard_normal(plan.nu), dtype=torch.float64, device="cuda")
+        outs = {}
+        for prec in ("fp64", "df"):
+            out = torch.zeros_like(u)
+            _lib.check(plan.lib.obte_bte_sweep(plan.handle, _lib.PRECISION[prec], C.c_void_p(u.data_ptr()),
+                                               C.c_void_p(out.data_ptr()), src), prec)
+            outs[prec] = out.cpu().numpy()
+        scale = np.abs(outs["fp64"]).max()
+        np.testing.assert_allclose(outs["df"], outs["fp64"], rtol=0, atol=1e-12 * scale)
+
+
+@pytest.mark.parametrize("double_float", [False, True])
+def test_fp32_refine_output_pass(case, monkeypatch, double_float):
+    """FP32+refine solves run their output pass in FP64, or with OBTE_REFINE_DF=1 in double-float arithmetic on
+    the FP32 pipe; either keeps the reference's kappa (golden c0_2k at bte_rtol 1e-12) to 1e-8."""
+    from openbte_gb300 import BTE_RTA
+    if double_float:
+        monkeypatch.setenv("OBTE_REFINE_DF", "1")
+    else:
+        monkeypatch.delenv("OBTE_REFINE_DF", raising=False)
+    geo, mat, bcs, ek, d = case("c0_2k")
+    f = O.SolverResults(variables={"Temperature_Fourier": {"data": d["fourier_T"]}})
+    r = BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-10, precision="fp32_refine")
+    if double_float:
+        assert r.aux["n_sweeps_df"] >= 1 and r.aux["n_sweeps_fp64"] == 0, r.aux
+    else:
+        assert r.aux["n_sweeps_fp64"] >= 1 and r.aux["n_sweeps_df"] == 0, r.aux
+    assert abs(r.kappa_eff - d["bte_kappa"]) / abs(d["bte_kappa"]) < 1e-8

@@ -12,8 +12,8 @@
   (fixtures from tests/golden/make_golden_scale.py): kappa within 1e-6, fields within 1e-6 of their maxima
   in FP64; kappa within 1e-4 in FP32+refine.
 
-Per-ordinate temperatures come from obte_bte_sweep_fields.  Tolerances: 1e-11 (FP64) and 2e-5 (FP32) of
-the largest sampled temperature, as in the small-mesh sweep tests.
+Per-ordinate temperatures come from obte_bte_sweep_fields.  Tolerances: 1e-11 (FP64, and the double-float
+output pass of FP32+refine) and 2e-5 (FP32) of the largest sampled temperature, as in the small-mesh sweep tests.
 """
 import ctypes as C
 
@@ -26,7 +26,7 @@ from openbte_gb300 import objects as O
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-11, "fp32": 2e-5}
+TOL = {"fp64": 1e-11, "df": 1e-11, "fp32": 2e-5}
 
 
 def _benchmark_2d():
@@ -85,7 +85,7 @@ def _sweep_fields(plan, precision, u):
     import torch
     from openbte_gb300 import _lib
     n_dir, n, n_mfp = plan.hp.n_dir, plan.n, plan.hp.n_mfp
-    T = torch.empty((n_dir, n, n_mfp), dtype=torch.float64 if precision == "fp64" else torch.float32, device="cuda")
+    T = torch.empty((n_dir, n, n_mfp), dtype=torch.float32 if precision == "fp32" else torch.float64, device="cuda")
     out = torch.zeros_like(u)
     _lib.check(plan.lib.obte_bte_sweep_fields(plan.handle, _lib.PRECISION[precision], C.c_void_p(u.data_ptr()),
                                               C.c_void_p(out.data_ptr()), 1, C.c_void_p(T.data_ptr())),
@@ -116,7 +116,7 @@ def exact_2d():
     return geo, mat, bcs, ek, st, x, exact
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "df", "fp32"])
 def test_benchmark_2d_sweep_equals_exact_ordinate_solves(exact_2d, precision):
     import torch
     from openbte_gb300.runtime import HostProblem, Plan
