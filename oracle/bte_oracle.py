@@ -262,9 +262,11 @@ def solve_ordinate(geo, mat, bcs, q, m, B):
     return s.solve(q, m, B)
 
 
-def _one_pass(ops, solver, mat, ct, dT, TB, with_source, hs=None):
+def _one_pass(ops, solver, mat, ct, dT, TB, with_source, hs=None, dirs=None):
     """The reference's per-ordinate solves and reductions at the state (DeltaT, T_B) (openbte/bte.py:199-249);
-    with_source=False leaves out the periodic-jump and heat sources (the linear part of the map)."""
+    with_source=False leaves out the periodic-jump and heat sources (the linear part of the map).  dirs: only
+    these directions (one worker's share of the ordinates, openbte/utils.py:209; the reductions are then
+    that worker's partial sums, which the reference adds over workers, openbte/objects.py:86-101)."""
     n = len(dT)
     mfps = np.asarray(mat.mfps, dtype=np.float64)
     t_coeff = np.asarray(mat.t_coeff)
@@ -276,7 +278,7 @@ def _one_pass(ops, solver, mat, ct, dT, TB, with_source, hs=None):
     pJ = np.zeros((n, np.asarray(mat.vmfp).shape[1]))
     pK = np.zeros((n_mfp, ops["n_angles"]))
     pS = np.zeros_like(pK)
-    for q in range(ops["n_angles"]):
+    for q in (range(ops["n_angles"]) if dirs is None else dirs):
         for m, mfp in enumerate(mfps):
             B = dT.copy()
             if with_source:
