@@ -149,6 +149,8 @@ obte_status obte_device_cache_bytes(int64_t* cached_bytes);
 const char* obte_last_error(void);
 /* Number of kernel launches this library issued in the calling process (instrumentation). */
 int64_t obte_launch_count(void);
+/* Bytes this library copied host -> device for plan tables in the calling process (instrumentation). */
+int64_t obte_h2d_bytes(void);
 
 /* ---- BTE_RTA (openbte/bte.py:19-271) ------------------------------------ */
 /*

@@ -94,6 +94,7 @@ SIGNATURES = [
     ("obte_status_string", C.c_char_p, [C.c_int]),
     ("obte_last_error", C.c_char_p, []),
     ("obte_launch_count", C.c_int64, []),
+    ("obte_h2d_bytes", C.c_int64, []),
     ("obte_device_cache_trim", C.c_int, [p_i64]),
     ("obte_device_cache_bytes", C.c_int, [p_i64]),
     ("obte_bte_plan_create", C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(MaterialC), C.POINTER(C.c_void_p)]),

@@ -12,6 +12,7 @@ namespace obte {
 
 static thread_local std::string g_last_error;
 static std::atomic<int64_t> g_launches{0};
+static std::atomic<int64_t> g_h2d{0};   // bytes the table uploads copied host -> device
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -206,6 +207,7 @@ obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
   if (!v.empty()) {
     OBTE_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
     OBTE_CUDA(wait_stream(stream));
+    g_h2d += (int64_t)(v.size() * sizeof(T));
   }
   return OBTE_OK;
 }
@@ -214,6 +216,7 @@ obte_status upload_bytes(DevBuf& b, const void* p, size_t bytes, cudaStream_t st
   if (bytes) {
     OBTE_CUDA(cudaMemcpyAsync(b.p, p, bytes, cudaMemcpyHostToDevice, stream));
     OBTE_CUDA(wait_stream(stream));
+    g_h2d += (int64_t)bytes;
   }
   return OBTE_OK;
 }
@@ -245,6 +248,8 @@ extern "C" const char* obte_status_string(int status) {
 extern "C" const char* obte_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" int64_t obte_launch_count(void) { return g_launches.load(); }
+
+extern "C" int64_t obte_h2d_bytes(void) { return g_h2d.load(); }
 
 extern "C" obte_status obte_context_create(int device, void* stream, obte_context* out) {
   if (!out) { set_error("null out"); return OBTE_ERR_BAD_ARG; }

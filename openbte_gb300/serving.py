@@ -97,7 +97,6 @@ class GPUBackend:
         self._cache: "collections.OrderedDict[str, Any]" = collections.OrderedDict()
         self._busy = collections.Counter()
         self._lock = threading.Lock()
-        self.uploaded_bytes = 0      # device table bytes uploaded by prepare (host -> device)
 
     def _stream(self):
         s = getattr(self._tl, "stream", None)
@@ -150,8 +149,6 @@ class GPUBackend:
         pl.set_stream(st.cuda_stream)
         pl.prepare(req.precision, self.restart)
         with self._lock:
-            if not pl.tables:
-                self.uploaded_bytes += pl.footprint(req.precision, self.restart)[0]
             pl.tables |= _TABLES[req.precision]
             pl.resident = max(pl.resident, self._footprint(pl, req))
 
