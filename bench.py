@@ -417,7 +417,10 @@ def run_inverse(args, dev):
     fields = [np.clip(rho + 0.1 * (density_field(n, seed + 1 + i) - 0.5), 0.0, 1.0)
               for i in range(args.warmup + args.steps)]
     mat = IsotropicMaterial.lognormal(n_mfp, n_dir)
-    solver = PixelSolver(n, mat, size=100.0, precision=args.precision, rtol=1e-8, restart=100)
+    # --warm-start: each field's solve starts from the previous field's solution, as the reference's design
+    # loop reuses its previous solution (openbte/inverse/bte.py:234-236)
+    solver = PixelSolver(n, mat, size=100.0, precision=args.precision, rtol=1e-8, restart=100,
+                         warm_start=args.warm_start)
     if args.profile_gradients:
         out = []
         for i in range(args.profile_gradients):
@@ -456,7 +459,8 @@ def run_inverse(args, dev):
                    "unknowns_per_sweep": n * n * n_mfp * n_dir, "precision": args.precision, "rtol": 1e-8,
                    "l2": "inputs and per-ordinate field (210 MB) larger than L2", "parallelism": "single",
                    "fields": "a new density field every step (base field + 0.1 x seeded field); one PixelSolver, "
-                             "its plan built once and its transmissions replaced per field"},
+                             "its plan built once and its transmissions replaced per field",
+                   "warm_start": bool(args.warm_start)},
         "kappa_eff": kaps[-1], "kappa_fp64": kap64, "kappa_rel_err_vs_fp64": abs(kaps[-1] - kap64) / abs(kap64),
         "sweeps_per_eval": float(np.median(sweeps)), "fp64_sweeps_per_eval": info.n_sweeps_fp64,
         "gradient_abs_max": float(np.abs(gh).max()),
@@ -503,6 +507,28 @@ def run_inverse(args, dev):
             "significant_pixels": int(len(pb)),
             "significant_max_rel_err": float(rel.max()), "significant_median_rel_err": float(np.median(rel)),
             "significant_vector_rel_err": float(np.linalg.norm(g0[pb] - fb) / np.linalg.norm(fb))}
+        # A pixel's density moves kappa by ~2 h g / kappa ~ 1e-7 relative at these steps (16,384 pixels share
+        # it), so a central difference at h amplifies the solves' error by 1e7; Richardson extrapolation of two
+        # larger steps, (4 fd(h1 / 2) - fd(h1)) / 3 with h1 = min(1e-2, rho / 30), cancels the h^2 truncation
+        # term while dividing the noise amplification by ~10.
+        def fd_h(pi, hp):
+            r1, r2 = rho.copy(), rho.copy()
+            r1[pi] += hp
+            r2[pi] -= hp
+            return (fd_solver.kappa_and_gradient(r1)[0] - fd_solver.kappa_and_gradient(r2)[0]) / (2 * hp)
+
+        okr = ok & (rho <= 1 - 1e-2)
+        pr = [pi for pi in pb if okr[pi]]
+        h1 = np.array([min(1e-2, rho[pi] / 30.0) for pi in pr])
+        f1 = np.array([fd_h(pi, h) for pi, h in zip(pr, h1)])
+        f2 = np.array([fd_h(pi, h / 2) for pi, h in zip(pr, h1)])
+        fr = (4 * f2 - f1) / 3
+        relr = np.abs(g0[pr] - fr) / np.abs(fr)
+        line["finite_difference_check"]["richardson"] = {
+            "h1": "min(1e-2, rho/30) and h1/2", "pixels": len(pr),
+            "max_rel_err": float(relr.max()), "median_rel_err": float(np.median(relr)),
+            "vector_rel_err": float(np.linalg.norm(g0[pr] - fr) / np.linalg.norm(fr)),
+            "max_rel_err_fd_h1_half_alone": float((np.abs(g0[pr] - f2) / np.abs(f2)).max())}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_inverse(n, n_mfp, n_dir)
     print(json.dumps(line))
@@ -892,6 +918,9 @@ def main():
     ap.add_argument("--host-threads", type=int, default=2, help="serving stream: host threads per plan build")
     ap.add_argument("--fp64-subset-every", type=int, default=8,
                     help="serving stream: plain FP64 one at a time on every n-th request")
+    ap.add_argument("--cold-start", dest="warm_start", action="store_false",
+                    help="config 4: start each density field's solve from zero instead of the previous field's "
+                         "solution (the default warm start is the reference design loop's own x0 reuse)")
     ap.add_argument("--fd-pixels", type=int, default=0,
                     help="config 4: also check dkappa/drho against central differences on this many pixels")
     ap.add_argument("--profile-sweeps", type=int, default=0,
