@@ -147,7 +147,7 @@ def serving_stream(n_req, seed=0, only=None):
     return reqs
 
 
-def serve_requests(reqs, precision, rtol, device, slots, builders, preparers, rate=None, seed=1):
+def serve_requests(reqs, precision, rtol, device, slots, builders, preparers, rate=None, seed=1, restart=30):
     """Replay `reqs` through a fresh server (Poisson arrivals at `rate`, None: all at once).
     Returns (results, wall seconds, server, backend)."""
     import torch
@@ -155,7 +155,7 @@ def serve_requests(reqs, precision, rtol, device, slots, builders, preparers, ra
     for r in reqs:
         r.precision = precision
         r.rtol = rtol
-    be = GPUBackend(device=device)
+    be = GPUBackend(device=device, restart=restart)
     srv = Server(backend=be, slots=slots, builders=builders, preparers=preparers)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
