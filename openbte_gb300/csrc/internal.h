@@ -306,6 +306,8 @@ struct DevSchedule {
   DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, sx, ksx, mfp, tco, sig, wo_wall, wo_geo, kcoef, scoef, hs, vals, cellmap,
       Pq, si, sr, wo_off, spec;
   DevBuf lpt;                              // launch order: CTAs of the directions with the most units first
+  // deterministic reductions (OBTE_DETERMINISTIC=1): per-(direction, chunk) partials and per-position sums
+  DevBuf det_d, det_j, det_w, det_k, det_s, det_S, det_SJ;
   // transmission plans: host copies of the packed records and of the special-entry index, so that new
   // transmissions rewrite the coefficient words in place (refresh_tables)
   RawVec<int32_t> h_rec, h_spec;
@@ -365,6 +367,10 @@ struct obte_plan_s {
   int64_t nx = 0;                   // periodic-inflow unknowns (source cells x n_mfp)
   int64_t nu = 0;                   // state length
   bool has_solution = false;        // work->u holds the last converged state
+  // deterministic reductions: position of element c in direction q's order [n_dir][n], wall -> wall-output
+  // entries (CSR, in entry order), first contact entry of each direction [n_dir + 1]
+  obte::DevBuf det_inv, det_wptr, det_went, det_ceoff;
+  int64_t det_nce = -1;             // contact entries (-1: tables not built)
   float* xstore = nullptr;          // set during a gradient solve: final-pass per-ordinate temperatures
   double* xstore64 = nullptr;       // set during obte_bte_sweep_fields in FP64: the same in FP64
   obte::DevBuf fields_J, fields_K, fields_S;   // final-pass outputs of obte_bte_sweep_fields (discarded)

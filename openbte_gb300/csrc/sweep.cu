@@ -477,6 +477,15 @@ struct SweepParams {
   // and the poll cap of the wait for a unit's copy (kWaitPolls normally)
   int skip_unit;
   int wait_limit;
+  // deterministic reductions (det != 0, full sweeps only): each (direction, chunk) CTA stores its partial sums
+  // instead of adding them atomically; fixed-order reduction kernels sum them afterwards
+  int det;
+  Real* __restrict__ dpart;   // [n_dir n_chunks][n] lattice-temperature partial of each sweep position
+  Real* __restrict__ jpart;   // [n_dir n_chunks][n][ds] flux partials (final pass)
+  Real* __restrict__ wpart;   // [n_chunks][n_wo] wall-output partials (wall-output entries of all directions)
+  Real* __restrict__ kpart;   // [n_ce][m_pad] kcoef T of each contact entry (final pass)
+  Real* __restrict__ spart;   // [n_ce][m_pad] scoef T
+  int64_t n_wo;
 };
 
 template <typename Real>
@@ -947,15 +956,25 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
             if (mo + j < mc) p.Xd[((int64_t)q * p.n + c) * p.n_mfp + m0 + mo + j] = (double)T[j];
         }
         dacc = group_sum<G>(dacc, gmask);
-        if (lane == 0) atomicAdd(&dT_out[c], (double)dacc);
+        if (lane == 0) {
+          if (p.det) p.dpart[(int64_t)cta * p.n + a + el] = dacc;
+          else atomicAdd(&dT_out[c], (double)dacc);
+        }
         if (FINAL) {
           j0 = group_sum<G>(j0, gmask);
           j1 = group_sum<G>(j1, gmask);
           j2 = group_sum<G>(j2, gmask);
           if (lane == 0) {
-            atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
-            if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
-            if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
+            if (p.det) {
+              Real* jp = p.jpart + ((int64_t)cta * p.n + a + el) * p.ds;
+              jp[0] = j0;
+              if (p.ds > 1) jp[1] = j1;
+              if (p.ds > 2) jp[2] = j2;
+            } else {
+              atomicAdd(&p.Jraw[(int64_t)c * p.ds], (double)j0);
+              if (p.ds > 1) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 1], (double)j1);
+              if (p.ds > 2) atomicAdd(&p.Jraw[(int64_t)c * p.ds + 2], (double)j2);
+            }
           }
         }
         // per-MFP outputs of special elements (the group is uniform in these conditions)
@@ -987,17 +1006,30 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
           if (wn > 1) w1 = group_sum<G>(w1, gmask);
           if (wn > 2) w2 = group_sum<G>(w2, gmask);
           if (lane == 0) {
-            atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
-            if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 1]], (double)w1);
-            if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 2]], (double)w2);
+            if (p.det) {
+              Real* wp = p.wpart + (int64_t)chunk * p.n_wo + wo0 + wb;
+              wp[0] = w0;
+              if (wn > 1) wp[1] = w1;
+              if (wn > 2) wp[2] = w2;
+            } else {
+              atomicAdd(&TB_out[p.wo_wall[wo0 + wb]], (double)w0);
+              if (wn > 1) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 1]], (double)w1);
+              if (wn > 2) atomicAdd(&TB_out[p.wo_wall[wo0 + wb + 2]], (double)w2);
+            }
           }
         }
         if (FINAL && ce >= 0) {
 #pragma unroll
           for (int j = 0; j < KV; ++j) {
             if (mo + j < mc) {
-              atomicAdd(&s_k[mo + j], p.kcoef[(int64_t)ce * p.m_pad + m0 + mo + j] * T[j]);
-              atomicAdd(&s_s[mo + j], p.scoef[ce] * T[j]);
+              const Real kv = p.kcoef[(int64_t)ce * p.m_pad + m0 + mo + j] * T[j], sv = p.scoef[ce] * T[j];
+              if (p.det) {
+                p.kpart[(int64_t)ce * p.m_pad + m0 + mo + j] = kv;
+                p.spart[(int64_t)ce * p.m_pad + m0 + mo + j] = sv;
+              } else {
+                atomicAdd(&s_k[mo + j], kv);
+                atomicAdd(&s_s[mo + j], sv);
+              }
             }
           }
         }
@@ -1038,11 +1070,87 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
     kpf1 = kpf2;
     kpf2 = kpf3;
   }
-  if (FINAL) {
+  if (FINAL && !p.det) {
     for (int j = tid; j < mc; j += blockDim.x) {
       p.K[(int64_t)(m0 + j) * p.n_dir + q] = (double)s_k[j];
       p.S_out[(int64_t)(m0 + j) * p.n_dir + q] = (double)s_s[j];
     }
+  }
+}
+
+// ---- deterministic reductions -------------------------------------------------------
+// Every sum below runs in a fixed order (chunks, then directions; a wall's entries in entry order; a
+// direction's contact entries in order), so the result does not depend on which CTA ran first.
+
+// S[q][pos] = sum over chunks of the lattice-temperature partials (and the flux partials)
+template <typename Real>
+__global__ void det_pos_sum_kernel(const Real* __restrict__ dpart, const Real* __restrict__ jpart, int n_chunks,
+                                   int64_t n, int64_t total, int ds, double* __restrict__ S, double* __restrict__ SJ) {
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < total; it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = it / n, pos = it - q * n;
+    const int64_t b0 = q * n_chunks * n + pos;
+    double acc = 0;
+    for (int ch = 0; ch < n_chunks; ++ch) acc += (double)dpart[b0 + (int64_t)ch * n];
+    S[it] = acc;
+    if (jpart)
+      for (int d = 0; d < ds; ++d) {
+        double aj = 0;
+        for (int ch = 0; ch < n_chunks; ++ch) aj += (double)jpart[(b0 + (int64_t)ch * n) * ds + d];
+        SJ[it * ds + d] = aj;
+      }
+  }
+}
+
+// element sums over the directions, through the position of the element in each direction's order
+__global__ void det_elem_sum_kernel(const double* __restrict__ S, const double* __restrict__ SJ,
+                                    const int32_t* __restrict__ inv, int n_dir, int64_t n, int ds,
+                                    double* __restrict__ dT_out, double* __restrict__ Jraw) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0, a0 = 0, a1 = 0, a2 = 0;
+    for (int q = 0; q < n_dir; ++q) {
+      const int64_t it = (int64_t)q * n + inv[(int64_t)q * n + c];
+      acc += S[it];
+      if (SJ) {
+        a0 += SJ[it * ds];
+        if (ds > 1) a1 += SJ[it * ds + 1];
+        if (ds > 2) a2 += SJ[it * ds + 2];
+      }
+    }
+    dT_out[c] = acc;
+    if (SJ) {
+      Jraw[c * ds] = a0;
+      if (ds > 1) Jraw[c * ds + 1] = a1;
+      if (ds > 2) Jraw[c * ds + 2] = a2;
+    }
+  }
+}
+
+template <typename Real>
+__global__ void det_wall_sum_kernel(const Real* __restrict__ wpart, int n_chunks, int64_t n_wo,
+                                    const int32_t* __restrict__ wptr, const int32_t* __restrict__ went, int64_t nd,
+                                    double* __restrict__ TB_out) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nd; w += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int k = wptr[w]; k < wptr[w + 1]; ++k)
+      for (int ch = 0; ch < n_chunks; ++ch) acc += (double)wpart[(int64_t)ch * n_wo + went[k]];
+    TB_out[w] = acc;
+  }
+}
+
+template <typename Real>
+__global__ void det_contact_sum_kernel(const Real* __restrict__ kpart, const Real* __restrict__ spart,
+                                       const int32_t* __restrict__ ce_off, int n_dir, int n_mfp, int m_pad,
+                                       double* __restrict__ K, double* __restrict__ S) {
+  const int64_t total = (int64_t)n_mfp * n_dir;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < total; it += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(it / n_dir), q = (int)(it - (int64_t)m * n_dir);
+    double ak = 0, as = 0;
+    for (int ce = ce_off[q]; ce < ce_off[q + 1]; ++ce) {
+      ak += (double)kpart[(int64_t)ce * m_pad + m];
+      as += (double)spart[(int64_t)ce * m_pad + m];
+    }
+    K[it] = ak;
+    S[it] = as;
   }
 }
 
@@ -1316,6 +1424,57 @@ obte_status ensure_tables(obte_plan plan, bool fp32) {
 
 // ---- launch -----------------------------------------------------------------------
 
+// Deterministic reductions requested (OBTE_DETERMINISTIC=1, read per call).
+static bool deterministic() {
+  const char* e = std::getenv("OBTE_DETERMINISTIC");
+  return e && std::atoi(e) != 0;
+}
+
+// Tables and partial buffers of the deterministic reductions (plan-level tables once, buffers per precision).
+template <typename Real>
+static obte_status ensure_det(obte_plan plan, DevSchedule& d) {
+  const Schedule& s = plan->sched;
+  cudaStream_t st = plan->stream;
+  const int64_t n = s.n, n_wo = (int64_t)s.wo_wall.size();
+  if (plan->det_nce < 0) {
+    std::vector<int32_t> inv((size_t)s.n_dir * n);
+    parallel_for(s.n_dir, [&](int64_t q) {
+      for (int64_t pos = 0; pos < n; ++pos) inv[(size_t)q * n + s.cell[(size_t)q * n + pos]] = (int32_t)pos;
+    });
+    std::vector<int32_t> wptr(s.nd + 1, 0), went(std::max<int64_t>(n_wo, 1), 0);
+    for (int64_t e = 0; e < n_wo; ++e) wptr[s.wo_wall[e] + 1]++;
+    for (int64_t w = 0; w < s.nd; ++w) wptr[w + 1] += wptr[w];
+    {
+      std::vector<int32_t> fill(wptr.begin(), wptr.end() - 1);
+      for (int64_t e = 0; e < n_wo; ++e) went[fill[s.wo_wall[e]]++] = (int32_t)e;   // entry order within a wall
+    }
+    std::vector<int32_t> ceoff(s.n_dir + 1, 0);
+    for (int q = 0; q < s.n_dir; ++q) {
+      int32_t cnt = 0;
+      for (int64_t pos = 0; pos < n; ++pos) cnt += s.contact[(size_t)q * n + pos] >= 0 ? 1 : 0;
+      ceoff[q + 1] = ceoff[q] + cnt;
+    }
+    OBTE_TRY(upload(plan->det_inv, inv, st));
+    OBTE_TRY(upload(plan->det_wptr, wptr, st));
+    OBTE_TRY(upload(plan->det_went, went, st));
+    OBTE_TRY(upload(plan->det_ceoff, ceoff, st));
+    plan->det_nce = ceoff[s.n_dir];
+  }
+  if (!d.det_d.p) {
+    const size_t parts = (size_t)s.n_dir * d.n_chunks * n;
+    OBTE_TRY(d.det_d.alloc(parts * sizeof(Real)));
+    OBTE_TRY(d.det_j.alloc(parts * s.ds * sizeof(Real)));
+    OBTE_TRY(d.det_w.alloc((size_t)std::max<int64_t>(n_wo, 1) * d.n_chunks * sizeof(Real)));
+    OBTE_TRY(d.det_k.alloc((size_t)std::max<int64_t>(plan->det_nce, 1) * s.m_pad * sizeof(Real)));
+    OBTE_TRY(d.det_s.alloc((size_t)std::max<int64_t>(plan->det_nce, 1) * s.m_pad * sizeof(Real)));
+    OBTE_TRY(d.det_S.alloc((size_t)s.n_dir * n * sizeof(double)));
+    OBTE_TRY(d.det_SJ.alloc((size_t)s.n_dir * n * s.ds * sizeof(double)));
+    // wall partials of entries a chunk does not reach (MFPs beyond n_mfp) stay zero
+    OBTE_CUDA(cudaMemsetAsync(d.det_w.p, 0, d.det_w.bytes, st));
+  }
+  return OBTE_OK;
+}
+
 template <typename Real, int NF, int G, int KV, bool FINAL, bool DF = false>
 static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const double* u_in, double* u_out,
                                bool with_src, double* Jraw, double* K, double* S) {
@@ -1364,6 +1523,20 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.skip_unit = plan->test_skip_unit;
   p.wait_limit = plan->test_wait_limit > 0 ? plan->test_wait_limit : kWaitPolls;
   const bool subset = !FINAL && plan->sweep_cta_map != nullptr;
+  // deterministic reductions: full sweeps of the FP32 and FP64 kernels (not the probes' subset sweeps, not the
+  // double-float pass)
+  const bool det = deterministic() && !subset && !DF;
+  p.det = det ? 1 : 0;
+  p.dpart = p.jpart = p.wpart = p.kpart = p.spart = nullptr;
+  p.n_wo = (int64_t)s.wo_wall.size();
+  if (det) {
+    OBTE_TRY(ensure_det<Real>(plan, const_cast<DevSchedule&>(d)));
+    p.dpart = d.det_d.as<Real>();
+    p.jpart = d.det_j.as<Real>();
+    p.wpart = d.det_w.as<Real>();
+    p.kpart = d.det_k.as<Real>();
+    p.spart = d.det_s.as<Real>();
+  }
   static const bool index_order = std::getenv("OBTE_SWEEP_NO_LPT") != nullptr;   // plain index order
   // (the double-float pass runs in index order: the launch order table belongs to the tables' chunking)
   p.cta_map = subset ? plan->sweep_cta_map : (index_order || DF ? nullptr : d.lpt.as<int32_t>());
@@ -1374,6 +1547,30 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   kern<<<grid, kUnit * G, smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());
+  if (det) {
+    const int nb = plan->ctx->num_sms * 8;
+    const int64_t total = (int64_t)s.n_dir * s.n;
+    det_pos_sum_kernel<Real><<<(int)std::min<int64_t>((total + 255) / 256, nb), 256, 0, st>>>(
+        d.det_d.as<Real>(), FINAL ? d.det_j.as<Real>() : nullptr, n_chunks, s.n, total, s.ds, d.det_S.as<double>(),
+        d.det_SJ.as<double>());
+    det_elem_sum_kernel<<<(int)std::min<int64_t>((s.n + 255) / 256, nb), 256, 0, st>>>(
+        d.det_S.as<double>(), FINAL ? d.det_SJ.as<double>() : nullptr, plan->det_inv.as<int32_t>(), s.n_dir, s.n, s.ds,
+        u_out, Jraw);
+    count_launch(2);
+    if (s.nd > 0) {
+      det_wall_sum_kernel<Real><<<(int)std::min<int64_t>((s.nd + 255) / 256, nb), 256, 0, st>>>(
+          d.det_w.as<Real>(), n_chunks, p.n_wo, plan->det_wptr.as<int32_t>(), plan->det_went.as<int32_t>(), s.nd,
+          u_out + s.n);
+      count_launch();
+    }
+    if (FINAL) {
+      const int64_t nk = (int64_t)s.n_mfp * s.n_dir;
+      det_contact_sum_kernel<Real><<<(int)std::min<int64_t>((nk + 255) / 256, nb), 256, 0, st>>>(
+          d.det_k.as<Real>(), d.det_s.as<Real>(), plan->det_ceoff.as<int32_t>(), s.n_dir, s.n_mfp, s.m_pad, K, S);
+      count_launch();
+    }
+    OBTE_CUDA(cudaGetLastError());
+  }
   return OBTE_OK;
 }
 
@@ -1522,6 +1719,9 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.batch_stride = 0;
   p.skip_unit = -1;
   p.wait_limit = kWaitPolls;
+  p.det = 0;
+  p.dpart = p.jpart = p.wpart = p.kpart = p.spart = nullptr;
+  p.n_wo = 0;
   kern<<<s.n_dir * d.n_chunks, kUnit * G, d.smem, st>>>(p);
   count_launch();
   OBTE_CUDA(cudaGetLastError());

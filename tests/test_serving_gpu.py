@@ -43,6 +43,28 @@ def test_same_alone_and_in_the_mix():
         assert rel < 1e-6, (res.rid, res.kappa, alone[res.rid])
 
 
+def test_same_alone_and_in_the_mix_bit_for_bit(monkeypatch):
+    """With deterministic reductions (OBTE_DETERMINISTIC=1) a served result does not depend on what else ran
+    on the GPU at the same time: alone and in the mix give the same kappa, bit for bit."""
+    from openbte_gb300.serving import GPUBackend, Server, replay
+    monkeypatch.setenv("OBTE_DETERMINISTIC", "1")
+    reqs = _requests()
+    alone = {}
+    srv = Server(backend=GPUBackend(), slots=1, builders=1)
+    for r in reqs:
+        res = replay(srv, [r])[0]
+        assert res.status == "ok", res.error
+        alone[r.rid] = res.kappa
+    srv.close()
+    srv = Server(backend=GPUBackend(), slots=4, builders=3)
+    mixed = replay(srv, reqs)
+    srv.close()
+    assert srv.max_concurrent >= 2
+    for res in mixed:
+        assert res.status == "ok", res.error
+        assert res.kappa == alone[res.rid], (res.rid, res.kappa, alone[res.rid])
+
+
 def test_served_kappa_matches_oracle():
     import bte_oracle
     from openbte_gb300.serving import GPUBackend, Server, replay
