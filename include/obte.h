@@ -279,12 +279,20 @@ obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_opts* opts,
 obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x);
 /*
  * Periodic-inflow preconditioner of the plan (no counterpart in the reference, whose per-ordinate
- * sparse LU solves the periodic coupling directly): built on the plan's first solve unless the
- * environment sets OBTE_XPREC=0.  n_blocks: ordinates it covers (0: none, or not built yet);
+ * sparse LU solves the periodic coupling directly): built when obte_solve_opts.precond asks for it (by
+ * default on the plan's second solve).  n_blocks: ordinates it covers (0: none, or not built yet);
  * setup_sweeps: FP32 sweeps its setup ran (detection and probing); setup_ms: host wall time of the
  * setup.  Any pointer may be null.
  */
 obte_status obte_bte_precond_info(obte_plan plan, int32_t* n_blocks, int32_t* setup_sweeps, double* setup_ms);
+/*
+ * Device memory of the plan's periodic-inflow preconditioner, for admission control: resident = bytes
+ * the built preconditioner holds (0 when none was built; obte_bte_plan_footprint's plan_bytes include
+ * them); build_bound = upper bound of the device bytes building it would allocate, resident blocks and
+ * transient probe vectors together (0 once a build was tried, when the plan has no periodic inflow a
+ * block could cover, or for a host-only plan).  Any pointer may be null.
+ */
+obte_status obte_bte_precond_bytes(obte_plan plan, int64_t* resident, int64_t* build_bound);
 /*
  * Sweep schedule of direction q, as built on the host (for bit-exact checks):
  *   order  host [n_elems]      element processed at each position

@@ -397,6 +397,7 @@ extern "C" obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision
   if (precision == OBTE_FP64) pb += t64;
   else if (precision == OBTE_FP32) pb += t32;
   else pb += t64 + t32;
+  pb += xprec_resident_bytes(plan->xprec.get());
   if (plan_bytes) *plan_bytes = pb;
   if (solve_bytes) *solve_bytes = plan->ctx ? solve_scratch_bytes(plan, restart > 0 ? restart : 30) : 0;
   return OBTE_OK;
@@ -417,6 +418,13 @@ extern "C" obte_status obte_bte_precond_info(obte_plan plan, int32_t* n_blocks, 
   if (n_blocks) *n_blocks = P ? P->nblk : 0;
   if (setup_sweeps) *setup_sweeps = P ? P->detect_sweeps + P->probe_sweeps : 0;
   if (setup_ms) *setup_ms = P ? P->setup_ms : 0.0;
+  return OBTE_OK;
+}
+
+extern "C" obte_status obte_bte_precond_bytes(obte_plan plan, int64_t* resident, int64_t* build_bound) {
+  if (!plan) { set_error("null plan"); return OBTE_ERR_BAD_ARG; }
+  if (resident) *resident = xprec_resident_bytes(plan->xprec.get());
+  if (build_bound) *build_bound = plan->ctx ? xprec_build_bound(plan) : 0;
   return OBTE_OK;
 }
 

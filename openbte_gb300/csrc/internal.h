@@ -404,6 +404,8 @@ obte_status tables_digest(obte_plan plan, bool fp32, uint64_t* digest);
 obte_status ensure_xprec(obte_plan plan, SolveWork& wk);
 // out[X blocks] += W in[X blocks] (fp32: FP32 accumulation, for stages with an FP32 Krylov basis)
 void xprec_add(obte_plan plan, const double* in, double* out, bool fp32);
+int64_t xprec_resident_bytes(const XPrec* P);
+int64_t xprec_build_bound(obte_plan plan);   // device bytes a build would allocate (0 once tried)
 obte_status check_device_error(obte_plan plan);
 // Plan-owned J, K, S buffers for sweeps whose final-pass accumulations are discarded (api.cu).
 obte_status ensure_fields_scratch(obte_plan plan);

@@ -198,6 +198,29 @@ void xprec_add(obte_plan plan, const double* in, double* out, bool fp32) {
   count_launch();
 }
 
+int64_t xprec_resident_bytes(const XPrec* P) {
+  if (!P) return 0;
+  return (int64_t)(P->bm.bytes + P->bs.bytes + P->boff.bytes + P->bwoff.bytes + P->bslot.bytes + P->W.bytes);
+}
+
+int64_t xprec_build_bound(obte_plan plan) {
+  if (plan->xprec && plan->xprec->tried) return 0;
+  const Schedule& s = plan->sched;
+  const int64_t nsrc = s.x_base.empty() ? 0 : s.x_base[s.n_dir];
+  bool any_fits = false;
+  for (int q = 0; q < s.n_dir && !any_fits; ++q) {
+    const int64_t nsl = s.x_base[q + 1] - s.x_base[q];
+    any_fits = nsl > 0 && nsl <= kMaxSlots;
+  }
+  if (nsrc == 0 || s.n_mfp == 0 || !any_fits) return 0;
+  const int64_t nord = (int64_t)s.n_dir * s.n_mfp;
+  const int64_t nu = plan->nu;
+  // W (capped), per-block tables (at most one block per ordinate, every block's slots at most its
+  // direction's), detection norms, CTA map, the batched probe vectors (16 pairs or 2 GB at most)
+  const int64_t probes = std::min<int64_t>(16 * 2 * nu * (int64_t)sizeof(double), (int64_t)2e9);
+  return (int64_t)kMaxBytes + nord * (4 + 4 + 8 + 8 + 4 + 16 + 4) + nsrc * s.n_mfp * 4 + probes;
+}
+
 obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   if (plan->xprec && plan->xprec->tried) return OBTE_OK;
   plan->xprec.reset(new XPrec());

@@ -227,6 +227,13 @@ class Plan:
                                                     C.byref(sb)), "footprint")
         return pb.value, sb.value
 
+    def precond_bytes(self):
+        """(bytes the built periodic-inflow preconditioner holds, upper bound of what building it would
+        allocate; 0 once a build was tried)"""
+        r, b = C.c_int64(), C.c_int64()
+        _lib.check(self.lib.obte_bte_precond_bytes(self.handle, C.byref(r), C.byref(b)), "precond_bytes")
+        return r.value, b.value
+
     def schedule(self, q):
         nl, ns = C.c_int64(), C.c_int64()
         _lib.check(self.lib.obte_bte_schedule(self.handle, q, None, None, C.byref(nl), C.byref(ns)), "schedule")

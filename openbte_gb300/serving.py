@@ -19,8 +19,9 @@ state resident and can warm-start from it; it also builds the periodic-inflow pr
 second solve, with the preconditioner's memory added to the plan's footprint.
 
 The scheduling logic talks to a backend with the calls ``build``, ``solve`` and ``release`` (and
-optionally ``prepare``, ``resident_bytes``, ``is_resident``, ``evict_idle``); :class:`GPUBackend` is the
-real one, tests plug a fake one to exercise admission and ordering without a GPU.
+optionally ``extra_bytes``, ``prepare``, ``resident_bytes``, ``evict_idle``, ``drop_optional``);
+:class:`GPUBackend` is the real one, tests plug a fake one to exercise admission and ordering without a
+GPU.
 """
 from __future__ import annotations
 
@@ -79,20 +80,38 @@ class Result:
 _TABLES = {"fp64": {"fp64"}, "fp32": {"fp32"}, "fp32_refine": {"fp32", "fp64"}}
 
 
+class _Lease:
+    """One request's hold on a cached plan: `use` counts the requests that took the plan before it."""
+
+    __slots__ = ("plan", "use", "bound", "builds_precond")
+
+    def __init__(self, plan, use):
+        self.plan = plan
+        self.use = use
+        self.bound = None             # device bytes this request's preconditioner build may take
+        self.builds_precond = False
+
+
 class GPUBackend:
     """Plans and solves on one CUDA device through the C ABI.
 
     Every plan the backend holds is in ``_cache`` (least recently used first): busy ones (a request is
     between build and release) and idle ones kept for repeated geometries.  ``resident_bytes`` is the
-    device memory of the prepared ones, which the server's admission counts."""
+    device memory of the prepared ones, which the server's admission counts.
 
-    def __init__(self, device=0, restart=30, max_sweeps=2000, cache_plans=8):
+    A repeated geometry builds the plan's periodic-inflow preconditioner: the plan's second request
+    (``precond_repeats``) reserves the build's upper bound (``Plan.precond_bytes``) at admission, builds it
+    during its solve, and the plan's resident bytes then include what the preconditioner keeps.  Requests
+    on one plan solve one at a time (a plan has one set of solver vectors)."""
+
+    def __init__(self, device=0, restart=30, max_sweeps=2000, cache_plans=8, precond_repeats=True):
         import torch
         self.torch = torch
         self.device = device
         self.restart = restart
         self.max_sweeps = max_sweeps
         self.cache_plans = cache_plans
+        self.precond_repeats = precond_repeats
         self._tl = threading.local()
         self._cache: "collections.OrderedDict[str, Any]" = collections.OrderedDict()
         self._busy = collections.Counter()
@@ -110,8 +129,8 @@ class GPUBackend:
         return int(free * fraction)
 
     def build(self, req: Request):
-        """Host part of a plan (the C++ schedule) or the cached plan -> (plan, footprint bytes, reused?)"""
-        from .runtime import HostProblem, Plan
+        """Host part of a plan (the C++ schedule) or the cached plan -> (lease, footprint bytes, reused?)"""
+        from .runtime import HostProblem
         hp = HostProblem(req.geo, req.mat, req.bcs, req.ek)
         key = hp.key()
         with self._lock:
@@ -119,60 +138,116 @@ class GPUBackend:
             if pl is not None:
                 self._cache.move_to_end(key)
                 self._busy[key] += 1
-                return pl, self._footprint(pl, req), True
-        st = self._stream()
-        with self.torch.cuda.stream(st):
-            pl = Plan(hp, self.device, stream=st.cuda_stream)
+                lease = _Lease(pl, pl.uses)
+                pl.uses += 1
+                return lease, self._footprint(pl, req), True
+        pl = self._new_plan(hp)
         pl.key = key
         pl.tables = set()        # table sets uploaded
-        pl.resident = 0          # device bytes once prepared
+        pl.resident = 0          # device bytes once prepared (tables, solver vectors, preconditioner)
+        pl.pending = 0           # reserved for a preconditioner build in progress
+        pl.uses = 1
+        pl.solve_lock = threading.Lock()
         with self._lock:
             self._cache[key] = pl
             self._busy[key] += 1
-        return pl, self._footprint(pl, req), False
+        return _Lease(pl, 0), self._footprint(pl, req), False
+
+    def _new_plan(self, hp):
+        from .runtime import Plan
+        st = self._stream()
+        with self.torch.cuda.stream(st):
+            return Plan(hp, self.device, stream=st.cuda_stream)
 
     def _footprint(self, pl, req):
         a, b = pl.footprint(req.precision, self.restart)
         return int(a + b)
 
-    def extra_bytes(self, pl, req) -> int:
-        """Device bytes that preparing `pl` for `req` adds (0 for a plan already prepared for it)."""
-        if _TABLES[req.precision] <= pl.tables:
-            return 0
-        return max(0, self._footprint(pl, req) - pl.resident)
+    def _precond_bound(self, lease) -> int:
+        """Device bytes the lease's solve may add by building the preconditioner (the plan's second use
+        builds it), fixed when first asked (at admission)."""
+        if lease.bound is None:
+            lease.bound = lease.plan.precond_bytes()[1] if self.precond_repeats and lease.use == 1 else 0
+        return lease.bound
 
-    def prepare(self, pl, req: Request):
-        """Upload the plan's device tables and allocate its solver scratch (host threads, before a slot)."""
-        if _TABLES[req.precision] <= pl.tables:
-            return
-        st = self._stream()
-        pl.set_stream(st.cuda_stream)
-        pl.prepare(req.precision, self.restart)
+    def extra_bytes(self, lease, req) -> int:
+        """Device bytes that preparing and solving `req` on the lease's plan adds (0 for a plan already
+        prepared for it, unless this solve builds the preconditioner)."""
+        pl = lease.plan
+        tables = 0 if _TABLES[req.precision] <= pl.tables else max(0, self._footprint(pl, req) - pl.resident)
+        return tables + self._precond_bound(lease)
+
+    def drop_optional(self, lease) -> bool:
+        """The lease's solve will not build the preconditioner (its bound does not fit); True if it was to."""
+        if self._precond_bound(lease):
+            lease.bound = 0
+            return True
+        return False
+
+    def prepare(self, lease, req: Request):
+        """Upload the plan's device tables and allocate its solver scratch (host threads, before a slot);
+        from here on the bytes the server reserved for the request count in ``resident_bytes``."""
+        pl = lease.plan
+        bound = self._precond_bound(lease)
+        if not _TABLES[req.precision] <= pl.tables:
+            with pl.solve_lock:          # not while another request solves on the plan
+                if not _TABLES[req.precision] <= pl.tables:
+                    self._prepare_plan(pl, req)
+                    with self._lock:
+                        pl.tables |= _TABLES[req.precision]
         with self._lock:
             pl.tables |= _TABLES[req.precision]
             pl.resident = max(pl.resident, self._footprint(pl, req))
+            if bound:
+                lease.builds_precond = True
+                pl.pending += bound
+
+    def _prepare_plan(self, pl, req):
+        st = self._stream()
+        pl.set_stream(st.cuda_stream)
+        pl.prepare(req.precision, self.restart)
 
     def resident_bytes(self) -> int:
         with self._lock:
-            return sum(pl.resident for pl in self._cache.values())
+            return sum(pl.resident + pl.pending for pl in self._cache.values())
 
-    def solve(self, pl, req: Request, slot: int) -> dict:
+    def _solve_plan(self, pl, req, precond):
+        """One solve of `pl` on this thread's stream, waited for -> SolveInfo."""
         from .bte import solve_plan
         torch = self.torch
         st = self._stream()
         pl.set_stream(st.cuda_stream)
         with torch.cuda.stream(st):
             dT0 = torch.zeros(pl.n, dtype=torch.float64, device=f"cuda:{self.device}")
-            # the periodic-inflow preconditioner stays off: its setup costs about as many sweeps as a solve
-            # saves, and a served request's plan is usually solved once
             info, *_ = solve_plan(pl, dT0, precision=req.precision, rtol=req.rtol, max_sweeps=self.max_sweeps,
-                                  restart=self.restart, warm_start=req.warm_start, precond=-1)
+                                  restart=self.restart, warm_start=req.warm_start, precond=precond)
         st.synchronize()
+        return info
+
+    def solve(self, lease, req: Request, slot: int) -> dict:
+        pl = lease.plan
+        # only the request that reserved the build's memory builds the preconditioner; the others use it
+        # once it exists (0: the default policy, whose build on a second solve has then been tried) and
+        # otherwise leave it off
+        with pl.solve_lock:
+            if lease.builds_precond:
+                precond = 1
+            else:
+                precond = 0 if pl.precond_bytes()[1] == 0 else -1
+            try:
+                info = self._solve_plan(pl, req, precond)
+            finally:
+                if lease.builds_precond:
+                    with self._lock:
+                        pl.pending -= lease.bound
+                        pl.resident = max(pl.resident, self._footprint(pl, req))
+                    lease.builds_precond = False
         return {"kappa": info.kappa_eff, "converged": bool(info.converged), "n_sweeps": info.n_sweeps,
                 "n_sweeps_fp64": info.n_sweeps_fp64}
 
-    def release(self, pl):
+    def release(self, lease):
         """A request is done with the plan: it stays cached (resident) unless the cache is over its size."""
+        pl = lease.plan
         victims = []
         with self._lock:
             self._busy[pl.key] -= 1
@@ -271,6 +346,11 @@ class Server:
             if pick is None:
                 evict = getattr(self.backend, "evict_idle", None)
                 if evict is not None and evict(held + self._need(self._waiting[0]) - self.budget) > 0:
+                    continue
+                # nothing admitted will free memory: the head request gives up its optional reservations
+                # (a preconditioner build) rather than wait forever
+                drop = getattr(self.backend, "drop_optional", None)
+                if self._admitted == 0 and drop is not None and drop(self._waiting[0][3]):
                     continue
                 return
             i, item, need = pick

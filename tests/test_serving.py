@@ -178,3 +178,102 @@ def test_cached_idle_plans_count_against_the_budget():
     assert be.max_held <= 100, be.max_held
     assert srv.max_held <= 100
     assert be.evicted, "idle cached plans must be evicted to admit new ones"
+
+
+class _PlanStub:
+    """Stands in for runtime.Plan on the CPU: tables + solver bytes, and a preconditioner whose build
+    takes `bound` bytes and leaves `kept` resident."""
+
+    def __init__(self, bound=500, kept=300):
+        self.n = 4
+        self.bound, self.kept, self.built = bound, kept, False
+        self.prepared = 0
+        self.active = 0
+        self.overlap = False
+        self.peak = 0
+
+    def footprint(self, precision, restart):
+        return 100 + (self.kept if self.built else 0), 50
+
+    def precond_bytes(self):
+        return (self.kept if self.built else 0), (0 if self.built else self.bound)
+
+    def set_stream(self, s):
+        pass
+
+    def prepare(self, precision, restart):
+        self.prepared += 1
+
+
+def _stub_backend(monkeypatch, plan):
+    import openbte_gb300.runtime as runtime
+    from openbte_gb300.serving import GPUBackend
+
+    class _HP:
+        def __init__(self, *a):
+            pass
+
+        def key(self):
+            return "k"
+
+    monkeypatch.setattr(runtime, "HostProblem", _HP)
+
+    class StubBackend(GPUBackend):
+        def __init__(self):
+            super().__init__()
+            self.seen = []
+
+        def _new_plan(self, hp):
+            return plan
+
+        def _stream(self):
+            return type("Stream", (), {"cuda_stream": 0})()
+
+        def _solve_plan(self, pl, req, precond):
+            pl.active += 1
+            pl.overlap |= pl.active > 1
+            self.seen.append((req.rid, precond, self.resident_bytes()))
+            time.sleep(0.02)
+            if precond == 1:
+                pl.built = True
+            pl.active -= 1
+            return type("Info", (), {"kappa_eff": 1.0, "converged": 1, "n_sweeps": 3, "n_sweeps_fp64": 1})()
+
+    return StubBackend()
+
+
+def test_repeated_plan_reserves_and_builds_the_preconditioner(monkeypatch):
+    """GPUBackend's accounting with a stub plan: the second request of a geometry reserves the build's
+    bound, builds (precond=1) with it counted as resident, and the plan keeps only the built bytes; the
+    requests of one plan never solve at the same time."""
+    plan = _PlanStub()
+    be = _stub_backend(monkeypatch, plan)
+    srv = Server(backend=be, slots=3, builders=2, hbm_budget=10_000)
+    res = replay(srv, [Request(None, None, None, None, rid=i) for i in range(4)])
+    srv.close()
+    assert all(r.status == "ok" for r in res), [r.error for r in res]
+    assert not plan.overlap
+    assert plan.prepared == 1
+    by_rid = {rid: (pc, held) for rid, pc, held in be.seen}
+    builder = [rid for rid, (pc, _) in by_rid.items() if pc == 1]
+    assert len(builder) == 1
+    # while the build ran, its bound was held on top of the plan's 150 bytes
+    assert by_rid[builder[0]][1] >= 150 + 500
+    assert plan.pending == 0
+    assert be.resident_bytes() == 150 + 300
+    assert srv.max_held <= 10_000
+
+
+def test_preconditioner_build_that_cannot_fit_is_dropped(monkeypatch):
+    """A budget that holds the plan but never the build's bound: the repeated request gives up the build
+    (solves with the preconditioner off) instead of waiting forever."""
+    plan = _PlanStub(bound=500)
+    be = _stub_backend(monkeypatch, plan)
+    srv = Server(backend=be, slots=2, builders=1, hbm_budget=600)
+    res = []
+    for i in range(3):
+        res += replay(srv, [Request(None, None, None, None, rid=i)])
+    srv.close()
+    assert all(r.status == "ok" for r in res)
+    assert srv.max_held <= 600
+    assert [pc for _, pc, _ in be.seen] == [-1, -1, -1] and not plan.built

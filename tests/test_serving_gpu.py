@@ -91,6 +91,41 @@ def test_repeated_geometry_stays_resident_and_warm_starts():
     assert abs(again.kappa - first.kappa) / abs(first.kappa) < 1e-6
 
 
+def test_repeated_geometry_builds_the_preconditioner():
+    """Three cold requests of one geometry, two slots: they solve one at a time on the shared plan; the
+    second builds the periodic-inflow preconditioner inside its admission reservation, and the plan's
+    resident bytes then include the preconditioner's blocks."""
+    import ctypes as C
+    from openbte_gb300 import objects as O
+    from openbte_gb300.geometry import porous_cell_2d
+    from openbte_gb300.material import synthetic_isotropic_2d
+    from openbte_gb300.mesh import mesh_from_cell
+    from openbte_gb300.serving import GPUBackend, Request, Server, replay
+    bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
+    ek = O.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
+    geo = mesh_from_cell(porous_cell_2d(1500, 0.25, "square", seed=7))
+    mat = synthetic_isotropic_2d(16, 32)
+    reqs = [Request(geo, mat, bcs, ek, precision="fp32_refine", rtol=1e-9, rid=i) for i in range(3)]
+    be = GPUBackend()
+    srv = Server(backend=be, slots=2)
+    first = replay(srv, reqs[:1])[0]
+    later = replay(srv, reqs[1:])
+    srv.close()
+    assert first.status == "ok" and all(r.status == "ok" for r in later), [r.error for r in later]
+    assert all(r.cached_plan for r in later)
+    (pl,) = list(be._cache.values())
+    nb, ns, ms = C.c_int32(), C.c_int32(), C.c_double()
+    assert pl.lib.obte_bte_precond_info(pl.handle, C.byref(nb), C.byref(ns), C.byref(ms)) == 0
+    assert nb.value > 0
+    resident, bound = pl.precond_bytes()
+    assert resident > 0 and bound == 0 and pl.pending == 0
+    a, b = pl.footprint("fp32_refine", be.restart)
+    assert be.resident_bytes() == a + b >= resident
+    for r in later:
+        assert abs(r.kappa - first.kappa) <= 1e-7 * abs(first.kappa), (r.kappa, first.kappa)
+    assert min(r.n_sweeps for r in later) < first.n_sweeps
+
+
 def test_request_over_budget_is_rejected():
     from openbte_gb300.serving import GPUBackend, Server, replay
     r = _requests()[0]
