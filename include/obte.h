@@ -117,6 +117,10 @@ typedef struct {
                                      0 built on the plan's second solve (plans solved once do not pay
                                      its setup), 1 built on the first solve, -1 off; other values: 0.
                                      The environment variable OBTE_XPREC=0 / 1 overrides it. */
+  int32_t dsa;                    /* diffusion-synthetic acceleration (no counterpart in the reference):
+                                     1 on, -1 off, 0 (other values) on for problems with partially
+                                     transmitting sides (side_transmission < 1), else off.
+                                     OBTE_DSA=0 / 1 overrides it. */
 } obte_solve_opts;
 
 typedef struct {

@@ -54,7 +54,7 @@ class MaterialC(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_sweeps", C.c_int32),
                 ("restart", C.c_int32), ("refine_steps", C.c_int32), ("inner_rtol", C.c_double),
-                ("warm_start", C.c_int32), ("precond", C.c_int32)]
+                ("warm_start", C.c_int32), ("precond", C.c_int32), ("dsa", C.c_int32)]
 
 
 class SolveInfo(C.Structure):

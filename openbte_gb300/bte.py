@@ -28,11 +28,12 @@ def _tensor_ptr(t):
 
 
 def solve_plan(plan, dT0, precision="fp64", rtol=1e-10, max_sweeps=1000, restart=30, refine_steps=3,
-               inner_rtol=1e-5, warm_start=False, precond=0):
+               inner_rtol=1e-5, warm_start=False, precond=0, dsa=0):
     """Solve on a prepared plan. dT0: torch CUDA float64 tensor [n]. Returns (info, dT, J, K, S) tensors.
 
     precond: periodic-inflow preconditioner, 0 = built on the plan's second solve, 1 = on the first,
-    -1 = off (the converged solution is the same; only the number of sweeps changes).
+    -1 = off.  dsa: diffusion-synthetic acceleration, 1 = on, -1 = off, 0 = on for problems with partially
+    transmitting sides.  Neither changes the converged solution, only the number of sweeps.
 
     Allocations and the solve run on the plan's stream; the plan lock keeps one solve per plan at a time.
     """
@@ -57,6 +58,7 @@ def solve_plan(plan, dT0, precision="fp64", rtol=1e-10, max_sweeps=1000, restart
         o.inner_rtol = float(inner_rtol)
         o.warm_start = 1 if warm_start else 0
         o.precond = int(precond)
+        o.dsa = int(dsa)
         info = _lib.SolveInfo()
         st = plan.lib.obte_bte_solve(plan.handle, C.byref(o), _tensor_ptr(dT0), _tensor_ptr(dT), _tensor_ptr(J),
                                      _tensor_ptr(K), _tensor_ptr(S), C.byref(info))
@@ -88,7 +90,8 @@ def BTE_RTA(geo, mat, bcs, fourier=None, effective_thermal_conductivity=None, he
     dT0_d = torch.from_numpy(np.ascontiguousarray(dT0)).to(f"cuda:{device}")
     info, dT, J, K, S = solve_plan(plan, dT0_d, precision=precision, rtol=bte_rtol, max_sweeps=max_sweeps,
                                    restart=restart, refine_steps=kwargs.get("refine_steps", 3),
-                                   inner_rtol=kwargs.get("inner_rtol", 1e-5), precond=kwargs.get("precond", 0))
+                                   inner_rtol=kwargs.get("inner_rtol", 1e-5), precond=kwargs.get("precond", 0),
+                                   dsa=kwargs.get("dsa", 0))
     if not info.converged:
         warnings.warn(f"BTE_RTA did not reach bte_rtol={bte_rtol} in {info.n_sweeps} sweeps "
                       f"(residual {info.residual:.3e})", RuntimeWarning)

@@ -330,6 +330,7 @@ extern "C" obte_status obte_bte_plan_set_transmission(obte_plan plan, const doub
   plan->ell_sum = offset_weights(plan, ell);
   // the preconditioner belongs to the old transmissions; the last solution stays as a warm start
   plan->xprec.reset();
+  plan->dsa.reset();                       // its interface conductances change with t
   plan->n_solves = 0;
   if (!plan->ctx) return OBTE_OK;
   cudaStream_t strm = plan->stream;
@@ -398,6 +399,14 @@ extern "C" obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision
   else if (precision == OBTE_FP32) pb += t32;
   else pb += t64 + t32;
   pb += xprec_resident_bytes(plan->xprec.get());
+  if (plan->dsa) {
+    pb += plan->dsa->bytes;
+  } else if (dsa_default(s)) {
+    // the diffusion operator a solve will build: CSR of L, five element vectors and a hierarchy of at
+    // most about three times L's size
+    const int64_t nnz = s.n + 2 * (int64_t)s.dsa.e1.size();
+    pb += 4 * (nnz * 12 + (s.n + 1) * 4) + s.n * 8 * 5;
+  }
   if (plan_bytes) *plan_bytes = pb;
   if (solve_bytes) *solve_bytes = plan->ctx ? solve_scratch_bytes(plan, restart > 0 ? restart : 30) : 0;
   return OBTE_OK;

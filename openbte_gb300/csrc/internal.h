@@ -269,6 +269,19 @@ struct Schedule {
   bool extra_sources = false;                // isothermal walls, heat source or nanowire terms
   bool isothermal = false;                   // isothermal (mixed) walls: they fix the temperature level, so
                                              // I - K has no constant null mode and no offset is applied
+  // Diffusion-synthetic acceleration data (dsa.cu): the cell-temperature diffusion operator that the
+  // transport operator I - K approaches on smooth temperature errors.
+  struct DsaData {
+    std::vector<double> vol;                 // [n] element volumes
+    std::vector<int32_t> e1, e2;             // [nfc] the two elements of each internal side (periodic too)
+    std::vector<int32_t> side;               // [nfc] its side id
+    std::vector<double> area, dist;          // [nfc] side area, centre-to-centre distance estimate
+    std::vector<double> t;                   // [nfc] side transmission (1: plain side)
+    std::vector<int32_t> iso_cell;           // [niso] isothermal walls: element
+    std::vector<double> iso_area, iso_dist;  // [niso] area, centre-to-wall distance estimate
+    std::vector<double> Dm, Gm;              // [n_mfp] per MFP: sum_q t_coeff (mfp v_q)(mfp v_q)^T / dim
+                                             // (isotropic part) and the half-range flux moment
+  } dsa;
   // Transmission plans without isothermal walls or nanowire terms keep the transmission-free factor of
   // every coefficient that depends on the side transmissions t: the sweep order, the levels, the slots and
   // the packed table layout depend on the mesh and the directions only, so new transmissions replace
@@ -334,6 +347,24 @@ struct SolveWork {
 // Right preconditioner of the GMRES on the periodic-inflow unknowns: for the ordinates whose inflow
 // circulates through the periodic cell for many periods, the exact inverse of their one-period
 // inflow -> outflow transfer, (I - T_b)^-1 - I, as a dense FP32 block over the direction's source slots.
+// Diffusion-synthetic acceleration (dsa.cu): right preconditioner term E L^-1 R, with R the volume-
+// weighted temperature part of a state vector, L the cell diffusion operator of Schedule::DsaData solved
+// by `cycles` stationary smoothed-aggregation V-cycle iterations (a fixed linear map, as GMRES needs), and
+// E the extension of a cell correction to the temperatures, the wall temperatures of each wall's element
+// and the periodic inflow of each source slot's element.
+struct DsaOp {
+  AmgPtr amg;
+  DevBuf rp, ci, val;            // L (CSR, symmetric, volume-weighted)
+  DevBuf vol;                    // [n]
+  DevBuf b, d, r, e, mean;       // right-hand side, correction, residual, cycle update; weighted mean
+  double inv_vol_sum = 0;
+  bool project = true;           // L has the constant null vector (no isothermal walls)
+  int cycles = 1;
+  int levels = 0;
+  double setup_ms = 0;
+  int64_t bytes = 0;             // device bytes held
+};
+
 struct XPrec {
   bool tried = false;            // setup ran (blocks may still be empty)
   int nblk = 0, smax = 0;
@@ -385,6 +416,7 @@ struct obte_plan_s {
   int sweep_batch = 1;                    // with the map: that many state vectors, sweep_batch_stride apart
   int64_t sweep_batch_stride = 0;
   std::unique_ptr<obte::XPrec> xprec;     // periodic-inflow block preconditioner
+  std::unique_ptr<obte::DsaOp> dsa;       // diffusion-synthetic acceleration (built on first use)
   int n_solves = 0;                       // obte_bte_solve calls on this plan
 };
 
@@ -405,6 +437,10 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk);
 // out[X blocks] += W in[X blocks] (fp32: FP32 accumulation, for stages with an FP32 Krylov basis)
 void xprec_add(obte_plan plan, const double* in, double* out, bool fp32);
 int64_t xprec_resident_bytes(const XPrec* P);
+// Diffusion-synthetic acceleration (dsa.cu).
+obte_status ensure_dsa(obte_plan plan);
+void dsa_add(obte_plan plan, const double* in, double* out);    // out += E L^-1 R in
+bool dsa_default(const Schedule& s);                            // on by default for this problem?
 int64_t xprec_build_bound(obte_plan plan);   // device bytes a build would allocate (0 once tried)
 obte_status check_device_error(obte_plan plan);
 // Plan-owned J, K, S buffers for sweeps whose final-pass accumulations are discarded (api.cu).

@@ -398,17 +398,24 @@ struct Solver {
   double t_wall = 0;
   int t_iters = 0;
 
-  // right preconditioner (periodic-inflow blocks), or off
+  // right preconditioner (periodic-inflow blocks and / or diffusion-synthetic acceleration), or off
   bool xp = false;
+  bool xblocks = false;     // periodic-inflow blocks
+  bool dsa = false;         // diffusion-synthetic acceleration
   // the next gmres call starts from x = 0 (its initial residual is the right-hand side: no sweep)
   bool x_zero = false;
   // a final pass that recomputes the true residual follows every gmres call: end a cycle whose Arnoldi
   // estimate met the tolerance without the confirming sweep
   bool estimate_exit = false;
-  // out = M^-1 in = in + W in (W on the slow inflow blocks)
+  // out += (M^-1 - I) in: W in on the slow inflow blocks, E L^-1 R in of the diffusion correction
+  void prec_add(const double* in, double* out, bool fp32) {
+    if (xblocks) xprec_add(plan, in, out, fp32);
+    if (dsa) dsa_add(plan, in, out);
+  }
+  // out = M^-1 in
   obte_status prec(const double* in, double* out, bool fp32) {
     OBTE_CUDA(cudaMemcpyAsync(out, in, (size_t)wk.nu * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    xprec_add(plan, in, out, fp32);
+    prec_add(in, out, fp32);
     OBTE_CUDA(cudaGetLastError());
     return OBTE_OK;
   }
@@ -614,7 +621,7 @@ struct Solver {
           xupdate32_kernel<<<nb, VT, 0, st>>>(z, V, ld, j, wk.hdev.as<double>(), n);
           count_launch();
           OBTE_TRY(axpby(1.0, z, 1.0, x));
-          xprec_add(plan, z, x, true);
+          prec_add(z, x, true);
         } else {
           xupdate32_kernel<<<nb, VT, 0, st>>>(x, V, ld, j, wk.hdev.as<double>(), n);
           count_launch();
@@ -753,7 +760,7 @@ struct Solver {
           update_kernel<<<wk.nb, VT, 0, st>>>(z, V, n, j, wk.hdev.as<double>(), n, nullptr, nullptr);
           count_launch();
           OBTE_TRY(axpby(1.0, z, 1.0, x));
-          xprec_add(plan, z, x, false);
+          prec_add(z, x, false);
         } else {
           update_kernel<<<wk.nb, VT, 0, st>>>(x, V, n, j, wk.hdev.as<double>(), n, nullptr, nullptr);
           count_launch();
@@ -907,10 +914,18 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
     }
   }
   const bool use_xp = pmode >= 0 && plan->xprec && plan->xprec->nblk > 0;
-  if (use_xp && !wk.pz.p) OBTE_TRY(wk.pz.alloc((size_t)wk.nu * sizeof(double)));
+  // diffusion-synthetic acceleration: opts->dsa 1 on, -1 off, 0 (other values) the problem's default;
+  // OBTE_DSA=0 / 1 overrides
+  int dmode = (opts->dsa >= -1 && opts->dsa <= 1) ? opts->dsa : 0;
+  if (const char* e = std::getenv("OBTE_DSA")) dmode = std::atoi(e) == 0 ? -1 : 1;
+  const bool use_dsa = dmode == 1 || (dmode == 0 && dsa_default(s));
+  if (use_dsa) OBTE_TRY(ensure_dsa(plan));
+  if ((use_xp || use_dsa) && !wk.pz.p) OBTE_TRY(wk.pz.alloc((size_t)wk.nu * sizeof(double)));
   plan->has_solution = false;
   Solver sv(plan, wk, max_sweeps);
-  sv.xp = use_xp;
+  sv.xp = use_xp || use_dsa;
+  sv.xblocks = use_xp;
+  sv.dsa = use_dsa;
   sv.estimate_exit = true;   // every GMRES call below is followed by a final pass
   double* u = wk.u.as<double>();
   const int64_t nsrc = s.x_base[s.n_dir];

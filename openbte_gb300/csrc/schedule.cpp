@@ -298,6 +298,53 @@ obte_status build_schedule(const obte_problem* pb, const obte_material* mt, Sche
   s.contact_alpha = pb->contact_alpha;
   s.extra_sources = pb->n_mixed > 0 || pb->is_nanowire || pb->heat_source != nullptr;
   s.isothermal = pb->n_mixed > 0;
+
+  // diffusion-synthetic acceleration: the cell diffusion operator's faces and coefficients.  Distance
+  // from an element's centre to a side: dim V / (sides x area), exact for simplices (the centroid sits
+  // at 1 / (dim + 1) of the height over the side) and for squares and cubes.
+  {
+    Schedule::DsaData& D = s.dsa;
+    D = Schedule::DsaData();
+    D.vol.assign(vol, vol + n);
+    auto side_area = [&](int64_t sd) {
+      double a2 = 0;
+      for (int d = 0; d < dim; ++d) a2 += na[sd * dim + d] * na[sd * dim + d];
+      return std::sqrt(a2);
+    };
+    auto half = [&](int64_t e, double a) { return (double)dim * vol[e] / ((double)nf * a); };
+    D.e1.resize(ni); D.e2.resize(ni); D.side.resize(ni); D.area.resize(ni); D.dist.resize(ni); D.t.resize(ni);
+    for (int64_t k = 0; k < ni; ++k) {
+      const int64_t sd = pb->internal[k];
+      const double a = side_area(sd);
+      D.e1[k] = f_row[k];
+      D.e2[k] = f_nb[k];
+      D.side[k] = (int32_t)sd;
+      D.area[k] = a;
+      D.dist[k] = a > 0 ? half(f_row[k], a) + half(f_nb[k], a) : 1.0;
+      D.t[k] = t_side[sd];
+    }
+    for (int64_t k = 0; k < pb->n_mixed; ++k) {
+      const int64_t sd = pb->mixed_sides[k];
+      const double a = side_area(sd);
+      if (!(a > 0)) continue;
+      D.iso_cell.push_back((int32_t)sem[2 * sd]);
+      D.iso_area.push_back(a);
+      D.iso_dist.push_back(half(sem[2 * sd], a));
+    }
+    // isotropic parts: n . (sum_q c_q F_q F_q^T) . n -> sum_q c_q |F_q|^2 / dim and sum_q c_q max(F_q . n, 0)
+    // -> sum_q c_q |F_q| <max(cos, 0)> (1 / pi in 2D, 1 / 4 in 3D), F_q = mfp v_q
+    const double cmean = dim == 2 ? 1.0 / 3.14159265358979323846 : 0.25;
+    D.Dm.assign(n_mfp, 0.0);
+    D.Gm.assign(n_mfp, 0.0);
+    for (int m = 0; m < n_mfp; ++m)
+      for (int q = 0; q < n_dir; ++q) {
+        double v2 = 0;
+        for (int d = 0; d < dim; ++d) v2 += mt->vmfp[(int64_t)q * dd + d] * mt->vmfp[(int64_t)q * dd + d];
+        const double c = mt->t_coeff[(int64_t)m * n_dir + q], L = mt->mfps[m];
+        D.Dm[m] += c * L * L * v2 / dim;
+        D.Gm[m] += c * L * std::sqrt(v2) * cmean;
+      }
+  }
   s.normalization = nrm;
   if (s.tim) {
     std::vector<double> jump_of(ns, 0.0);
@@ -737,6 +784,7 @@ obte_status set_transmission(Schedule& s, const double* t) {
   });
   for (int64_t w = 0; w < s.nd; ++w)
     s.ell_B[w] = tf.ell0[w] * (tf.w_side[w] < 0 ? 1.0 : 1.0 - t[tf.w_side[w]]);
+  for (size_t k = 0; k < s.dsa.t.size(); ++k) s.dsa.t[k] = t[s.dsa.side[k]];
   return OBTE_OK;
 }
 

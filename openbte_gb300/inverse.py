@@ -109,7 +109,7 @@ class PixelSolver:
 
     def __init__(self, n: int, material: IsotropicMaterial, size: float = 1.0, direction=(1, 0), device: int = 0,
                  precision: str = "fp32_refine", rtol: float = 1e-8, restart: int = 100, max_sweeps: int = 3000,
-                 reuse_plan: bool = True, warm_start: bool = False):
+                 reuse_plan: bool = True, warm_start: bool = False, dsa: int = 0):
         if tuple(direction) not in ((1, 0), (0, 1)):
             raise NotImplementedError("kappa along x ([1, 0]) or y ([0, 1])")
         self.lib = _lib.load()
@@ -127,6 +127,7 @@ class PixelSolver:
         self.last_info = None
         self.last_upload_bytes = 0
         self.reuse_plan, self.warm_start = reuse_plan, warm_start
+        self.dsa = dsa            # diffusion-synthetic acceleration: 0 = the default (on here), 1 on, -1 off
         self._h = None
 
     def _problem(self, t_host):
@@ -190,7 +191,7 @@ class PixelSolver:
         try:
             opts = _lib.SolveOpts(precision=_lib.PRECISION[self.precision], rtol=self.rtol, max_sweeps=self.max_sweeps,
                                   restart=self.restart, refine_steps=20, inner_rtol=1e-5,
-                                  warm_start=1 if self.warm_start else 0)
+                                  warm_start=1 if self.warm_start else 0, dsa=int(self.dsa))
             dT0 = torch.zeros(self.grid["n_elems"], dtype=torch.float64, device=dev)
             grad_t = torch.empty(self.grid["side_elem_map"].shape[0], dtype=torch.float64, device=dev)
             info = _lib.SolveInfo()
