@@ -338,12 +338,18 @@ def cpu_baseline(geo, mat, bcs, ek, budget_s=20.0, seed=0):
     from openbte_gb300.material import synthetic_isotropic_2d
     cores = os.cpu_count() or 1
     n_mfp, n_dir = np.asarray(mat.t_coeff).shape
+    if geo.dim == 3:
+        return {"value": None, "unit": "solves/s", "cores": cores, "kind": "port",
+                "sample": "not measured: SuperLU of one ordinate of the periodic operator on the 3D mesh takes "
+                          "minutes (~290 s at 110k tetrahedra), beyond the bench's budget"}
     # source iterations the reference needs for <=1e-4 kappa error, measured on a small proxy cell
     pg = mesh_from_cell(porous_cell_2d(600, 0.25, "square", seed=5))
     pm = synthetic_isotropic_2d(8, 16)
+    pb = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0}, diffuse="Boundary")
+    pe = O.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
     hist = []
-    kref = bte_oracle.bte_rta(pg, pm, bcs, effective_thermal_conductivity=ek, bte_rtol=1e-12, bte_max_iter=3000)[0]
-    bte_oracle.bte_rta(pg, pm, bcs, effective_thermal_conductivity=ek, bte_rtol=0, bte_max_iter=200, history=hist)
+    kref = bte_oracle.bte_rta(pg, pm, pb, effective_thermal_conductivity=pe, bte_rtol=1e-12, bte_max_iter=3000)[0]
+    bte_oracle.bte_rta(pg, pm, pb, effective_thermal_conductivity=pe, bte_rtol=0, bte_max_iter=200, history=hist)
     n_iter = next((i + 1 for i, (k, _) in enumerate(hist) if abs(k - kref) / abs(kref) <= 1e-4), len(hist))
     ops = bte_oracle.setup_operators(geo, mat, bcs)
     solver = bte_oracle.OrdinateSolver(geo, np.asarray(mat.mfps, dtype=np.float64), ops)
@@ -460,7 +466,9 @@ def run_inverse(args, dev):
                    "l2": "inputs and per-ordinate field (210 MB) larger than L2", "parallelism": "single",
                    "fields": "a new density field every step (base field + 0.1 x seeded field); one PixelSolver, "
                              "its plan built once and its transmissions replaced per field",
-                   "warm_start": bool(args.warm_start)},
+                   "warm_start": bool(args.warm_start),
+                   "acceleration": "diffusion-synthetic (OBTE_DSA=0 turns it off)"
+                                   if os.environ.get("OBTE_DSA", "1") != "0" else "off (OBTE_DSA=0)"},
         "kappa_eff": kaps[-1], "kappa_fp64": kap64, "kappa_rel_err_vs_fp64": abs(kaps[-1] - kap64) / abs(kap64),
         "sweeps_per_eval": float(np.median(sweeps)), "fp64_sweeps_per_eval": info.n_sweeps_fp64,
         "gradient_abs_max": float(np.abs(gh).max()),
@@ -640,6 +648,10 @@ def reference_arm(args):
                                   "d2h_bytes_per_step": 0}, "wall_s": time.time() - t0}))
         return
     geo, mat, bcs, ek = problem(args.workload)
+    if geo.dim == 3:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's per-ordinate SuperLU on the "
+                          "3D benchmark mesh takes minutes per ordinate (~290 s at 110k tetrahedra)"}))
+        return
     t0 = time.time()
     steps = []
     for _ in range(args.warmup + args.steps):

@@ -206,6 +206,10 @@ obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision, int32_t r
  *   dT     device [n_elems]  Temperature_BTE
  *   J      device [n_elems, dim_sigma]  Flux_BTE / 1e9 (W/m/nm), as accumulated by the reference
  *   K, S   device [n_mfp, n_dir]  per-ordinate kappa and suppression (aux)
+ * OBTE_FP32_REFINE: GMRES with FP32 sweeps to inner_rtol, then an output pass that measures the true
+ * residual and gives J, K, S, with FP32-swept corrections until the residual meets rtol.  The output pass
+ * is FP64 below rtol = 5e-6; from 5e-6 up it is FP32 (its rounding, a few 1e-7 of the state, is under a
+ * tenth of the tolerance), so a loose solve runs no FP64 sweep (OBTE_REFINE_FP64_PASS=1: FP64 always).
  */
 obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opts, const double* dT0,
                            double* dT, double* J, double* K, double* S, obte_solve_info* info);

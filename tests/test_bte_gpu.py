@@ -127,3 +127,20 @@ def test_fp32_refine_output_pass(case, monkeypatch, double_float):
     else:
         assert r.aux["n_sweeps_fp64"] >= 1 and r.aux["n_sweeps_df"] == 0, r.aux
     assert abs(r.kappa_eff - d["bte_kappa"]) / abs(d["bte_kappa"]) < 1e-8
+
+
+def test_fp32_refine_loose_tolerance_runs_no_fp64_sweep(case, monkeypatch):
+    """At a tolerance of 5e-6 or looser the output pass is FP32 (its rounding is under a tenth of the
+    tolerance): no FP64 sweep, kappa within the tolerance of the reference's (golden c0_2k), and the same
+    solve with the FP64 pass forced agrees to the tolerance."""
+    from openbte_gb300 import BTE_RTA
+    monkeypatch.delenv("OBTE_REFINE_DF", raising=False)
+    geo, mat, bcs, ek, d = case("c0_2k")
+    f = O.SolverResults(variables={"Temperature_Fourier": {"data": d["fourier_T"]}})
+    r = BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-5, precision="fp32_refine")
+    assert r.aux["n_sweeps_fp64"] == 0 and r.aux["residual"] <= 1e-5, r.aux
+    assert abs(r.kappa_eff - d["bte_kappa"]) / abs(d["bte_kappa"]) < 1e-4
+    monkeypatch.setenv("OBTE_REFINE_FP64_PASS", "1")
+    r64 = BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-5, precision="fp32_refine")
+    assert r64.aux["n_sweeps_fp64"] >= 1
+    assert abs(r.kappa_eff - r64.kappa_eff) / abs(r64.kappa_eff) < 1e-5
