@@ -277,12 +277,25 @@ obte_status obte_bte_plan_test_wait_timeout(obte_plan plan, int32_t skip_unit, i
  * temperatures of the final sweep and evaluates the adjoint from them: the adjoint of
  * direction q is the forward solution of its reverse, so no second solve runs.
  *   grad_t  device [n_sides]; 0 on sides that are not internal.
- * Needs a direction set closed under reversal, sigma = a t_coeff mfp s (isotropic), the
- * periodic jump only on the contact sides, and no isothermal, heat-source or nanowire terms
- * (else OBTE_ERR_UNSUPPORTED).  info->kappa_eff is kappa_eff.
+ * Needs a direction set closed under reversal (else obte_bte_kappa_gradient_adjoint below),
+ * sigma = a t_coeff mfp s (isotropic), the periodic jump only on the contact sides, and no
+ * isothermal, heat-source or nanowire terms (else OBTE_ERR_UNSUPPORTED).  info->kappa_eff is
+ * kappa_eff.
  */
 obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_opts* opts, const double* dT0,
                                     double* grad_t, obte_solve_info* info);
+/*
+ * The same gradient for a direction set that is not closed under reversal: adjoint_plan is the plan's
+ * problem (mesh, sides, transmissions, contact) with every direction reversed (ordinate q: -s_q, the same
+ * t_coeff and MFP, sigma negated).  Its forward solve is the transposed transport of every ordinate, swept
+ * in reverse order; its per-ordinate temperatures give the adjoint (lam_mq(c) = k V_c t_mq X'_mq(c)), so
+ * the gradient costs two solves.  With sides that re-emit, sum_mq sigma_mq must be zero (else
+ * OBTE_ERR_UNSUPPORTED); an adjoint plan that does not match returns OBTE_ERR_BAD_ARG.  After new
+ * transmissions, update both plans.  adjoint_info (may be NULL) receives the adjoint solve's info.
+ */
+obte_status obte_bte_kappa_gradient_adjoint(obte_plan plan, obte_plan adjoint_plan, const obte_solve_opts* opts,
+                                            const double* dT0, double* grad_t, obte_solve_info* info,
+                                            obte_solve_info* adjoint_info);
 /* Sizes of the state vector pieces: n_elems, n_diffuse, n_x. */
 obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x);
 /*

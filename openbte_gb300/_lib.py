@@ -111,6 +111,8 @@ SIGNATURES = [
     ("obte_bte_plan_test_wait_timeout", C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     ("obte_bte_kappa_gradient", C.c_int, [C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p,
                                           C.POINTER(SolveInfo)]),
+    ("obte_bte_kappa_gradient_adjoint", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(SolveOpts), C.c_void_p,
+                                                  C.c_void_p, C.POINTER(SolveInfo), C.POINTER(SolveInfo)]),
     ("obte_bte_state_layout", C.c_int, [C.c_void_p, p_i64, p_i64, p_i64]),
     ("obte_bte_precond_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                         C.POINTER(C.c_double)]),

@@ -379,6 +379,7 @@ struct XPrec {
 // per-ordinate temperatures (built on the first gradient call of a plan).
 struct TimDevice {
   bool ready = false;
+  bool paired = false;  // adjoint fields from a separate plan with the reversed directions
   double kfac = 0;      // adjoint scale nrm * a / jump (sigma = a tau L s)
   DevBuf side, e1, e2, w1, w2, na, jump, contact, dirs, tl, sig, refl, xs, K;
 };

@@ -35,7 +35,8 @@ namespace obte {
 static constexpr int kGradThreads = 128;
 
 __global__ void __launch_bounds__(kGradThreads)
-tim_gradient_kernel(const float* __restrict__ X, const double* __restrict__ TB, int64_t n, int n_dir, int n_mfp,
+tim_gradient_kernel(const float* __restrict__ X, const float* __restrict__ Xq, const double* __restrict__ TB,
+                    int64_t n, int n_dir, int n_mfp,
                     int dim, const double* __restrict__ dirs, const double* __restrict__ tl,
                     const double* __restrict__ sig, const int32_t* __restrict__ refl, int64_t ni,
                     const int32_t* __restrict__ side, const int32_t* __restrict__ e1, const int32_t* __restrict__ e2,
@@ -59,10 +60,10 @@ tim_gradient_kernel(const float* __restrict__ X, const double* __restrict__ TB, 
       const int64_t qb = refl[q];
       const double w = tl[idx];
       if (sn < 0) {          // inflow of the e1 face (outward +n): owner e1, neighbour e2, jump +J
-        const double xo = X[(qb * n + c1) * n_mfp + m], xn = X[((int64_t)q * n + c2) * n_mfp + m];
+        const double xo = Xq[(qb * n + c1) * n_mfp + m], xn = X[((int64_t)q * n + c2) * n_mfp + m];
         e += sn * w * xo * (xn + J - R1);
       } else if (sn > 0) {   // inflow of the e2 face (outward -n): owner e2, neighbour e1, jump -J
-        const double xo = X[(qb * n + c2) * n_mfp + m], xn = X[((int64_t)q * n + c1) * n_mfp + m];
+        const double xo = Xq[(qb * n + c2) * n_mfp + m], xn = X[((int64_t)q * n + c1) * n_mfp + m];
         e += -sn * w * xo * (xn - J - R2);
       }
       if (con) {
@@ -88,12 +89,16 @@ tim_gradient_kernel(const float* __restrict__ X, const double* __restrict__ TB, 
   }
 }
 
-// Host checks of the adjoint identity's assumptions, then the device tables.
-static obte_status ensure_tim(obte_plan plan) {
+// Host checks of the adjoint identity's assumptions, then the device tables.  `paired`: the reversed
+// directions live in a separate adjoint plan (ordinate q of that plan is -s_q), so this plan's direction
+// set need not be closed under reversal and refl is the identity into the adjoint plan's fields.
+static obte_status ensure_tim(obte_plan plan, bool paired) {
   PhaseTimer timer("ensure_tim");
+  if (plan->tim && plan->tim->ready && plan->tim->paired != paired) plan->tim.reset();
   if (!plan->tim) plan->tim.reset(new TimDevice());
   TimDevice& T = *plan->tim;
   if (T.ready) return OBTE_OK;
+  T.paired = paired;
   const Schedule& s = plan->sched;
   const int dim = s.dim, nq = s.n_dir, nm = s.n_mfp;
   if (s.extra_sources) {
@@ -108,15 +113,23 @@ static obte_status ensure_tim(obte_plan plan) {
       for (int k = 0; k < dim; ++k) d = std::max(d, std::fabs(s.dirs[(size_t)q * dim + k] + s.dirs[(size_t)r * dim + k]));
       if (d < 1e-9) refl[q] = r;
     }
-  for (int q = 0; q < nq; ++q)
-    if (refl[q] < 0) { set_error("gradient: the direction set is not closed under reversal"); return OBTE_ERR_UNSUPPORTED; }
+  if (paired) {
+    for (int q = 0; q < nq; ++q) refl[q] = q;
+  } else {
+    for (int q = 0; q < nq; ++q)
+      if (refl[q] < 0) {
+        set_error("gradient: the direction set is not closed under reversal (pass an adjoint plan with the "
+                  "reversed directions to obte_bte_kappa_gradient_adjoint)");
+        return OBTE_ERR_UNSUPPORTED;
+      }
+  }
   // tau L and the flux scale a (sigma = a tau L s)
   std::vector<double> tl((size_t)nq * nm), sg((size_t)nq * nm * dim);
   double a = 0;
   for (int q = 0; q < nq; ++q)
     for (int m = 0; m < nm; ++m) {
       const double tau = s.tco[(size_t)q * s.m_pad + m];
-      if (std::fabs(tau - s.tco[(size_t)refl[q] * s.m_pad + m]) > 1e-12 * std::fabs(tau)) {
+      if (!paired && std::fabs(tau - s.tco[(size_t)refl[q] * s.m_pad + m]) > 1e-12 * std::fabs(tau)) {
         set_error("gradient: ordinate weights differ between a direction and its reverse");
         return OBTE_ERR_UNSUPPORTED;
       }
@@ -184,19 +197,89 @@ static obte_status ensure_tim(obte_plan plan) {
 
 using namespace obte;
 
-extern "C" obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_opts* opts, const double* dT0,
-                                               double* grad_t, obte_solve_info* info) {
+namespace {
+
+// The adjoint plan must be the plan's problem with every direction reversed: same mesh, sides,
+// transmissions and contact, ordinate q of `adj` = -s_q with the same weight and MFP and sigma negated.
+obte_status check_adjoint_pair(const Schedule& s, const Schedule& a) {
+  auto fail = [](const char* what) {
+    set_error(std::string("gradient: the adjoint plan is not the plan's problem with reversed directions (") +
+              what + ")");
+    return OBTE_ERR_BAD_ARG;
+  };
+  if (!a.tim) return fail("no side transmissions");
+  if (a.n != s.n || a.n_sides != s.n_sides || a.dim != s.dim || a.n_dir != s.n_dir || a.n_mfp != s.n_mfp ||
+      a.nd != s.nd || a.m_pad != s.m_pad || a.ds != s.ds)
+    return fail("sizes");
+  if (a.tim_side != s.tim_side || a.tim_e1 != s.tim_e1 || a.tim_e2 != s.tim_e2 || a.tim_contact != s.tim_contact)
+    return fail("sides");
+  for (size_t k = 0; k < s.tim_jump.size(); ++k)
+    if (a.tim_jump[k] != s.tim_jump[k]) return fail("periodic jump");
+  for (size_t k = 0; k < s.dsa.t.size(); ++k)
+    if (a.dsa.t[k] != s.dsa.t[k]) return fail("transmissions");
+  for (size_t i = 0; i < s.dirs.size(); ++i)
+    if (std::fabs(a.dirs[i] + s.dirs[i]) > 1e-9) return fail("directions");
+  for (int m = 0; m < s.n_mfp; ++m)
+    if (a.mfp[m] != s.mfp[m]) return fail("MFPs");
+  double ssum[3] = {0, 0, 0}, sabs = 0;
+  for (int q = 0; q < s.n_dir; ++q)
+    for (int m = 0; m < s.n_mfp; ++m) {
+      const double t0 = s.tco[(size_t)q * s.m_pad + m], t1 = a.tco[(size_t)q * a.m_pad + m];
+      if (std::fabs(t0 - t1) > 1e-12 * std::fabs(t0)) return fail("ordinate weights");
+      for (int d = 0; d < s.ds; ++d) {
+        const double v0 = s.sig[((size_t)q * s.m_pad + m) * s.ds + d], v1 = a.sig[((size_t)q * a.m_pad + m) * a.ds + d];
+        if (std::fabs(v0 + v1) > 1e-12 * std::fabs(v0) + 1e-300) return fail("sigma");
+        if (d < 3) ssum[d] += v0;
+        sabs += std::fabs(v0);
+      }
+    }
+  // re-emitting sides normalise their weights by the incoming sigma flux; the reversed problem uses the
+  // outgoing one, which is the same only when sum sigma = 0
+  if (s.nd > 0)
+    for (int d = 0; d < std::min(3, s.ds); ++d)
+      if (std::fabs(ssum[d]) > 1e-9 * sabs) {
+        set_error("gradient: sum of sigma over the ordinates is not zero (re-emitting sides would not conserve "
+                  "energy in the reversed problem)");
+        return OBTE_ERR_UNSUPPORTED;
+      }
+  return OBTE_OK;
+}
+
+obte_status gradient_impl(obte_plan plan, obte_plan adj, const obte_solve_opts* opts, const double* dT0,
+                          double* grad_t, obte_solve_info* info, obte_solve_info* adj_info) {
   if (!plan || !opts || !dT0 || !grad_t) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
   if (!plan->ctx) { set_error("host-only plan cannot solve"); return OBTE_ERR_BAD_ARG; }
   const Schedule& s = plan->sched;
   if (!s.tim) { set_error("gradient: the plan was created without side transmissions"); return OBTE_ERR_BAD_ARG; }
-  OBTE_TRY(ensure_tim(plan));
+  if (adj) {
+    if (!adj->ctx) { set_error("host-only adjoint plan cannot solve"); return OBTE_ERR_BAD_ARG; }
+    if (adj == plan) { set_error("gradient: the adjoint plan is the plan itself"); return OBTE_ERR_BAD_ARG; }
+    OBTE_TRY(check_adjoint_pair(s, adj->sched));
+    OBTE_TRY(ensure_tim(adj, true));
+  }
+  OBTE_TRY(ensure_tim(plan, adj != nullptr));
   TimDevice& T = *plan->tim;
   obte_solve_info inf{};
   plan->xstore = T.xs.as<float>();
   const obte_status st = obte_bte_solve(plan, opts, dT0, nullptr, nullptr, T.K.as<double>(), nullptr, &inf);
   plan->xstore = nullptr;
   if (st != OBTE_OK && st != OBTE_ERR_NOT_CONVERGED) return st;
+  const float* Xq = T.xs.as<float>();
+  obte_status sta = OBTE_OK;
+  if (adj) {
+    // the adjoint fields: the forward solution of the reversed directions (the transposed sweep of every
+    // direction, which visits its elements in reverse order), on the adjoint plan's own stream
+    TimDevice& A = *adj->tim;
+    obte_solve_info ainf{};
+    OBTE_CUDA(wait_stream(plan->stream));
+    adj->xstore = A.xs.as<float>();
+    sta = obte_bte_solve(adj, opts, dT0, nullptr, nullptr, A.K.as<double>(), nullptr, &ainf);
+    adj->xstore = nullptr;
+    if (sta != OBTE_OK && sta != OBTE_ERR_NOT_CONVERGED) return sta;
+    OBTE_CUDA(wait_stream(adj->stream));
+    Xq = A.xs.as<float>();
+    if (adj_info) *adj_info = ainf;
+  }
   cudaStream_t stream = plan->stream;
   OBTE_CUDA(cudaMemsetAsync(grad_t, 0, (size_t)s.n_sides * sizeof(double), stream));
   const int64_t ni = (int64_t)s.tim_side.size();
@@ -204,7 +287,7 @@ extern "C" obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_
     const int blocks = (int)std::min<int64_t>(ni, (int64_t)plan->ctx->num_sms * 16);
     const double* TB = plan->work->Fu.as<double>() + s.n;   // reflected temperatures of the final sweep
     tim_gradient_kernel<<<blocks, kGradThreads, 0, stream>>>(
-        T.xs.as<float>(), TB, s.n, s.n_dir, s.n_mfp, s.dim, T.dirs.as<double>(), T.tl.as<double>(),
+        T.xs.as<float>(), Xq, TB, s.n, s.n_dir, s.n_mfp, s.dim, T.dirs.as<double>(), T.tl.as<double>(),
         T.sig.as<double>(), T.refl.as<int32_t>(), ni, T.side.as<int32_t>(), T.e1.as<int32_t>(), T.e2.as<int32_t>(),
         T.w1.as<int32_t>(), T.w2.as<int32_t>(), T.na.as<double>(), T.jump.as<double>(), T.contact.as<int8_t>(),
         s.normalization, s.contact_alpha, T.kfac, grad_t);
@@ -213,5 +296,19 @@ extern "C" obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_
   }
   OBTE_CUDA(cudaStreamSynchronize(stream));
   if (info) *info = inf;
-  return st;
+  return st != OBTE_OK ? st : sta;
+}
+
+}  // namespace
+
+extern "C" obte_status obte_bte_kappa_gradient(obte_plan plan, const obte_solve_opts* opts, const double* dT0,
+                                               double* grad_t, obte_solve_info* info) {
+  return gradient_impl(plan, nullptr, opts, dT0, grad_t, info, nullptr);
+}
+
+extern "C" obte_status obte_bte_kappa_gradient_adjoint(obte_plan plan, obte_plan adjoint_plan,
+                                                       const obte_solve_opts* opts, const double* dT0,
+                                                       double* grad_t, obte_solve_info* info,
+                                                       obte_solve_info* adjoint_info) {
+  return gradient_impl(plan, adjoint_plan, opts, dT0, grad_t, info, adjoint_info);
 }

@@ -88,6 +88,20 @@ class IsotropicMaterial:
         mfps = np.logspace(math.log10(mfp_min), math.log10(mfp_max), n_mfp)
         return IsotropicMaterial(mfps, lognormal_kappa(mfps, kappa_bulk, median, sigma_ln), n_phi)
 
+    def reversed(self):
+        """The same material with every direction reversed (s_q -> -s_q, sigma -> -sigma): the adjoint
+        problem of a direction set that is not closed under reversal."""
+        r = IsotropicMaterial.__new__(IsotropicMaterial)
+        r.mfps, r.kappas, r.kappa_bulk = self.mfps, self.kappas, self.kappa_bulk
+        r.vmfp = np.ascontiguousarray(-self.vmfp)
+        r.t_coeff = self.t_coeff
+        r.sigma = np.ascontiguousarray(-self.sigma)
+        return r
+
+    def closed_under_reversal(self) -> bool:
+        v = self.vmfp
+        return all(np.min(np.abs(v + v[q]).max(axis=1)) < 1e-9 for q in range(len(v)))
+
     def c_struct(self):
         m = _lib.MaterialC()
         m.n_mfp, m.n_dir = len(self.mfps), self.vmfp.shape[0]
@@ -129,6 +143,11 @@ class PixelSolver:
         self.reuse_plan, self.warm_start = reuse_plan, warm_start
         self.dsa = dsa            # diffusion-synthetic acceleration: 0 = the default (on here), 1 on, -1 off
         self._h = None
+        # a direction set not closed under reversal takes its adjoint from a second plan with the reversed
+        # directions (obte_bte_kappa_gradient_adjoint)
+        self.paired = not material.closed_under_reversal()
+        self._ha = None
+        self.last_adjoint_info = None
 
     def _problem(self, t_host):
         g = self.grid
@@ -149,12 +168,17 @@ class PixelSolver:
         return p
 
     def _plan(self, t_host):
-        """The plan with side transmissions t_host: the cached one updated, or a new one."""
+        """The plan with side transmissions t_host: the cached one updated, or a new one (and the reversed
+        directions' plan for a set that is not closed under reversal)."""
         if self._h is not None:
             nb = C.c_int64()
             _lib.check(self.lib.obte_bte_plan_set_transmission(self._h, ptr(t_host), C.byref(nb)),
                        "obte_bte_plan_set_transmission")
             self.last_upload_bytes = nb.value          # coefficients copied to the device
+            if self._ha is not None:
+                _lib.check(self.lib.obte_bte_plan_set_transmission(self._ha, ptr(t_host), C.byref(nb)),
+                           "obte_bte_plan_set_transmission")
+                self.last_upload_bytes += nb.value
             return self._h
         ctx = context(self.device)
         prob = self._problem(t_host)
@@ -162,6 +186,13 @@ class PixelSolver:
         h = C.c_void_p()
         _lib.check(self.lib.obte_bte_plan_create(ctx, C.byref(prob), C.byref(mat), C.byref(h)), "obte_bte_plan_create")
         self._h = h
+        if self.paired:
+            rev = self.material.reversed()
+            self._rev = rev                            # keeps the arrays the C struct points to alive
+            ha = C.c_void_p()
+            _lib.check(self.lib.obte_bte_plan_create(ctx, C.byref(prob), C.byref(rev.c_struct()), C.byref(ha)),
+                       "obte_bte_plan_create")
+            self._ha = ha
         pb, sb = C.c_int64(), C.c_int64()
         _lib.check(self.lib.obte_bte_plan_footprint(h, _lib.PRECISION[self.precision], self.restart, C.byref(pb),
                                                     C.byref(sb)), "obte_bte_plan_footprint")
@@ -169,9 +200,12 @@ class PixelSolver:
         return h
 
     def close(self):
-        """Release the cached plan."""
+        """Release the cached plan(s)."""
         if self._h is not None:
             h, self._h = self._h, None
+            self.lib.obte_bte_plan_destroy(h)
+        if getattr(self, "_ha", None) is not None:
+            h, self._ha = self._ha, None
             self.lib.obte_bte_plan_destroy(h)
 
     def __del__(self):
@@ -195,9 +229,17 @@ class PixelSolver:
             dT0 = torch.zeros(self.grid["n_elems"], dtype=torch.float64, device=dev)
             grad_t = torch.empty(self.grid["side_elem_map"].shape[0], dtype=torch.float64, device=dev)
             info = _lib.SolveInfo()
-            st = self.lib.obte_bte_kappa_gradient(h, C.byref(opts), C.c_void_p(dT0.data_ptr()),
-                                                  C.c_void_p(grad_t.data_ptr()), C.byref(info))
-            _lib.check(st, "obte_bte_kappa_gradient")
+            if self._ha is not None:
+                ainfo = _lib.SolveInfo()
+                st = self.lib.obte_bte_kappa_gradient_adjoint(h, self._ha, C.byref(opts), C.c_void_p(dT0.data_ptr()),
+                                                              C.c_void_p(grad_t.data_ptr()), C.byref(info),
+                                                              C.byref(ainfo))
+                self.last_adjoint_info = ainfo
+                _lib.check(st, "obte_bte_kappa_gradient_adjoint")
+            else:
+                st = self.lib.obte_bte_kappa_gradient(h, C.byref(opts), C.c_void_p(dT0.data_ptr()),
+                                                      C.c_void_p(grad_t.data_ptr()), C.byref(info))
+                _lib.check(st, "obte_bte_kappa_gradient")
         finally:
             if not self.reuse_plan:
                 self.close()

@@ -129,3 +129,38 @@ def test_updated_plan_matches_new_plan(precision):
         g1, g2 = g1.cpu().numpy(), g2.cpu().numpy()
         np.testing.assert_allclose(g1, g2, rtol=0, atol=gtol * np.abs(g2).max())
     reused.close()
+
+
+def test_direction_set_not_closed_under_reversal_matches_oracle_adjoint():
+    """An odd number of directions (phi_q = 2 pi q / 15: no -s_q in the set): the adjoint comes from a second
+    plan with the reversed directions, whose forward solve is the transposed, reverse-order sweep of every
+    ordinate.  kappa and dkappa/drho against the oracle's explicit adjoint (A^T lam = dkappa/dX)."""
+    from openbte_gb300.inverse import IsotropicMaterial, PixelSolver
+    mfps, kappas = [0.05, 0.4, 2.0], [0.5, 0.3, 0.2]
+    rng = np.random.default_rng(11)
+    rho = rng.uniform(0.05, 1.0, 64)
+    grid = T.pixel_grid(8)
+    mat = T.material(mfps, kappas, 15)
+    k_ref, g_ref, _ = T.kappa_and_gradient(rho, grid, mat, method="adjoint")
+    solver = PixelSolver(8, IsotropicMaterial(mfps, kappas, 15), precision="fp64", rtol=1e-12)
+    assert solver.paired
+    k, g = solver.kappa_and_gradient(rho)
+    assert solver.last_adjoint_info is not None and solver.last_adjoint_info.converged
+    assert abs(k - k_ref) <= 1e-8 * abs(k_ref), (k, k_ref)
+    np.testing.assert_allclose(g.cpu().numpy(), g_ref, rtol=0, atol=1e-6 * np.abs(g_ref).max())
+    # a second density field on the same pair of plans (both get the new transmissions)
+    rho2 = np.clip(rho + 0.1 * rng.standard_normal(64), 0.05, 1.0)
+    k2_ref, g2_ref, _ = T.kappa_and_gradient(rho2, grid, mat, method="adjoint")
+    k2, g2 = solver.kappa_and_gradient(rho2)
+    assert abs(k2 - k2_ref) <= 1e-8 * abs(k2_ref)
+    np.testing.assert_allclose(g2.cpu().numpy(), g2_ref, rtol=0, atol=1e-6 * np.abs(g2_ref).max())
+
+
+def test_unpaired_gradient_of_an_open_direction_set_is_refused():
+    """Without the reversed plan the single-solve identity does not apply: OBTE_ERR_UNSUPPORTED."""
+    from openbte_gb300 import _lib
+    from openbte_gb300.inverse import IsotropicMaterial, PixelSolver
+    solver = PixelSolver(8, IsotropicMaterial([0.4], [1.0], 15), precision="fp64", rtol=1e-10)
+    solver.paired = False
+    with pytest.raises(_lib.OBTEError, match="closed under reversal"):
+        solver.kappa_and_gradient(np.full(64, 0.7))
