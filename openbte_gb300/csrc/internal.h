@@ -404,6 +404,7 @@ struct obte_plan_s {
   obte::DevBuf det_inv, det_wptr, det_went, det_ceoff;
   int64_t det_nce = -1;             // contact entries (-1: tables not built)
   float* xstore = nullptr;          // set during a gradient solve: final-pass per-ordinate temperatures
+  bool xstore_add = false;          // the final pass adds its temperatures to xstore (pass at a correction)
   double* xstore64 = nullptr;       // set during obte_bte_sweep_fields in FP64: the same in FP64
   obte::DevBuf fields_J, fields_K, fields_S;   // final-pass outputs of obte_bte_sweep_fields (discarded)
   // bounded-wait test (obte_bte_plan_test_wait_timeout): level unit whose bulk copy the sweeps skip

@@ -960,9 +960,9 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   // u + d is the pass at u plus the source-free pass at d.  d is small (the correction of a residual
   // near the FP32 stage tolerance), so the source-free pass runs in FP32: its rounding is ~1e-7 of
   // ‖K d‖, i.e. ~1e-12 of ‖u‖, far below any tolerance this mode accepts.  This replaces the second
-  // FP64 pass (FP64 sweeps run on GB300's narrow FP64 pipe, ~10x the time of an FP32 sweep).  A
-  // correction that is not small (‖d‖ > 1e-3 ‖u‖), and gradient solves (which keep the final pass's
-  // per-ordinate temperatures), get a full FP64 pass instead.
+  // FP64 pass (FP64 sweeps run on GB300's narrow FP64 pipe, ~10x the time of an FP32 sweep).  The
+  // per-ordinate temperatures a gradient solve keeps are affine in u as well: the pass at d adds its
+  // own to them.  A correction that is not small (‖d‖ > 1e-3 ‖u‖) gets a full FP64 pass instead.
   constexpr double kPass32Rtol = 5e-6;
   const bool fin32 = prec == OBTE_FP32;
   double* Fu = wk.Fu.as<double>();
@@ -970,7 +970,7 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   double* d = wk.delta.as<double>();
   const int steps = prec == OBTE_FP32_REFINE ? std::max(1, opts->refine_steps) : 0;
   const double inner = inner_tol;
-  const bool split = prec == OBTE_FP32_REFINE && plan->xstore == nullptr;
+  const bool split = prec == OBTE_FP32_REFINE;
   if (split && !wk.rc.p) {
     OBTE_TRY(wk.rc.alloc((size_t)wk.nu * sizeof(double)));
     OBTE_TRY(wk.Jraw2.alloc((size_t)s.n * s.ds * sizeof(double)));
@@ -1021,8 +1021,11 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
     full_pass = !split || dn > 1e-3 * unorm;
     if (!full_pass) {
       // F(u + d) = F(u) + K d; outputs likewise (source-free FP32 final pass at d)
-      OBTE_TRY(launch_sweep(plan, true, d, wk.tmp.as<double>(), false, true, wk.Jraw2.as<double>(),
-                            wk.Kraw2.as<double>(), wk.Sraw2.as<double>()));
+      plan->xstore_add = true;
+      const obte_status ds = launch_sweep(plan, true, d, wk.tmp.as<double>(), false, true, wk.Jraw2.as<double>(),
+                                          wk.Kraw2.as<double>(), wk.Sraw2.as<double>());
+      plan->xstore_add = false;
+      OBTE_TRY(ds);
       ++sv.sweeps;
       OBTE_TRY(sv.axpby(1.0, wk.tmp.as<double>(), 1.0, Fu));
       add_kernel<<<wk.nb, VT, 0, st>>>(wk.Jraw.as<double>(), wk.Jraw2.as<double>(), s.n * s.ds);

@@ -466,6 +466,7 @@ struct SweepParams {
   double* __restrict__ S_out;
   int* __restrict__ err;
   float* __restrict__ Xs;   // final pass only: per-ordinate temperatures [n_dir][n][n_mfp], or null
+  int xs_add;               // 1: add this pass's temperatures to Xs (the pass at a correction d)
   double* __restrict__ Xd;  // the same in FP64 (FP64 sweeps of obte_bte_sweep_fields), or null
   const int32_t* __restrict__ cta_map;   // CTA -> direction * n_chunks + chunk (a subset), or null: all
   // batched subset sweeps (batch_stride > 0): CTA b runs entry b % n_cta_batch of cta_map on the state
@@ -948,7 +949,10 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
         if (FINAL && p.Xs != nullptr) {
 #pragma unroll
           for (int j = 0; j < KV; ++j)
-            if (mo + j < mc) p.Xs[((int64_t)q * p.n + c) * p.n_mfp + m0 + mo + j] = (float)T[j];
+            if (mo + j < mc) {
+              float* xs = p.Xs + ((int64_t)q * p.n + c) * p.n_mfp + m0 + mo + j;
+              *xs = p.xs_add ? *xs + (float)T[j] : (float)T[j];
+            }
         }
         if (FINAL && p.Xd != nullptr) {
 #pragma unroll
@@ -1519,6 +1523,7 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S_out = S;
   p.err = plan->err.as<int>();
   p.Xs = FINAL ? plan->xstore : nullptr;
+  p.xs_add = plan->xstore_add ? 1 : 0;
   p.Xd = FINAL ? plan->xstore64 : nullptr;
   p.skip_unit = plan->test_skip_unit;
   p.wait_limit = plan->test_wait_limit > 0 ? plan->test_wait_limit : kWaitPolls;
@@ -1711,6 +1716,7 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.u_in = u_in; p.u_out = u_out; p.Jraw = nullptr; p.K = nullptr; p.S_out = nullptr;
   p.err = err;
   p.Xs = nullptr;
+  p.xs_add = 0;
   p.Xd = nullptr;
   // the launch order of obte_bte_sweep: longest chains first (FP32 tables), unless OBTE_SWEEP_NO_LPT is set
   static const bool index_order = std::getenv("OBTE_SWEEP_NO_LPT") != nullptr;

@@ -164,3 +164,22 @@ def test_unpaired_gradient_of_an_open_direction_set_is_refused():
     solver.paired = False
     with pytest.raises(_lib.OBTEError, match="closed under reversal"):
         solver.kappa_and_gradient(np.full(64, 0.7))
+
+
+def test_gradient_fields_through_the_correction_pass():
+    """FP32+refine gradient solves update the stored per-ordinate temperatures through the FP32 pass at the
+    refinement's correction d (X(u + d) = X(u) + X_0(d)) instead of a second FP64 pass: one FP64 sweep, and
+    the same gradient as the FP64 solve."""
+    from openbte_gb300.inverse import IsotropicMaterial, PixelSolver
+    rng = np.random.default_rng(5)
+    rho = rng.uniform(0.3, 1.0, 16 * 16)
+    mat = IsotropicMaterial([0.3, 2.0], [0.6, 0.4], 16)
+    s64 = PixelSolver(16, mat, precision="fp64", rtol=1e-12)
+    k64, g64 = s64.kappa_and_gradient(rho)
+    s32 = PixelSolver(16, mat, precision="fp32_refine", rtol=1e-10)
+    k32, g32 = s32.kappa_and_gradient(rho)
+    assert s32.last_info.n_sweeps_fp64 == 1, (s32.last_info.n_sweeps_fp64, s32.last_info.n_sweeps)
+    assert s32.last_info.residual <= 1e-10
+    assert abs(k32 - k64) <= 1e-9 * abs(k64), (k32, k64)
+    g32, g64 = g32.cpu().numpy(), g64.cpu().numpy()
+    np.testing.assert_allclose(g32, g64, rtol=0, atol=2e-6 * np.abs(g64).max())
