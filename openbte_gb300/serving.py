@@ -149,9 +149,20 @@ class GPUBackend:
         pl.uses = 1
         pl.solve_lock = threading.Lock()
         with self._lock:
-            self._cache[key] = pl
-            self._busy[key] += 1
-        return _Lease(pl, 0), self._footprint(pl, req), False
+            other = self._cache.get(key)
+            if other is not None:
+                # the same geometry was built by another thread meanwhile: share that plan, drop this one
+                self._cache.move_to_end(key)
+                self._busy[key] += 1
+                lease = _Lease(other, other.uses)
+                other.uses += 1
+                dup, pl = pl, other
+            else:
+                self._cache[key] = pl
+                self._busy[key] += 1
+                lease, dup = _Lease(pl, 0), None
+        del dup                  # a duplicate plan is destroyed here, outside the lock
+        return lease, self._footprint(pl, req), lease.use > 0
 
     def _new_plan(self, hp):
         from .runtime import Plan

@@ -277,3 +277,41 @@ def test_preconditioner_build_that_cannot_fit_is_dropped(monkeypatch):
     assert all(r.status == "ok" for r in res)
     assert srv.max_held <= 600
     assert [pc for _, pc, _ in be.seen] == [-1, -1, -1] and not plan.built
+
+
+def test_concurrent_builds_of_one_geometry_share_a_plan(monkeypatch):
+    """Two builder threads that miss the cache for the same geometry at once end up on one cached plan."""
+    import threading as th
+    import openbte_gb300.runtime as runtime
+    from openbte_gb300.serving import GPUBackend
+
+    class _HP:
+        def __init__(self, *a):
+            pass
+
+        def key(self):
+            return "same"
+
+    monkeypatch.setattr(runtime, "HostProblem", _HP)
+    gate = th.Barrier(2)
+    made = []
+
+    class Racy(GPUBackend):
+        def _new_plan(self, hp):
+            gate.wait(timeout=5)          # both threads are past the cache lookup
+            p = _PlanStub()
+            made.append(p)
+            return p
+
+    be = Racy()
+    out = []
+    ts = [th.Thread(target=lambda: out.append(be.build(Request(None, None, None, None)))) for _ in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert len(made) == 2 and len(be._cache) == 1
+    plans = {id(lease.plan) for lease, _, _ in out}
+    assert len(plans) == 1
+    assert sorted(lease.use for lease, _, _ in out) == [0, 1]
+    assert sorted(cached for _, _, cached in out) == [False, True]
