@@ -41,11 +41,24 @@ constexpr int XT = 256;
 constexpr int kDetect = 10;        // applications of the inflow map in the detection (OBTE_XPREC_DETECT)
 constexpr double kSlow = 0.35;     // norm kept by the last application above which an ordinate is slow
                                    // (OBTE_XPREC_SLOW)
-constexpr int kMaxSlots = 1024;    // largest block
+constexpr int kMaxSlots = 1024;    // largest block (OBTE_XPREC_MAX_SLOTS, at most kSlotsCap)
+constexpr int kSlotsCap = 4096;    // the inversion kernel's column buffer
 constexpr double kActive = 0.0;    // slots of a block: detection iterate above this fraction of its largest
                                    // (OBTE_XPREC_ACTIVE; 1e-3 took the largest block 348 -> 298 slots and
                                    // the setup 400 -> 294 ms but cost a sweep per solve on the 60k cell)
-constexpr double kMaxBytes = 1.0e9;
+constexpr double kMaxBytes = 1.0e9;  // dense blocks' memory (OBTE_XPREC_MAX_GB)
+
+int max_slots() {
+  int v = kMaxSlots;
+  if (const char* e = std::getenv("OBTE_XPREC_MAX_SLOTS")) v = std::atoi(e);
+  return std::max(1, std::min(v, kSlotsCap));
+}
+
+double max_bytes() {
+  double v = kMaxBytes;
+  if (const char* e = std::getenv("OBTE_XPREC_MAX_GB")) v = std::atof(e) * 1e9;
+  return v > 0 ? v : kMaxBytes;
+}
 
 // per-ordinate sum of squares of the inflow part: out[q * n_mfp + m]
 __global__ void xnorm_kernel(const double* __restrict__ x, int64_t xoff, const int64_t* __restrict__ x_base,
@@ -105,7 +118,7 @@ __global__ void xprobe_get_kernel(const int32_t* __restrict__ bm, const int32_t*
 __global__ void __launch_bounds__(1024) xprec_invert_kernel(const int32_t* __restrict__ bs,
                                                             const int64_t* __restrict__ bwoff, float* __restrict__ W,
                                                             int* __restrict__ bad) {
-  __shared__ float colk[kMaxSlots];
+  __shared__ float colk[kSlotsCap];
   const int b = blockIdx.x;
   const int s = bs[b], sp = row_stride(s);
   float* A = W + bwoff[b];
@@ -210,7 +223,7 @@ int64_t xprec_build_bound(obte_plan plan) {
   bool any_fits = false;
   for (int q = 0; q < s.n_dir && !any_fits; ++q) {
     const int64_t nsl = s.x_base[q + 1] - s.x_base[q];
-    any_fits = nsl > 0 && nsl <= kMaxSlots;
+    any_fits = nsl > 0 && nsl <= max_slots();
   }
   if (nsrc == 0 || s.n_mfp == 0 || !any_fits) return 0;
   const int64_t nord = (int64_t)s.n_dir * s.n_mfp;
@@ -218,7 +231,7 @@ int64_t xprec_build_bound(obte_plan plan) {
   // W (capped), per-block tables (at most one block per ordinate, every block's slots at most its
   // direction's), detection norms, CTA map, the batched probe vectors (16 pairs or 2 GB at most)
   const int64_t probes = std::min<int64_t>(16 * 2 * nu * (int64_t)sizeof(double), (int64_t)2e9);
-  return (int64_t)kMaxBytes + nord * (4 + 4 + 8 + 8 + 4 + 16 + 4) + nsrc * s.n_mfp * 4 + probes;
+  return (int64_t)max_bytes() + nord * (4 + 4 + 8 + 8 + 4 + 16 + 4) + nsrc * s.n_mfp * 4 + probes;
 }
 
 obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
@@ -234,7 +247,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   bool any_fits = false;
   for (int q = 0; q < s.n_dir && !any_fits; ++q) {
     const int64_t nsl = s.x_base[q + 1] - s.x_base[q];
-    any_fits = nsl > 0 && nsl <= kMaxSlots;
+    any_fits = nsl > 0 && nsl <= max_slots();
   }
   if (!any_fits) return OBTE_OK;
   OBTE_TRY(ensure_tables(plan, true));
@@ -304,7 +317,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
       c.ratio = std::sqrt(b / a);
       for (int64_t i = 0; i < nsl; ++i)
         if (hx[(size_t)i * s.n_mfp + m] > active * vmax) c.slots.push_back((int32_t)(s.x_base[q] + i));
-      if (!c.slots.empty() && (int)c.slots.size() <= kMaxSlots) cand.push_back(std::move(c));
+      if (!c.slots.empty() && (int)c.slots.size() <= max_slots()) cand.push_back(std::move(c));
     }
   }
   // memory cap: keep the slowest blocks
@@ -314,7 +327,7 @@ obte_status ensure_xprec(obte_plan plan, SolveWork& wk) {
   for (; keep < cand.size(); ++keep) {
     const int sz = (int)cand[keep].slots.size();
     const double bb = (double)sz * row_stride(sz) * sizeof(float);
-    if (bytes + bb > kMaxBytes) break;
+    if (bytes + bb > max_bytes()) break;
     bytes += bb;
   }
   cand.resize(keep);
