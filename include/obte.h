@@ -299,6 +299,15 @@ obte_status obte_bte_kappa_gradient_adjoint(obte_plan plan, obte_plan adjoint_pl
 /* Sizes of the state vector pieces: n_elems, n_diffuse, n_x. */
 obte_status obte_bte_state_layout(obte_plan plan, int64_t* n_elems, int64_t* n_diffuse, int64_t* n_x);
 /*
+ * The cell diffusion operator of the plan's diffusion-synthetic acceleration (obte_solve_opts.dsa), as
+ * built on the host (for inspection and tests; works on host-only plans): CSR over the elements, columns
+ * sorted, volume-weighted and symmetric.  Call with row_ptr = col = val = NULL to get *nnz; then with
+ * arrays of n_elems + 1 / *nnz / *nnz entries (*nnz = their capacity).  *project = 1 when the operator
+ * has the constant null vector (no isothermal walls) and a solve projects its source to zero sum.
+ */
+obte_status obte_bte_dsa_operator(obte_plan plan, int64_t* nnz, int32_t* row_ptr, int32_t* col, double* val,
+                                  int32_t* project);
+/*
  * Periodic-inflow preconditioner of the plan (no counterpart in the reference, whose per-ordinate
  * sparse LU solves the periodic coupling directly): built when obte_solve_opts.precond asks for it (by
  * default on the plan's second solve).  n_blocks: ordinates it covers (0: none, or not built yet);

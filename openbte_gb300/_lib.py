@@ -117,6 +117,8 @@ SIGNATURES = [
     ("obte_bte_precond_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                         C.POINTER(C.c_double)]),
     ("obte_bte_precond_bytes", C.c_int, [C.c_void_p, p_i64, p_i64]),
+    ("obte_bte_dsa_operator", C.c_int, [C.c_void_p, p_i64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.POINTER(C.c_int32)]),
     ("obte_bte_schedule", C.c_int, [C.c_void_p, C.c_int32, p_i64, p_i64, p_i64, p_i64]),
     ("obte_bte_schedule_coefficients", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("obte_bte_tables_digest", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint64)]),

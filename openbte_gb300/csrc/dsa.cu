@@ -22,7 +22,7 @@
 // max(F_mq . n, 0) (the half-range flux; two-stream balance of the transmitted and reflected streams at
 // the interface).  Periodic sides couple their elements like internal ones (the correction carries no
 // jump); diffuse walls are insulating; isothermal walls hold the correction at zero through
-// A sum_m 1 / (d / D_m + 1 / (2 G_m)).  No diagonal is below 5 % of the median (per volume): an element
+// A sum_m 1 / (d / D_m + 1 / (2 G_m)).  No diagonal is below 5 % of the (upper) median (per volume): an element
 // whose sides barely transmit keeps its slow mode to GMRES.  Without isothermal walls L has the constant
 // null vector, as I - K has the uniform shift: the source is projected onto zero mean and the
 // correction's volume-weighted mean removed, and a diagonal of 1e-6 of the largest keeps the hierarchy's
@@ -129,11 +129,9 @@ bool dsa_default(const Schedule& s) {
   return false;
 }
 
-obte_status ensure_dsa(obte_plan plan) {
-  if (plan->dsa) return OBTE_OK;
-  PhaseTimer timer("dsa setup");
-  const auto t0 = std::chrono::steady_clock::now();
-  const Schedule& s = plan->sched;
+// L as CSR (columns sorted, duplicates merged); `project`: L has the constant null vector
+void dsa_matrix(const Schedule& s, std::vector<int32_t>& rp, std::vector<int32_t>& ci, std::vector<double>& val,
+                bool& project) {
   const Schedule::DsaData& D = s.dsa;
   const int64_t n = s.n;
   const int n_mfp = s.n_mfp;
@@ -169,7 +167,7 @@ obte_status ensure_dsa(obte_plan plan) {
     for (int m = 0; m < n_mfp; ++m) c += 1.0 / (D.iso_dist[k] / D.Dm[m] + 0.5 / D.Gm[m]);
     diag[D.iso_cell[k]] += D.iso_area[k] * c;
   }
-  const bool project = D.iso_cell.empty();
+  project = D.iso_cell.empty();
   double dmax = 0;
   for (double v : diag) dmax = std::max(dmax, v);
   const double reg = 1e-6 * (dmax > 0 ? dmax : 1.0);
@@ -187,10 +185,10 @@ obte_status ensure_dsa(obte_plan plan) {
   }
   // CSR: diagonal first, then the neighbours in side order; two sides joining the same pair (periodic
   // images) stay separate entries
-  std::vector<int32_t> rp(n + 1, 0);
+  rp.assign(n + 1, 0);
   for (int64_t i = 0; i < n; ++i) rp[i + 1] = rp[i] + 1 + deg[i + 1];
-  std::vector<int32_t> ci(rp[n]);
-  std::vector<double> val(rp[n]);
+  ci.assign(rp[n], 0);
+  val.assign(rp[n], 0.0);
   std::vector<int32_t> pos(rp.begin(), rp.end() - 1);
   for (int64_t i = 0; i < n; ++i) {
     ci[pos[i]] = (int32_t)i;
@@ -229,6 +227,20 @@ obte_status ensure_dsa(obte_plan plan) {
     ci.swap(ci2);
     val.swap(val2);
   }
+}
+
+obte_status ensure_dsa(obte_plan plan) {
+  if (plan->dsa) return OBTE_OK;
+  PhaseTimer timer("dsa setup");
+  const auto t0 = std::chrono::steady_clock::now();
+  const Schedule& s = plan->sched;
+  const Schedule::DsaData& D = s.dsa;
+  const int64_t n = s.n;
+  const int64_t nfc = (int64_t)D.e1.size();
+  std::vector<int32_t> rp, ci;
+  std::vector<double> val;
+  bool project = true;
+  dsa_matrix(s, rp, ci, val, project);
   std::unique_ptr<DsaOp> op(new DsaOp());
   cudaStream_t st = plan->stream;
   OBTE_TRY(amg_build(n, rp, ci, val, -1, plan->ctx->num_sms, st, op->amg));
@@ -284,3 +296,23 @@ void dsa_add(obte_plan plan, const double* in, double* out) {
 }
 
 }  // namespace obte
+
+using namespace obte;
+
+extern "C" obte_status obte_bte_dsa_operator(obte_plan plan, int64_t* nnz, int32_t* row_ptr, int32_t* col,
+                                             double* val, int32_t* project) {
+  if (!plan || !nnz) { set_error("null argument"); return OBTE_ERR_BAD_ARG; }
+  std::vector<int32_t> rp, ci;
+  std::vector<double> v;
+  bool proj = true;
+  dsa_matrix(plan->sched, rp, ci, v, proj);
+  const int64_t cap = *nnz;
+  *nnz = (int64_t)ci.size();
+  if (project) *project = proj ? 1 : 0;
+  if (!row_ptr && !col && !val) return OBTE_OK;          // size query
+  if (cap < (int64_t)ci.size()) { set_error("dsa operator: arrays too small"); return OBTE_ERR_BAD_ARG; }
+  if (row_ptr) std::copy(rp.begin(), rp.end(), row_ptr);
+  if (col) std::copy(ci.begin(), ci.end(), col);
+  if (val) std::copy(v.begin(), v.end(), val);
+  return OBTE_OK;
+}

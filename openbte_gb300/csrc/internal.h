@@ -443,6 +443,8 @@ int64_t xprec_resident_bytes(const XPrec* P);
 obte_status ensure_dsa(obte_plan plan);
 void dsa_add(obte_plan plan, const double* in, double* out);    // out += E L^-1 R in
 bool dsa_default(const Schedule& s);                            // on by default for this problem?
+void dsa_matrix(const Schedule& s, std::vector<int32_t>& rp, std::vector<int32_t>& ci, std::vector<double>& val,
+                bool& project);                                 // the diffusion operator (host)
 int64_t xprec_build_bound(obte_plan plan);   // device bytes a build would allocate (0 once tried)
 obte_status check_device_error(obte_plan plan);
 // Plan-owned J, K, S buffers for sweeps whose final-pass accumulations are discarded (api.cu).
