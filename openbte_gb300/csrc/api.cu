@@ -392,7 +392,15 @@ extern "C" obte_status obte_bte_plan_footprint(obte_plan plan, int32_t precision
     return (int64_t)b;
   };
   // tables that are uploaded count with their actual size, the others with an upper estimate
-  const int64_t t64 = plan->d64.ready ? (int64_t)plan->d64.bytes() : tab(8);
+  // FP64 tables before upload: plus the reciprocal table (n_dir x n x the MFPs rounded up to a chunk), unless
+  // it is switched off or over its cap
+  int64_t rinv_est = (int64_t)s.n_dir * s.n * ((s.n_mfp + 3) & ~3) * 8;
+  {
+    const char* off = std::getenv("OBTE_SWEEP64_RINV");
+    const char* cap = std::getenv("OBTE_SWEEP64_RINV_GB");
+    if ((off && std::atoi(off) == 0) || (double)rinv_est > (cap ? std::atof(cap) : 32.0) * 1e9) rinv_est = 0;
+  }
+  const int64_t t64 = plan->d64.ready ? (int64_t)plan->d64.bytes() : tab(8) + rinv_est;
   const int64_t t32 = plan->d32.ready ? (int64_t)plan->d32.bytes() : tab(4);
   int64_t pb = (int64_t)plan->nu * 8 + (int64_t)s.x_cell.size() * 4 + (int64_t)s.kconst.size() * 24;
   if (precision == OBTE_FP64) pb += t64;

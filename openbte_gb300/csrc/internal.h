@@ -319,6 +319,9 @@ struct DevSchedule {
   DevBuf rec, klev_ptr, klev_off, knlev, kwo, kpf, pf, sx, ksx, mfp, tco, sig, wo_wall, wo_geo, kcoef, scoef, hs, vals, cellmap,
       Pq, si, sr, wo_off, spec;
   DevBuf lpt;                              // launch order: CTAs of the directions with the most units first
+  // FP64 tables: 1 / (1 + mfp_m D) per (direction, chunk, position, MFP of the chunk), so that the FP64
+  // sweep multiplies instead of dividing on GB300's narrow FP64 pipe (null when over its memory cap)
+  DevBuf rinv;
   // deterministic reductions (OBTE_DETERMINISTIC=1): per-(direction, chunk) partials and per-position sums
   DevBuf det_d, det_j, det_w, det_k, det_s, det_S, det_SJ;
   // transmission plans: host copies of the packed records and of the special-entry index, so that new
@@ -344,9 +347,6 @@ struct SolveWork {
   HostBuf hcol;      // pinned copy of the Hessenberg column
 };
 
-// Right preconditioner of the GMRES on the periodic-inflow unknowns: for the ordinates whose inflow
-// circulates through the periodic cell for many periods, the exact inverse of their one-period
-// inflow -> outflow transfer, (I - T_b)^-1 - I, as a dense FP32 block over the direction's source slots.
 // Diffusion-synthetic acceleration (dsa.cu): right preconditioner term E L^-1 R, with R the volume-
 // weighted temperature part of a state vector, L the cell diffusion operator of Schedule::DsaData solved
 // by `cycles` stationary smoothed-aggregation V-cycle iterations (a fixed linear map, as GMRES needs), and
@@ -365,6 +365,9 @@ struct DsaOp {
   int64_t bytes = 0;             // device bytes held
 };
 
+// Right preconditioner of the GMRES on the periodic-inflow unknowns: for the ordinates whose inflow
+// circulates through the periodic cell for many periods, the exact inverse of their one-period
+// inflow -> outflow transfer, (I - T_b)^-1 - I, as a dense FP32 block over the direction's source slots.
 struct XPrec {
   bool tried = false;            // setup ran (blocks may still be empty)
   int nblk = 0, smax = 0;

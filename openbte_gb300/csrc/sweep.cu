@@ -465,6 +465,7 @@ struct SweepParams {
   double* __restrict__ K;
   double* __restrict__ S_out;
   int* __restrict__ err;
+  const double* __restrict__ rinv;   // FP64: 1 / (1 + mfp D) [n_dir][n_chunks][n][MC], or null: divide
   float* __restrict__ Xs;   // final pass only: per-ordinate temperatures [n_dir][n][n_mfp], or null
   int xs_add;               // 1: add this pass's temperatures to Xs (the pass at a correction d)
   double* __restrict__ Xd;  // the same in FP64 (FP64 sweeps of obte_bte_sweep_fields), or null
@@ -805,6 +806,13 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
   // the value window of a unit starts (q n + a) pairs into the array; FP32 pairs are 8 bytes, so the
   // 16-byte aligned window starts one pair early when q n + a is odd (FP64 pairs are 16 bytes: never)
   const int qn_odd = (int)(((int64_t)q * p.n) & 1);
+  // FP64 with the reciprocal table: this element's 1 / (1 + mfp D) for the current unit, and for the next
+  // unit loaded one unit ahead (a coalesced 16-byte global load per lane, off the unit's critical path)
+  constexpr bool kRinv = sizeof(Real) == 8 && !DF;
+  double rcur[KV], rnxt[KV];
+  const double* __restrict__ rinv_qc =
+      (kRinv && p.rinv) ? p.rinv + ((int64_t)q * p.n_chunks + chunk) * p.n * MC : nullptr;
+  if (rinv_qc && nlev > 0 && el < e - a) vload(rinv_qc + (int64_t)(a + el) * MC + mo, rcur);
   int bi = 0;            // buffer of unit u (u mod nbuf)
   unsigned phase = 0;    // parity of its mbarrier phase ((u / nbuf) & 1)
   for (int u = 0; u < nlev; ++u) {
@@ -813,6 +821,7 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
     const int kpf3 = u + 3 <= nlev ? kpf[u + 3] : 0;
     const int npf = u + 1 < nlev ? kpf2 - kpf1 : 0;   // padded length of unit u+1's list
     const int prow_next = prow0 + ((u + 1) & 1) * p.emax;
+    if (rinv_qc && u + 1 < nlev && el < e_next - e) vload(rinv_qc + (int64_t)(e + el) * MC + mo, rnxt);
     // buffer (u + nbuf - 1) mod nbuf was last read during unit u - 1, finished at the barrier below
     if (tid == kIssuer && u + nbuf - 1 < nlev) issue(u + nbuf - 1, bi == 0 ? nbuf - 1 : bi - 1);
     const bool ready = mbar_wait_bounded(&bars[bi], phase, p.wait_limit);
@@ -935,7 +944,8 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
           for (int j = 0; j < KV; ++j) {
             Real sm = c0 * v0[j] + c1 * v1[j] + c2 * v2[j];
             if (NF > 3) sm += c3 * v3[j];
-            T[j] = quot(b + lam[j] * (pw - sm), Real(1) + lam[j] * D);
+            if (kRinv && rinv_qc) T[j] = (Real)((b + lam[j] * (pw - sm)) * rcur[j]);
+            else T[j] = quot(b + lam[j] * (pw - sm), Real(1) + lam[j] * D);
             dacc += tt[j] * T[j];
             if (FINAL) {
               const Real* sj = s_sig + (mo + j) * 3;
@@ -1073,6 +1083,10 @@ __global__ void __launch_bounds__(kUnit * G, SweepMinBlocks<Real, G, KV>::v) bte
     wu = wu_next;
     kpf1 = kpf2;
     kpf2 = kpf3;
+    if (rinv_qc) {
+#pragma unroll
+      for (int j = 0; j < KV; ++j) rcur[j] = rnxt[j];
+    }
   }
   if (FINAL && !p.det) {
     for (int j = tid; j < mc; j += blockDim.x) {
@@ -1162,7 +1176,7 @@ __global__ void det_contact_sum_kernel(const Real* __restrict__ kpart, const Rea
 
 size_t DevSchedule::bytes() const {
   const DevBuf* all[] = {&rec, &klev_ptr, &klev_off, &knlev, &kwo, &kpf, &pf, &sx, &ksx, &mfp, &tco, &sig, &wo_wall, &wo_geo,
-                         &kcoef, &scoef, &hs, &vals, &cellmap, &Pq, &si, &sr, &wo_off, &spec, &lpt};
+                         &kcoef, &scoef, &hs, &vals, &cellmap, &Pq, &si, &sr, &wo_off, &spec, &lpt, &rinv};
   size_t b = 0;
   for (auto* x : all) b += x->bytes;
   return b;
@@ -1413,6 +1427,55 @@ obte_status refresh_tables(obte_plan plan, int64_t* bytes) {
   return OBTE_OK;
 }
 
+// 1 / (1 + mfp_m D) for every (direction, chunk, position, MFP of the chunk) of the FP64 tables, D read
+// from the packed records (padded MFPs: 1, as their mfp is 0)
+template <int NF>
+__global__ void rinv_build_kernel(const int32_t* __restrict__ rec, int64_t n, int n_dir, int n_chunks, int mcp,
+                                  int n_mfp, const double* __restrict__ mfp, double* __restrict__ out) {
+  using RR = Rec<double, NF>;
+  const int64_t total = (int64_t)n_dir * n_chunks * n * mcp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i % mcp);
+    int64_t t = i / mcp;
+    const int64_t pos = t % n;
+    t /= n;
+    const int chunk = (int)(t % n_chunks);
+    const int64_t q = t / n_chunks;
+    const int m = chunk * mcp + j;
+    const int32_t* r = rec + (q * n + pos) * RR::W;
+    const double D = __hiloint2double(r[RR::D + 1], r[RR::D]);
+    const double L = m < n_mfp ? mfp[m] : 0.0;
+    out[i] = 1.0 / (1.0 + L * D);
+  }
+}
+
+// The FP64 reciprocal table, unless OBTE_SWEEP64_RINV=0 or it would exceed OBTE_SWEEP64_RINV_GB (default 32)
+// or device memory (the sweep then divides)
+static obte_status build_rinv(obte_plan plan, DevSchedule& d) {
+  const Schedule& s = plan->sched;
+  if (const char* e = std::getenv("OBTE_SWEEP64_RINV"))
+    if (std::atoi(e) == 0) return OBTE_OK;
+  double cap_gb = 32.0;
+  if (const char* e = std::getenv("OBTE_SWEEP64_RINV_GB")) cap_gb = std::atof(e);
+  const int64_t total = (int64_t)s.n_dir * d.n_chunks * s.n * d.mcp;
+  if ((double)total * 8.0 > cap_gb * 1e9 || (s.nf != 3 && s.nf != 4)) return OBTE_OK;
+  if (d.rinv.alloc((size_t)total * sizeof(double)) != OBTE_OK) {
+    cudaGetLastError();
+    d.rinv.release();
+    return OBTE_OK;            // no room: the sweep divides
+  }
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)plan->ctx->num_sms * 16);
+  if (s.nf == 3)
+    rinv_build_kernel<3><<<blocks, 256, 0, plan->stream>>>(d.rec.as<int32_t>(), s.n, s.n_dir, d.n_chunks, d.mcp,
+                                                            s.n_mfp, d.mfp.as<double>(), d.rinv.as<double>());
+  else
+    rinv_build_kernel<4><<<blocks, 256, 0, plan->stream>>>(d.rec.as<int32_t>(), s.n, s.n_dir, d.n_chunks, d.mcp,
+                                                            s.n_mfp, d.mfp.as<double>(), d.rinv.as<double>());
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  return OBTE_OK;
+}
+
 obte_status ensure_tables(obte_plan plan, bool fp32) {
   if (!plan->err.p) {
     OBTE_TRY(plan->err.alloc(sizeof(int)));
@@ -1421,7 +1484,10 @@ obte_status ensure_tables(obte_plan plan, bool fp32) {
   if (fp32) {
     if (!plan->d32.ready) return upload_tables<float>(plan, plan->d32);
   } else {
-    if (!plan->d64.ready) return upload_tables<double>(plan, plan->d64);
+    if (!plan->d64.ready) {
+      OBTE_TRY(upload_tables<double>(plan, plan->d64));
+      OBTE_TRY(build_rinv(plan, plan->d64));
+    }
   }
   return OBTE_OK;
 }
@@ -1522,6 +1588,7 @@ static obte_status launch_impl(obte_plan plan, const DevSchedule& d, const doubl
   p.kcoef = d.kcoef.as<Real>(); p.scoef = d.scoef.as<Real>();
   p.u_in = u_in; p.u_out = u_out; p.Jraw = Jraw; p.K = K; p.S_out = S;
   p.err = plan->err.as<int>();
+  p.rinv = (sizeof(Real) == 8 && !DF) ? d.rinv.as<double>() : nullptr;
   p.Xs = FINAL ? plan->xstore : nullptr;
   p.xs_add = plan->xstore_add ? 1 : 0;
   p.Xd = FINAL ? plan->xstore64 : nullptr;
@@ -1717,6 +1784,7 @@ static obte_status launch_static_impl(obte_plan plan, const DevSchedule& d, cons
   p.err = err;
   p.Xs = nullptr;
   p.xs_add = 0;
+  p.rinv = nullptr;
   p.Xd = nullptr;
   // the launch order of obte_bte_sweep: longest chains first (FP32 tables), unless OBTE_SWEEP_NO_LPT is set
   static const bool index_order = std::getenv("OBTE_SWEEP_NO_LPT") != nullptr;

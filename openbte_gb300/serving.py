@@ -78,6 +78,16 @@ class Result:
 
 # sweep-table sets a solve of each precision reads (FP32+refine: FP32 sweeps and one FP64 pass)
 _TABLES = {"fp64": {"fp64"}, "fp32": {"fp32"}, "fp32_refine": {"fp32", "fp64"}}
+# FP32+refine at this tolerance or looser runs no FP64 sweep (its output pass is FP32, obte_bte_solve), so
+# its plan needs only the FP32 tables
+_PASS32_RTOL = 5e-6
+
+
+def _table_precision(req) -> str:
+    """The precision whose device tables a request's solve reads."""
+    if req.precision == "fp32_refine" and req.rtol >= _PASS32_RTOL:
+        return "fp32"
+    return req.precision
 
 
 class _Lease:
@@ -171,7 +181,7 @@ class GPUBackend:
             return Plan(hp, self.device, stream=st.cuda_stream)
 
     def _footprint(self, pl, req):
-        a, b = pl.footprint(req.precision, self.restart)
+        a, b = pl.footprint(_table_precision(req), self.restart)
         return int(a + b)
 
     def _precond_bound(self, lease) -> int:
@@ -185,7 +195,7 @@ class GPUBackend:
         """Device bytes that preparing and solving `req` on the lease's plan adds (0 for a plan already
         prepared for it, unless this solve builds the preconditioner)."""
         pl = lease.plan
-        tables = 0 if _TABLES[req.precision] <= pl.tables else max(0, self._footprint(pl, req) - pl.resident)
+        tables = 0 if _TABLES[_table_precision(req)] <= pl.tables else max(0, self._footprint(pl, req) - pl.resident)
         return tables + self._precond_bound(lease)
 
     def drop_optional(self, lease) -> bool:
@@ -200,14 +210,14 @@ class GPUBackend:
         from here on the bytes the server reserved for the request count in ``resident_bytes``."""
         pl = lease.plan
         bound = self._precond_bound(lease)
-        if not _TABLES[req.precision] <= pl.tables:
+        if not _TABLES[_table_precision(req)] <= pl.tables:
             with pl.solve_lock:          # not while another request solves on the plan
-                if not _TABLES[req.precision] <= pl.tables:
+                if not _TABLES[_table_precision(req)] <= pl.tables:
                     self._prepare_plan(pl, req)
                     with self._lock:
-                        pl.tables |= _TABLES[req.precision]
+                        pl.tables |= _TABLES[_table_precision(req)]
         with self._lock:
-            pl.tables |= _TABLES[req.precision]
+            pl.tables |= _TABLES[_table_precision(req)]
             pl.resident = max(pl.resident, self._footprint(pl, req))
             if bound:
                 lease.builds_precond = True
@@ -216,7 +226,7 @@ class GPUBackend:
     def _prepare_plan(self, pl, req):
         st = self._stream()
         pl.set_stream(st.cuda_stream)
-        pl.prepare(req.precision, self.restart)
+        pl.prepare(_table_precision(req), self.restart)
 
     def resident_bytes(self) -> int:
         with self._lock:
