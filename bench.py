@@ -48,6 +48,9 @@ WORKLOADS = {
     "c2_100k_30x16x32": (100000, 30, (16, 32), 0.10, "sphere", 1),
     # the 3D benchmark mesh with 4 x 8 directions: device tables of ~0.5 GB, for profiler captures
     "c2_100k_30x4x8": (100000, 30, (4, 8), 0.10, "sphere", 1),
+    # the 2D cell at a third of the benchmark size: FP64 tables with their reciprocal table ~2 GB, for
+    # profiler captures of the FP64 sweep
+    "c1_20k_100x96": (20000, 100, 96, 0.25, "square", 1),
     # inverse design: pixels per side, n_mfp, n_dir, density-field seed
     "c4_inverse_128x50x64": (128, 50, 64, None, "pixels", 0),
 }
