@@ -65,10 +65,11 @@ L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes of one sweep launch (dram__bytes.sum.per_second x gpu__time_duration of one ncu capture of
 # `bench.py --workload <w> --profile-sweeps 2` with the current kernel; profiles/bte_sweep_*.md); the
 # iterate stays in shared memory, so this is about an eighth of the algorithmic bytes
-SWEEP_DRAM_BYTES = {("c1_60k_100x96", "fp32"): 2.873e8, ("c1_60k_100x96", "fp64"): 4.299e8,
-                    ("c2_100k_30x4x8", "fp32"): 2.501e8}
+SWEEP_DRAM_BYTES = {("c1_60k_100x96", "fp32"): 2.873e8, ("c1_60k_100x96", "fp64"): 5.1e9,
+                    ("c1_20k_100x96", "fp64"): 1.70e9, ("c2_100k_30x4x8", "fp32"): 2.501e8}
 SWEEP_DRAM_SOURCE = {("c1_60k_100x96", "fp32"): "profiles/bte_sweep_fp32_c1_60k_100x96.md",
-                     ("c1_60k_100x96", "fp64"): "profiles/bte_sweep_fp64_c1_60k_100x96.md",
+                     ("c1_60k_100x96", "fp64"): "profiles/bte_sweep_fp64_c1_20k_100x96.md (scaled by elements)",
+                     ("c1_20k_100x96", "fp64"): "profiles/bte_sweep_fp64_c1_20k_100x96.md",
                      ("c2_100k_30x4x8", "fp32"): "profiles/bte_sweep_fp32_c2_110k_30x4x8.md"}
 
 
