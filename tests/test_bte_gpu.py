@@ -144,3 +144,31 @@ def test_fp32_refine_loose_tolerance_runs_no_fp64_sweep(case, monkeypatch):
     r64 = BTE_RTA(geo, mat, bcs, fourier=f, effective_thermal_conductivity=ek, bte_rtol=1e-5, precision="fp32_refine")
     assert r64.aux["n_sweeps_fp64"] >= 1
     assert abs(r.kappa_eff - r64.kappa_eff) / abs(r64.kappa_eff) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["c0_2k", "cube1k5"])
+def test_fp64_sweep_with_and_without_the_reciprocal_table(case, monkeypatch, name):
+    """FP64 sweeps multiply by the plan's table of 1 / (1 + mfp D); with the table off (OBTE_SWEEP64_RINV=0)
+    they divide (an FP32 seed with one quotient correction, relative error <= 2^-42).  Both give the same sweep
+    to 1e-12 of the largest output, with and without the source."""
+    import ctypes as C
+    import torch
+    from openbte_gb300 import _lib
+    from openbte_gb300.runtime import HostProblem, Plan
+    geo, mat, bcs, ek, d = case(name)
+    rng = np.random.default_rng(6)
+    outs = {}
+    for rinv in ("1", "0"):
+        monkeypatch.setenv("OBTE_SWEEP64_RINV", rinv)
+        plan = Plan(HostProblem(geo, mat, bcs, ek))
+        u = torch.tensor(rng.standard_normal(plan.nu) if rinv == "1" else outs["u"], dtype=torch.float64,
+                         device="cuda")
+        outs["u"] = u.cpu().numpy()
+        for src in (1, 0):
+            out = torch.zeros_like(u)
+            _lib.check(plan.lib.obte_bte_sweep(plan.handle, _lib.PRECISION["fp64"], C.c_void_p(u.data_ptr()),
+                                               C.c_void_p(out.data_ptr()), src), "fp64")
+            outs[(rinv, src)] = out.cpu().numpy()
+    for src in (1, 0):
+        a, b = outs[("1", src)], outs[("0", src)]
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-12 * np.abs(b).max())
