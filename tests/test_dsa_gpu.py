@@ -66,3 +66,32 @@ def test_dsa_on_a_porous_cell_keeps_the_fixed_point():
     (k0, t0, s0), (k1, t1, s1) = res[-1], res[1]
     assert abs(k1 - k0) <= 1e-8 * abs(k0), (k0, k1)
     assert np.max(np.abs(t1 - t0)) <= 1e-7 * np.max(np.abs(t0))
+
+
+def test_dsa_with_isothermal_walls_matches_oracle():
+    """Forced on with isothermal walls (the diffusion operator holds the correction at zero there and has no
+    null vector, so no projection): kappa and the temperature field of the oracle to 1e-9."""
+    import bte_oracle
+    from openbte_gb300 import BTE_RTA, objects as O
+    from openbte_gb300.geometry import porous_cell_2d
+    from openbte_gb300.material import synthetic_isotropic_2d
+    from openbte_gb300.mesh import mesh_from_cell
+    geo = mesh_from_cell(porous_cell_2d(500, 0.2, "circle", seed=9))
+    mat = synthetic_isotropic_2d(6, 12)
+    bcs = O.BoundaryConditions(periodic={"Periodic_x": 1, "Periodic_y": 0},
+                               mixed={"Boundary": {"value": 0.3, "boundary_conductance": 1e3}})
+    ek = O.EffectiveThermalConductivity(normalization=-1, contact="Periodic_x")
+    k_ref, dT_ref, *_ = bte_oracle.bte_rta(geo, mat, bcs, effective_thermal_conductivity=ek, bte_rtol=1e-13,
+                                           bte_max_iter=3000)
+    r = BTE_RTA(geo, mat, bcs, effective_thermal_conductivity=ek, bte_rtol=1e-11, precision="fp64", dsa=1)
+    assert abs(r.aux["kappa_eff"] - k_ref) <= 1e-9 * abs(k_ref), (r.aux["kappa_eff"], k_ref)
+    dT = r.variables["Temperature_BTE"]["data"]
+    assert np.abs(dT - dT_ref).max() <= 1e-8 * np.abs(dT_ref).max()
+
+
+def test_dsa_on_the_3d_cube_keeps_the_fixed_point(case):
+    """Forced on in 3D (tetrahedra, spherical pore): the reference's kappa (golden cube1k5) to 1e-6."""
+    from openbte_gb300 import BTE_RTA
+    geo, mat, bcs, ek, d = case("cube1k5")
+    r = BTE_RTA(geo, mat, bcs, effective_thermal_conductivity=ek, bte_rtol=1e-10, precision="fp64", dsa=1)
+    assert abs(r.kappa_eff - d["bte_kappa"]) <= 1e-6 * abs(d["bte_kappa"]), (r.kappa_eff, d["bte_kappa"])
