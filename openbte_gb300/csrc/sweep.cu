@@ -614,10 +614,19 @@ template <> struct V16<double> { static constexpr int K = 2; };
 
 template <int K>
 __device__ __forceinline__ void vload(const float* p, float (&x)[K]) {
+  if constexpr (K % 4 == 0) {
 #pragma unroll
-  for (int i = 0; i < K; i += 4) {
-    const float4 v = *reinterpret_cast<const float4*>(p + i);
-    x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
+    for (int i = 0; i < K; i += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(p + i);
+      x[i] = v.x; x[i + 1] = v.y; x[i + 2] = v.z; x[i + 3] = v.w;
+    }
+  } else {                 // 2 FP32 MFPs per lane: 8-byte rows
+    static_assert(K % 2 == 0, "an even number of FP32 MFPs per lane");
+#pragma unroll
+    for (int i = 0; i < K; i += 2) {
+      const float2 v = *reinterpret_cast<const float2*>(p + i);
+      x[i] = v.x; x[i + 1] = v.y;
+    }
   }
 }
 template <int K>
@@ -630,8 +639,13 @@ __device__ __forceinline__ void vload(const double* p, double (&x)[K]) {
 }
 template <int K>
 __device__ __forceinline__ void vstore(float* p, const float (&x)[K]) {
+  if constexpr (K % 4 == 0) {
 #pragma unroll
-  for (int i = 0; i < K; i += 4) *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
+    for (int i = 0; i < K; i += 4) *reinterpret_cast<float4*>(p + i) = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < K; i += 2) *reinterpret_cast<float2*>(p + i) = make_float2(x[i], x[i + 1]);
+  }
 }
 template <int K>
 __device__ __forceinline__ void vstore(double* p, const double (&x)[K]) {
@@ -1192,7 +1206,7 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
 // Compiled thread shapes (lanes per element G, MFPs per lane KV) for each precision.
 struct Shape { int G, KV; };
 template <typename Real> struct Shapes;
-template <> struct Shapes<float> { static constexpr Shape v[] = {{1, 4}, {1, 8}, {2, 4}}; };
+template <> struct Shapes<float> { static constexpr Shape v[] = {{1, 4}, {1, 8}, {2, 4}, {1, 2}}; };
 template <> struct Shapes<double> { static constexpr Shape v[] = {{1, 2}, {1, 4}, {2, 2}}; };
 constexpr Shape Shapes<float>::v[];
 constexpr Shape Shapes<double>::v[];
@@ -1670,7 +1684,7 @@ obte_status launch_sweep(obte_plan plan, bool fp32, const double* u_in, double* 
 #define OBTE_W(R, GG, KK) \
   if (d.G == GG && d.KV == KK) return launch_w<R, GG, KK>(plan, d, u_in, u_out, with_src, final_pass, Jraw, K, S)
   if (fp32) {
-    OBTE_W(float, 1, 4); OBTE_W(float, 1, 8); OBTE_W(float, 2, 4);
+    OBTE_W(float, 1, 4); OBTE_W(float, 1, 8); OBTE_W(float, 2, 4); OBTE_W(float, 1, 2);
   } else {
     OBTE_W(double, 1, 2); OBTE_W(double, 1, 4); OBTE_W(double, 2, 2);
   }
@@ -1825,7 +1839,7 @@ static obte_status sweep_static_on_device(obte_plan plan, bool fp32, const doubl
 #define OBTE_SW(R, GG, KK) \
   if (d.G == GG && d.KV == KK) rc = launch_static_w<R, GG, KK>(plan, d, u_in, u_out, with_src, static_cast<R*>(vals), err)
   if (fp32) {
-    OBTE_SW(float, 1, 4); else OBTE_SW(float, 1, 8); else OBTE_SW(float, 2, 4);
+    OBTE_SW(float, 1, 4); else OBTE_SW(float, 1, 8); else OBTE_SW(float, 2, 4); else OBTE_SW(float, 1, 2);
   } else {
     OBTE_SW(double, 1, 2); else OBTE_SW(double, 1, 4); else OBTE_SW(double, 2, 2);
   }
