@@ -355,7 +355,8 @@ static obte_status upload_csr(const HostCsr& A, DevCsr& d, cudaStream_t st) {
 }
 
 obte_status amg_build(int64_t n, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
-                      const std::vector<double>& val, int pin, int num_sms, cudaStream_t st, AmgPtr& out) {
+                      const std::vector<double>& val, int pin, int num_sms, cudaStream_t st, AmgPtr& out,
+                      int coarse_max) {
   PhaseTimer timer("amg_build");
   if (n >= (int64_t)1 << 31 || rp.back() < 0) { set_error("AMG: matrix too large"); return OBTE_ERR_BAD_ARG; }
   HostCsr A;
@@ -394,7 +395,7 @@ obte_status amg_build(int64_t n, const std::vector<int32_t>& rp, const std::vect
     }
     HostCsr Q, Ac;
     double omega = 0;
-    const bool more = A.n > 400 && H->lv.size() < 12 && coarsen(A, theta, Q, Ac, omega);
+    const bool more = A.n > coarse_max && H->lv.size() < 12 && coarsen(A, theta, Q, Ac, omega);
     if (!more) {
       std::vector<double> inv;
       if (!dense_inverse(A, inv)) { set_error("AMG: singular coarsest operator"); return OBTE_ERR_BAD_ARG; }

@@ -243,7 +243,9 @@ obte_status ensure_dsa(obte_plan plan) {
   dsa_matrix(s, rp, ci, val, project);
   std::unique_ptr<DsaOp> op(new DsaOp());
   cudaStream_t st = plan->stream;
-  OBTE_TRY(amg_build(n, rp, ci, val, -1, plan->ctx->num_sms, st, op->amg));
+  // rebuilt for every density field of a design loop: coarsen down to 64 rows, whose dense inverse costs
+  // little (the default 400 rows took ~15 of the ~18 ms of set-up on 128^2 pixels)
+  OBTE_TRY(amg_build(n, rp, ci, val, -1, plan->ctx->num_sms, st, op->amg, 64));
   OBTE_TRY(upload(op->rp, rp, st));
   OBTE_TRY(upload(op->ci, ci, st));
   OBTE_TRY(upload(op->val, val, st));

@@ -160,9 +160,11 @@ struct AmgDeleter {
   void operator()(AmgHierarchy* h) const;
 };
 using AmgPtr = std::unique_ptr<AmgHierarchy, AmgDeleter>;
-// Hierarchy of the SPD CSR matrix (rp, ci, val); row `pin` (>= 0) is replaced by the identity.
+// Hierarchy of the SPD CSR matrix (rp, ci, val); row `pin` (>= 0) is replaced by the identity.  Coarsening
+// stops at `coarse_max` rows or fewer, whose operator is inverted densely (host Gauss-Jordan, O(rows^3)).
 obte_status amg_build(int64_t n, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
-                      const std::vector<double>& val, int pin, int num_sms, cudaStream_t st, AmgPtr& out);
+                      const std::vector<double>& val, int pin, int num_sms, cudaStream_t st, AmgPtr& out,
+                      int coarse_max = 400);
 // Enqueue z = M^-1 r (one symmetric V-cycle) on `st`; with `part`, also the nb_part block partials of
 // r . z (launched on exactly nb_part blocks).  Returns the number of kernel launches.
 int amg_apply(const AmgHierarchy& H, const double* r, double* z, double* part, int nb_part, cudaStream_t st);
@@ -327,6 +329,15 @@ struct DevSchedule {
   // transmission plans: host copies of the packed records and of the special-entry index, so that new
   // transmissions rewrite the coefficient words in place (refresh_tables)
   RawVec<int32_t> h_rec, h_spec;
+  // h_rec page-locked on its first re-upload (the records are re-sent for every new set of transmissions);
+  // unregistered before h_rec is freed (members are destroyed in reverse order)
+  struct HostPin {
+    void* p = nullptr;
+    HostPin() = default;
+    HostPin(const HostPin&) = delete;
+    HostPin& operator=(const HostPin&) = delete;
+    ~HostPin() { if (p) cudaHostUnregister(p); }
+  } h_rec_pin;
   int64_t n_spec = 0;
   size_t bytes() const;
 };

@@ -1203,6 +1203,20 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
   return upload(b, h, st);
 }
 
+// The same into the buffer's existing allocation when the size matches (no cudaMalloc / cudaFree, which
+// synchronise the device), else as upload_real.  The copy is complete when this returns.
+template <typename Real>
+static obte_status reupload_real(DevBuf& b, const std::vector<double>& v, cudaStream_t st) {
+  std::vector<Real> h(v.begin(), v.end());
+  if (h.empty()) h.push_back(Real(0));
+  if (b.p && b.bytes == h.size() * sizeof(Real)) {
+    OBTE_CUDA(cudaMemcpyAsync(b.p, h.data(), b.bytes, cudaMemcpyHostToDevice, st));
+    OBTE_CUDA(wait_stream(st));
+    return OBTE_OK;
+  }
+  return upload(b, h, st);
+}
+
 // Compiled thread shapes (lanes per element G, MFPs per lane KV) for each precision.
 struct Shape { int G, KV; };
 template <typename Real> struct Shapes;
@@ -1340,6 +1354,10 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   OBTE_TRY(d.vals.alloc((size_t)s.n_dir * s.n * 2 * sizeof(Real) + 32));
   OBTE_CUDA(cudaMemsetAsync(d.vals.p, 0, d.vals.bytes, st));
   if (s.tf.ok) {   // transmission plans: keep what refresh_tables rewrites
+    if (d.h_rec_pin.p) {          // (a rebuilt table set: the old host records are about to be freed)
+      cudaHostUnregister(d.h_rec_pin.p);
+      d.h_rec_pin.p = nullptr;
+    }
     d.h_rec = std::move(pk.rec);
     d.h_spec = std::move(pk.spec);
     d.n_spec = (int64_t)(pk.sr.size() / SR);
@@ -1360,28 +1378,39 @@ static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) 
   constexpr int CSTEP = sizeof(Real) / 4, COEF = 4;
   std::vector<double> sr((size_t)d.n_spec * SR, 0.0);
   int32_t* rec = d.h_rec.data();
-  parallel_for((int64_t)s.n_dir * s.n, [&](int64_t it) {
-    int32_t* r = rec + it * W;
-    int k = 0, j = 0;
-    for (int f = 0; f < s.nf; ++f) {
-      const int32_t code = s.in_idx[it * s.nf + f];
-      const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
-      const double g = s.in_coef[it * s.nf + f];
-      if (kind == ITEM_CELL || kind == ITEM_PERIODIC) {
-        const Real v = (Real)g;
-        std::memcpy(&r[COEF + k * CSTEP], &v, sizeof(Real));
-        ++k;
-      } else if (kind == ITEM_WALL) {
-        sr[(size_t)d.h_spec[it] * SR + j] = g;
-        ++j;
+  {
+    PhaseTimer tw("refresh: coefficient words");
+    parallel_for((int64_t)s.n_dir * s.n, [&](int64_t it) {
+      int32_t* r = rec + it * W;
+      int k = 0, j = 0;
+      for (int f = 0; f < s.nf; ++f) {
+        const int32_t code = s.in_idx[it * s.nf + f];
+        const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
+        const double g = s.in_coef[it * s.nf + f];
+        if (kind == ITEM_CELL || kind == ITEM_PERIODIC) {
+          const Real v = (Real)g;
+          std::memcpy(&r[COEF + k * CSTEP], &v, sizeof(Real));
+          ++k;
+        } else if (kind == ITEM_WALL) {
+          sr[(size_t)d.h_spec[it] * SR + j] = g;
+          ++j;
+        }
       }
-    }
-  });
+    });
+  }
+  if (!d.h_rec_pin.p) {
+    // page-lock the host records once: later uploads then run at DMA speed (a failure only leaves them
+    // pageable)
+    if (cudaHostRegister(rec, d.h_rec.size() * sizeof(int32_t), cudaHostRegisterDefault) == cudaSuccess)
+      d.h_rec_pin.p = rec;
+    else
+      cudaGetLastError();
+  }
   OBTE_CUDA(cudaMemcpyAsync(d.rec.p, rec, d.h_rec.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  OBTE_CUDA(cudaMemcpyAsync(d.Pq.p, s.P.data(), s.P.size() * sizeof(double), cudaMemcpyHostToDevice, st));
   OBTE_CUDA(wait_stream(st));
-  OBTE_TRY(upload_real<Real>(d.sr, sr, st));
-  OBTE_CUDA(cudaMemcpy(d.Pq.p, s.P.data(), s.P.size() * sizeof(double), cudaMemcpyHostToDevice));
-  OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
+  OBTE_TRY(reupload_real<Real>(d.sr, sr, st));
+  OBTE_TRY(reupload_real<Real>(d.kcoef, s.kcoef, st));
   if (bytes)
     *bytes += (int64_t)(d.h_rec.size() * 4 + (sr.size() + s.kcoef.size()) * sizeof(Real) + s.P.size() * 8);
   return OBTE_OK;
