@@ -201,9 +201,13 @@ obte_status HostBuf::alloc(size_t n) {
   return OBTE_OK;
 }
 
+// A buffer that already holds an allocation of the needed size class is refilled in place: a re-upload
+// (new transmissions of a design loop, every step) then costs no cudaFree / cudaMalloc, which synchronise
+// the whole device.
 template <typename T>
 obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
-  OBTE_TRY(b.alloc(std::max<size_t>(v.size(), 1) * sizeof(T)));
+  const size_t need = std::max<size_t>(v.size(), 1) * sizeof(T);
+  if (!(b.p && b.bytes == size_class(need))) OBTE_TRY(b.alloc(need));
   if (!v.empty()) {
     OBTE_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
     OBTE_CUDA(wait_stream(stream));
@@ -212,7 +216,8 @@ obte_status upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
   return OBTE_OK;
 }
 obte_status upload_bytes(DevBuf& b, const void* p, size_t bytes, cudaStream_t stream) {
-  OBTE_TRY(b.alloc(std::max<size_t>(bytes, 1)));
+  const size_t need = std::max<size_t>(bytes, 1);
+  if (!(b.p && b.bytes == size_class(need))) OBTE_TRY(b.alloc(need));
   if (bytes) {
     OBTE_CUDA(cudaMemcpyAsync(b.p, p, bytes, cudaMemcpyHostToDevice, stream));
     OBTE_CUDA(wait_stream(stream));
@@ -330,21 +335,25 @@ extern "C" obte_status obte_bte_plan_set_transmission(obte_plan plan, const doub
   plan->ell_sum = offset_weights(plan, ell);
   // the preconditioner belongs to the old transmissions; the last solution stays as a warm start
   plan->xprec.reset();
+  dsa_join(plan);
   plan->dsa.reset();                       // its interface conductances change with t
   plan->n_solves = 0;
   if (!plan->ctx) return OBTE_OK;
+  // the acceleration's operator for the new t is built on a host thread while the tables are refreshed
+  dsa_start_async(plan);
   cudaStream_t strm = plan->stream;
   OBTE_TRY(upload(plan->ell, ell, strm));
   OBTE_TRY(upload(plan->kconst, s.kconst, strm));
   OBTE_TRY(upload(plan->kshift, s.kshift, strm));
   int64_t bytes = (int64_t)(ell.size() + s.kconst.size() + s.kshift.size()) * 8;
-  OBTE_TRY(refresh_tables(plan, &bytes));
+  OBTE_TRY(refresh_tables(plan, side_transmission, &bytes));
   if (upload_bytes) *upload_bytes = bytes;
   return OBTE_OK;
 }
 
 extern "C" obte_status obte_bte_plan_destroy(obte_plan plan) {
   if (!plan) return OBTE_OK;
+  dsa_join(plan);
   // every use of the plan's device buffers was on its stream: once it is idle they can be recycled
   const bool idle = plan->ctx && wait_stream(plan->stream) == cudaSuccess;
   if (idle) {

@@ -268,6 +268,29 @@ obte_status ensure_dsa(obte_plan plan) {
   return OBTE_OK;
 }
 
+void dsa_start_async(obte_plan plan) {
+  dsa_join(plan);
+  if (!plan->ctx || !dsa_default(plan->sched)) return;
+  plan->dsa.reset();
+  plan->dsa_build_status = OBTE_OK;
+  const int device = plan->ctx->device;
+  plan->dsa_build = std::thread([plan, device] {
+    if (cudaSetDevice(device) != cudaSuccess) {
+      plan->dsa_build_status = OBTE_ERR_CUDA;
+      return;
+    }
+    plan->dsa_build_status = ensure_dsa(plan);
+  });
+}
+
+obte_status dsa_join(obte_plan plan) {
+  if (plan->dsa_build.joinable()) plan->dsa_build.join();
+  const obte_status st = plan->dsa_build_status;
+  plan->dsa_build_status = OBTE_OK;
+  if (st != OBTE_OK) plan->dsa.reset();      // a failed build is redone (with its message) by the solve
+  return st;
+}
+
 void dsa_add(obte_plan plan, const double* in, double* out) {
   DsaOp& op = *plan->dsa;
   const Schedule& s = plan->sched;

@@ -326,18 +326,10 @@ struct DevSchedule {
   DevBuf rinv;
   // deterministic reductions (OBTE_DETERMINISTIC=1): per-(direction, chunk) partials and per-position sums
   DevBuf det_d, det_j, det_w, det_k, det_s, det_S, det_SJ;
-  // transmission plans: host copies of the packed records and of the special-entry index, so that new
-  // transmissions rewrite the coefficient words in place (refresh_tables)
-  RawVec<int32_t> h_rec, h_spec;
-  // h_rec page-locked on its first re-upload (the records are re-sent for every new set of transmissions);
-  // unregistered before h_rec is freed (members are destroyed in reverse order)
-  struct HostPin {
-    void* p = nullptr;
-    HostPin() = default;
-    HostPin(const HostPin&) = delete;
-    HostPin& operator=(const HostPin&) = delete;
-    ~HostPin() { if (p) cudaHostUnregister(p); }
-  } h_rec_pin;
+  // transmission plans: the special-entry index of each item (host), so that new transmissions rewrite
+  // the wall coefficients; the records' coefficient words are rewritten on the device (refresh_tables)
+  RawVec<int32_t> h_spec;
+  bool refreshable = false;
   int64_t n_spec = 0;
   size_t bytes() const;
 };
@@ -433,6 +425,13 @@ struct obte_plan_s {
   int64_t sweep_batch_stride = 0;
   std::unique_ptr<obte::XPrec> xprec;     // periodic-inflow block preconditioner
   std::unique_ptr<obte::DsaOp> dsa;       // diffusion-synthetic acceleration (built on first use)
+  // set-up of `dsa` for new transmissions, on a host thread beside the refresh of the tables (joined by
+  // the next solve or by destroy; a failure is retried there)
+  std::thread dsa_build;
+  obte_status dsa_build_status = OBTE_OK;
+  // transmission plans: per (item, inflow slot) the coefficient without t, its t factor (mode) and the
+  // record coefficient word it fills (-1: none), and the current side transmissions, on the device
+  obte::DevBuf tf_g0, tf_mode, tf_word, tf_t;
   int n_solves = 0;                       // obte_bte_solve calls on this plan
 };
 
@@ -445,7 +444,7 @@ obte_status ensure_tables(obte_plan plan, bool fp32);
 obte_status launch_sweep_df(obte_plan plan, const double* u_in, double* u_out, bool with_src, double* Jraw,
                             double* K, double* S);
 // After set_transmission: the coefficient words of the device tables that exist (bytes uploaded added to *bytes).
-obte_status refresh_tables(obte_plan plan, int64_t* bytes);
+obte_status refresh_tables(obte_plan plan, const double* side_transmission, int64_t* bytes);
 // Digest of the packed sweep tables of one precision, built on the host.
 obte_status tables_digest(obte_plan plan, bool fp32, uint64_t* digest);
 // Periodic-inflow preconditioner (xprec.cu): built once per plan.
@@ -457,6 +456,8 @@ int64_t xprec_resident_bytes(const XPrec* P);
 obte_status ensure_dsa(obte_plan plan);
 void dsa_add(obte_plan plan, const double* in, double* out);    // out += E L^-1 R in
 bool dsa_default(const Schedule& s);                            // on by default for this problem?
+void dsa_start_async(obte_plan plan);                           // build `dsa` on a host thread
+obte_status dsa_join(obte_plan plan);                           // wait for it (OBTE_OK if none ran)
 void dsa_matrix(const Schedule& s, std::vector<int32_t>& rp, std::vector<int32_t>& ci, std::vector<double>& val,
                 bool& project);                                 // the diffusion operator (host)
 int64_t xprec_build_bound(obte_plan plan);   // device bytes a build would allocate (0 once tried)

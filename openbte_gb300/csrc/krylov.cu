@@ -919,6 +919,7 @@ extern "C" obte_status obte_bte_solve(obte_plan plan, const obte_solve_opts* opt
   int dmode = (opts->dsa >= -1 && opts->dsa <= 1) ? opts->dsa : 0;
   if (const char* e = std::getenv("OBTE_DSA")) dmode = std::atoi(e) == 0 ? -1 : 1;
   const bool use_dsa = dmode == 1 || (dmode == 0 && dsa_default(s));
+  dsa_join(plan);                 // a set-up started by new transmissions
   if (use_dsa) OBTE_TRY(ensure_dsa(plan));
   if ((use_xp || use_dsa) && !wk.pz.p) OBTE_TRY(wk.pz.alloc((size_t)wk.nu * sizeof(double)));
   plan->has_solution = false;

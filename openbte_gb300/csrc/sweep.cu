@@ -1203,19 +1203,6 @@ static obte_status upload_real(DevBuf& b, const std::vector<double>& v, cudaStre
   return upload(b, h, st);
 }
 
-// The same into the buffer's existing allocation when the size matches (no cudaMalloc / cudaFree, which
-// synchronise the device), else as upload_real.  The copy is complete when this returns.
-template <typename Real>
-static obte_status reupload_real(DevBuf& b, const std::vector<double>& v, cudaStream_t st) {
-  std::vector<Real> h(v.begin(), v.end());
-  if (h.empty()) h.push_back(Real(0));
-  if (b.p && b.bytes == h.size() * sizeof(Real)) {
-    OBTE_CUDA(cudaMemcpyAsync(b.p, h.data(), b.bytes, cudaMemcpyHostToDevice, st));
-    OBTE_CUDA(wait_stream(st));
-    return OBTE_OK;
-  }
-  return upload(b, h, st);
-}
 
 // Compiled thread shapes (lanes per element G, MFPs per lane KV) for each precision.
 struct Shape { int G, KV; };
@@ -1354,11 +1341,7 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
   OBTE_TRY(d.vals.alloc((size_t)s.n_dir * s.n * 2 * sizeof(Real) + 32));
   OBTE_CUDA(cudaMemsetAsync(d.vals.p, 0, d.vals.bytes, st));
   if (s.tf.ok) {   // transmission plans: keep what refresh_tables rewrites
-    if (d.h_rec_pin.p) {          // (a rebuilt table set: the old host records are about to be freed)
-      cudaHostUnregister(d.h_rec_pin.p);
-      d.h_rec_pin.p = nullptr;
-    }
-    d.h_rec = std::move(pk.rec);
+    d.refreshable = true;
     d.h_spec = std::move(pk.spec);
     d.n_spec = (int64_t)(pk.sr.size() / SR);
   }
@@ -1369,50 +1352,85 @@ static obte_status upload_tables(obte_plan plan, DevSchedule& d) {
 // New transmissions: rewrite the coefficient words of the records and the wall inflow coefficients of
 // the special entries (the same walk over the inflow entries as pack), then P and the contact
 // coefficients; indices, units and launch order stay.
+// Coefficient word w of item `it`'s record from inflow slot f: g0 x (t_s, 1 - t_s or 1 by the slot's mode),
+// the same arithmetic as set_transmission on the host, rounded to the record's precision.
+template <typename Real, int NF>
+__global__ void refresh_rec_kernel(int64_t items, const double* __restrict__ g0, const int32_t* __restrict__ mode,
+                                   const int8_t* __restrict__ word, const double* __restrict__ t,
+                                   int32_t* __restrict__ rec) {
+  using RR = Rec<Real, NF>;
+  for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < items; it += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const int64_t e = it * NF + f;
+      const int w = word[e];
+      if (w < 0) continue;
+      const int32_t md = mode[e];
+      const double g = md >= 0 ? g0[e] * t[md] : md == -1 ? g0[e] * 1.0 : g0[e] * (1.0 - t[-md - 2]);
+      int32_t* r = rec + it * RR::W + RR::COEF + w * RR::CSTEP;
+      if constexpr (sizeof(Real) == 4) {
+        r[0] = __float_as_int((float)g);
+      } else {
+        r[0] = __double2loint(g);
+        r[1] = __double2hiint(g);
+      }
+    }
+  }
+}
+
+// The transmission-free factors of a transmission plan on the device (once), and the new t
+static obte_status upload_transmission(obte_plan plan, const double* t) {
+  const Schedule& s = plan->sched;
+  cudaStream_t st = plan->stream;
+  if (!plan->tf_g0.p) {
+    const int64_t items = (int64_t)s.n_dir * s.n;
+    std::vector<int8_t> word((size_t)items * s.nf, -1);
+    parallel_for(items, [&](int64_t it) {
+      int k = 0;
+      for (int f = 0; f < s.nf; ++f) {
+        const int kind = (int)((uint32_t)s.in_idx[it * s.nf + f] >> ITEM_SHIFT);
+        if (kind == ITEM_CELL || kind == ITEM_PERIODIC) word[(size_t)it * s.nf + f] = (int8_t)k++;
+      }
+    });
+    OBTE_TRY(upload(plan->tf_g0, s.tf.g0, st));
+    OBTE_TRY(upload(plan->tf_mode, s.tf.mode, st));
+    OBTE_TRY(upload(plan->tf_word, word, st));
+  }
+  std::vector<double> tv(t, t + s.n_sides);
+  return upload(plan->tf_t, tv, st);
+}
+
 template <typename Real>
 static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) {
   const Schedule& s = plan->sched;
   cudaStream_t st = plan->stream;
-  if (d.h_rec.empty()) { d.ready = false; return OBTE_OK; }   // rebuilt on next use
-  const int W = rec_words(sizeof(Real), s.nf);
-  constexpr int CSTEP = sizeof(Real) / 4, COEF = 4;
+  if (!d.refreshable) { d.ready = false; return OBTE_OK; }   // rebuilt on next use
+  const int64_t items = (int64_t)s.n_dir * s.n;
+  // the records' coefficient words, on the device from the transmission-free factors and t
+  const int blocks = (int)std::min<int64_t>((items + 255) / 256, (int64_t)plan->ctx->num_sms * 8);
+  auto kern = s.nf == 3 ? refresh_rec_kernel<Real, 3> : refresh_rec_kernel<Real, 4>;
+  if (s.nf != 3 && s.nf != 4) { d.ready = false; return OBTE_OK; }
+  kern<<<blocks, 256, 0, st>>>(items, plan->tf_g0.as<double>(), plan->tf_mode.as<int32_t>(),
+                               plan->tf_word.as<int8_t>(), plan->tf_t.as<double>(), d.rec.as<int32_t>());
+  count_launch();
+  OBTE_CUDA(cudaGetLastError());
+  // wall coefficients of the special entries (host, small)
+  PhaseTimer th(sizeof(Real) == 4 ? "refresh fp32: walls and uploads" : "refresh fp64: walls and uploads");
   std::vector<double> sr((size_t)d.n_spec * SR, 0.0);
-  int32_t* rec = d.h_rec.data();
-  {
-    PhaseTimer tw("refresh: coefficient words");
-    parallel_for((int64_t)s.n_dir * s.n, [&](int64_t it) {
-      int32_t* r = rec + it * W;
-      int k = 0, j = 0;
-      for (int f = 0; f < s.nf; ++f) {
-        const int32_t code = s.in_idx[it * s.nf + f];
-        const int kind = (int)((uint32_t)code >> ITEM_SHIFT);
-        const double g = s.in_coef[it * s.nf + f];
-        if (kind == ITEM_CELL || kind == ITEM_PERIODIC) {
-          const Real v = (Real)g;
-          std::memcpy(&r[COEF + k * CSTEP], &v, sizeof(Real));
-          ++k;
-        } else if (kind == ITEM_WALL) {
-          sr[(size_t)d.h_spec[it] * SR + j] = g;
-          ++j;
-        }
-      }
-    });
-  }
-  if (!d.h_rec_pin.p) {
-    // page-lock the host records once: later uploads then run at DMA speed (a failure only leaves them
-    // pageable)
-    if (cudaHostRegister(rec, d.h_rec.size() * sizeof(int32_t), cudaHostRegisterDefault) == cudaSuccess)
-      d.h_rec_pin.p = rec;
-    else
-      cudaGetLastError();
-  }
-  OBTE_CUDA(cudaMemcpyAsync(d.rec.p, rec, d.h_rec.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  parallel_for(items, [&](int64_t it) {
+    const int32_t sp = d.h_spec[it];
+    if (sp < 0) return;
+    int j = 0;
+    for (int f = 0; f < s.nf; ++f) {
+      const int32_t code = s.in_idx[it * s.nf + f];
+      if ((int)((uint32_t)code >> ITEM_SHIFT) == ITEM_WALL) sr[(size_t)sp * SR + j++] = s.in_coef[it * s.nf + f];
+    }
+  });
   OBTE_CUDA(cudaMemcpyAsync(d.Pq.p, s.P.data(), s.P.size() * sizeof(double), cudaMemcpyHostToDevice, st));
   OBTE_CUDA(wait_stream(st));
-  OBTE_TRY(reupload_real<Real>(d.sr, sr, st));
-  OBTE_TRY(reupload_real<Real>(d.kcoef, s.kcoef, st));
-  if (bytes)
-    *bytes += (int64_t)(d.h_rec.size() * 4 + (sr.size() + s.kcoef.size()) * sizeof(Real) + s.P.size() * 8);
+  OBTE_TRY(upload_real<Real>(d.sr, sr, st));
+  OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
+  if (bytes) *bytes += (int64_t)((sr.size() + s.kcoef.size()) * sizeof(Real) + s.P.size() * 8);
   return OBTE_OK;
 }
 
@@ -1463,8 +1481,14 @@ obte_status tables_digest(obte_plan plan, bool fp32, uint64_t* digest) {
   return fp32 ? tables_digest_impl<float>(plan->sched, digest) : tables_digest_impl<double>(plan->sched, digest);
 }
 
-obte_status refresh_tables(obte_plan plan, int64_t* bytes) {
+obte_status refresh_tables(obte_plan plan, const double* side_transmission, int64_t* bytes) {
   PhaseTimer timer("refresh_tables");
+  if (!plan->d32.ready && !plan->d64.ready) return OBTE_OK;
+  {
+    PhaseTimer tt("refresh: transmissions to the device");
+    OBTE_TRY(upload_transmission(plan, side_transmission));
+  }
+  if (bytes) *bytes += (int64_t)plan->sched.n_sides * 8;
   if (plan->d32.ready) OBTE_TRY(refresh_impl<float>(plan, plan->d32, bytes));
   if (plan->d64.ready) OBTE_TRY(refresh_impl<double>(plan, plan->d64, bytes));
   return OBTE_OK;
