@@ -1400,8 +1400,15 @@ static obte_status upload_transmission(obte_plan plan, const double* t) {
   return upload(plan->tf_t, tv, st);
 }
 
+__global__ void narrow_kernel(int64_t n, const double* __restrict__ in, float* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+// `done`: the FP64 tables, refreshed just before (the FP32 refresh then copies P and narrows the contact
+// coefficients on the device instead of uploading them again)
 template <typename Real>
-static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) {
+static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes, const DevSchedule* done = nullptr) {
   const Schedule& s = plan->sched;
   cudaStream_t st = plan->stream;
   if (!d.refreshable) { d.ready = false; return OBTE_OK; }   // rebuilt on next use
@@ -1426,11 +1433,22 @@ static obte_status refresh_impl(obte_plan plan, DevSchedule& d, int64_t* bytes) 
       if ((int)((uint32_t)code >> ITEM_SHIFT) == ITEM_WALL) sr[(size_t)sp * SR + j++] = s.in_coef[it * s.nf + f];
     }
   });
-  OBTE_CUDA(cudaMemcpyAsync(d.Pq.p, s.P.data(), s.P.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  const size_t kc_n = std::max<size_t>(s.kcoef.size(), 1);
+  const bool reuse = sizeof(Real) == 4 && done && done->Pq.p && d.Pq.bytes == done->Pq.bytes && done->kcoef.p &&
+                     d.kcoef.p && d.kcoef.bytes >= kc_n * sizeof(Real) && done->kcoef.bytes >= kc_n * sizeof(double);
+  if (reuse) {
+    OBTE_CUDA(cudaMemcpyAsync(d.Pq.p, done->Pq.p, s.P.size() * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    narrow_kernel<<<(int)std::min<size_t>((kc_n + 255) / 256, 1024), 256, 0, st>>>(
+        (int64_t)kc_n, done->kcoef.as<double>(), d.kcoef.as<float>());
+    count_launch();
+    OBTE_CUDA(cudaGetLastError());
+  } else {
+    OBTE_CUDA(cudaMemcpyAsync(d.Pq.p, s.P.data(), s.P.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
   OBTE_CUDA(wait_stream(st));
   OBTE_TRY(upload_real<Real>(d.sr, sr, st));
-  OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
-  if (bytes) *bytes += (int64_t)((sr.size() + s.kcoef.size()) * sizeof(Real) + s.P.size() * 8);
+  if (!reuse) OBTE_TRY(upload_real<Real>(d.kcoef, s.kcoef, st));
+  if (bytes) *bytes += (int64_t)(sr.size() * sizeof(Real) + (reuse ? 0 : s.kcoef.size() * sizeof(Real) + s.P.size() * 8));
   return OBTE_OK;
 }
 
@@ -1489,8 +1507,8 @@ obte_status refresh_tables(obte_plan plan, const double* side_transmission, int6
     OBTE_TRY(upload_transmission(plan, side_transmission));
   }
   if (bytes) *bytes += (int64_t)plan->sched.n_sides * 8;
-  if (plan->d32.ready) OBTE_TRY(refresh_impl<float>(plan, plan->d32, bytes));
   if (plan->d64.ready) OBTE_TRY(refresh_impl<double>(plan, plan->d64, bytes));
+  if (plan->d32.ready) OBTE_TRY(refresh_impl<float>(plan, plan->d32, bytes, plan->d64.ready ? &plan->d64 : nullptr));
   return OBTE_OK;
 }
 
