@@ -315,3 +315,30 @@ def test_concurrent_builds_of_one_geometry_share_a_plan(monkeypatch):
     assert len(plans) == 1
     assert sorted(lease.use for lease, _, _ in out) == [0, 1]
     assert sorted(cached for _, _, cached in out) == [False, True]
+
+
+def test_loose_refine_requests_prepare_fp32_tables_only(monkeypatch):
+    """A FP32+refine request at a tolerance of 5e-6 or looser never sweeps in FP64, so its plan is prepared
+    (and its footprint counted) with the FP32 tables only; a tighter one gets both."""
+    class RecPlan(_PlanStub):
+        def __init__(self):
+            super().__init__()
+            self.seen = []
+
+        def footprint(self, precision, restart):
+            self.seen.append(("footprint", precision))
+            return super().footprint(precision, restart)
+
+        def prepare(self, precision, restart):
+            self.seen.append(("prepare", precision))
+            super().prepare(precision, restart)
+
+    for rtol, want in ((1e-5, "fp32"), (5e-6, "fp32"), (1e-8, "fp32_refine")):
+        plan = RecPlan()
+        be = _stub_backend(monkeypatch, plan)
+        srv = Server(backend=be, slots=1, builders=1, hbm_budget=10_000)
+        res = replay(srv, [Request(None, None, None, None, precision="fp32_refine", rtol=rtol)])
+        srv.close()
+        assert res[0].status == "ok"
+        assert {p for _, p in plan.seen} == {want}, (rtol, plan.seen)
+        assert ("prepare", want) in plan.seen
