@@ -279,7 +279,8 @@ def kappa_eff(rho, solver: PixelSolver):
 def get_solver(**options):
     """The reference's solver factory (openbte/inverse/bte.py:171-255): options ``grid`` (pixels per
     side), ``Kn`` (gray: MFP / cell size) or ``material`` (an IsotropicMaterial), ``n_phi``,
-    ``directions`` (list of [1, 0] / [0, 1]), ``size``, ``precision``, ``rtol``.  Returns
+    ``directions`` (list of [1, 0] / [0, 1]), ``size``, ``precision``, ``rtol``, ``dsa`` (0: the default
+    acceleration, -1 off).  Returns
     ``func(rho) -> ((kappa[n_directions], 1), jacobian[n_directions, grid**2])``."""
     n = int(options["grid"])
     size = float(options.get("size", 1.0))
@@ -289,7 +290,8 @@ def get_solver(**options):
         mat = IsotropicMaterial.gray(float(options["Kn"]), n_phi, size)
     directions = options.get("directions", [[1, 0]])
     solvers = [PixelSolver(n, mat, size, tuple(d), device=int(options.get("device", 0)),
-                           precision=options.get("precision", "fp32_refine"), rtol=float(options.get("rtol", 1e-8)))
+                           precision=options.get("precision", "fp32_refine"), rtol=float(options.get("rtol", 1e-8)),
+                           dsa=int(options.get("dsa", 0)))
                for d in directions]
 
     def func(rho):
