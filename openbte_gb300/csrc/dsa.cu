@@ -63,17 +63,32 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return red[0];
 }
 
-// b = V in[0:n], projected onto zero sum when `project` (one CTA of 1024 threads)
-__global__ void __launch_bounds__(1024) dsa_restrict_kernel(int64_t n, const double* __restrict__ vol,
-                                                            double inv_vol_sum, int project,
-                                                            const double* __restrict__ in, double* __restrict__ b) {
+// part[block] = sum over the block's grid-stride range of V x (fixed order)
+__global__ void dsa_partial_kernel(int64_t n, const double* __restrict__ vol, const double* __restrict__ x,
+                                   double* __restrict__ part) {
   __shared__ double red[32];
   double s = 0;
-  if (project) {
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += vol[i] * in[i];
-    s = block_sum(s, red) * inv_vol_sum;
-  }
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) b[i] = vol[i] * (in[i] - s);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += vol[i] * x[i];
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// sum of the np partials, the same value (same order) in every block
+__device__ __forceinline__ double sum_partials(const double* __restrict__ part, int np, double* red) {
+  double s = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  return block_sum(s, red);
+}
+
+// b = V in[0:n], minus V times the volume-weighted mean of in when `part` (the partials of V in) is given
+__global__ void dsa_restrict_kernel(int64_t n, const double* __restrict__ vol, double inv_vol_sum,
+                                    const double* __restrict__ part, int np, const double* __restrict__ in,
+                                    double* __restrict__ b) {
+  __shared__ double red[32];
+  const double mu = part ? sum_partials(part, np, red) * inv_vol_sum : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = vol[i] * (in[i] - mu);
 }
 
 // r = b - L d (CSR, one thread per row)
@@ -91,23 +106,15 @@ __global__ void dsa_axpy_kernel(int64_t n, const double* __restrict__ e, double*
   for (int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x; i < n; i += (int64_t)gridDim.x * DT) d[i] += e[i];
 }
 
-// mean[0] = sum V d / sum V (one CTA of 1024 threads)
-__global__ void __launch_bounds__(1024) dsa_mean_kernel(int64_t n, const double* __restrict__ vol,
-                                                        double inv_vol_sum, const double* __restrict__ d,
-                                                        double* __restrict__ mean) {
-  __shared__ double red[32];
-  double s = 0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += vol[i] * d[i];
-  s = block_sum(s, red);
-  if (threadIdx.x == 0) mean[0] = s * inv_vol_sum;
-}
-
 // out[i] += d[cell(i)] - mean over the state: temperatures, wall temperatures (element of the wall),
-// periodic inflow (element of the source slot, every MFP)
+// periodic inflow (element of the source slot, every MFP); the mean is the volume-weighted one of d from its
+// partials (or 0 without them)
 __global__ void dsa_extend_kernel(int64_t n, int64_t nd, int64_t nu, int n_mfp, const int32_t* __restrict__ wcell,
                                   const int32_t* __restrict__ xcell, const double* __restrict__ d,
-                                  const double* __restrict__ mean, double* __restrict__ out) {
-  const double mu = mean ? mean[0] : 0.0;
+                                  const double* __restrict__ part, int np, double inv_vol_sum,
+                                  double* __restrict__ out) {
+  __shared__ double red[32];
+  const double mu = part ? sum_partials(part, np, red) * inv_vol_sum : 0.0;
   const int64_t xoff = n + nd;
   for (int64_t i = (int64_t)blockIdx.x * DT + threadIdx.x; i < nu; i += (int64_t)gridDim.x * DT) {
     const int64_t c = i < n ? i : i < xoff ? (int64_t)wcell[i - n] : (int64_t)xcell[(i - xoff) / n_mfp];
@@ -252,7 +259,7 @@ obte_status ensure_dsa(obte_plan plan) {
   OBTE_TRY(upload(op->val, val, st));
   OBTE_TRY(upload(op->vol, D.vol, st));
   for (DevBuf* b : {&op->b, &op->d, &op->r, &op->e}) OBTE_TRY(b->alloc((size_t)n * sizeof(double)));
-  OBTE_TRY(op->mean.alloc(sizeof(double)));
+  OBTE_TRY(op->mean.alloc((size_t)grid_for(n, plan->ctx->num_sms) * sizeof(double)));   // partial sums
   double vs = 0;
   for (double v : D.vol) vs += v;
   op->inv_vol_sum = vs > 0 ? 1.0 / vs : 0.0;
@@ -301,7 +308,13 @@ void dsa_add(obte_plan plan, const double* in, double* out) {
   const int gn = grid_for(n, num_sms);
   double* b = op.b.as<double>();
   double* d = op.d.as<double>();
-  dsa_restrict_kernel<<<1, 1024, 0, st>>>(n, op.vol.as<double>(), op.inv_vol_sum, op.project ? 1 : 0, in, b);
+  double* part = op.mean.as<double>();          // partial sums, one per block of the n-element grid
+  if (op.project) {
+    dsa_partial_kernel<<<gn, DT, 0, st>>>(n, op.vol.as<double>(), in, part);
+    count_launch();
+  }
+  dsa_restrict_kernel<<<gn, DT, 0, st>>>(n, op.vol.as<double>(), op.inv_vol_sum, op.project ? part : nullptr, gn,
+                                         in, b);
   count_launch();
   count_launch(amg_apply(*op.amg, b, d, nullptr, 0, st));
   for (int c = 1; c < op.cycles; ++c) {
@@ -312,12 +325,12 @@ void dsa_add(obte_plan plan, const double* in, double* out) {
     count_launch(2);
   }
   if (op.project) {
-    dsa_mean_kernel<<<1, 1024, 0, st>>>(n, op.vol.as<double>(), op.inv_vol_sum, d, op.mean.as<double>());
+    dsa_partial_kernel<<<gn, DT, 0, st>>>(n, op.vol.as<double>(), d, part);
     count_launch();
   }
   dsa_extend_kernel<<<grid_for(plan->nu, num_sms), DT, 0, st>>>(
       n, s.nd, plan->nu, s.n_mfp, plan->diffuse_cell.as<int32_t>(), plan->x_cell.as<int32_t>(), d,
-      op.project ? op.mean.as<double>() : nullptr, out);
+      op.project ? part : nullptr, gn, op.inv_vol_sum, out);
   count_launch();
 }
 

@@ -359,7 +359,8 @@ struct DsaOp {
   AmgPtr amg;
   DevBuf rp, ci, val;            // L (CSR, symmetric, volume-weighted)
   DevBuf vol;                    // [n]
-  DevBuf b, d, r, e, mean;       // right-hand side, correction, residual, cycle update; weighted mean
+  DevBuf b, d, r, e, mean;       // right-hand side, correction, residual, cycle update; partial sums of the
+                                 // weighted means (one per block)
   double inv_vol_sum = 0;
   bool project = true;           // L has the constant null vector (no isothermal walls)
   int cycles = 1;
