@@ -43,3 +43,19 @@ def test_step_time_is_max_over_ranks():
 def test_single_rank_is_identity():
     import bench
     assert bench.max_over_ranks(0.5, 1, "cpu") == 0.5
+
+
+def test_traffic_table_and_profiles_are_consistent():
+    """Every measured-traffic entry of the bench names a workload it can run and a committed profile
+    summary, and every profile summary gives the command that made it."""
+    import bench
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for (workload, precision), traffic in bench.SWEEP_DRAM_BYTES.items():
+        assert workload in bench.WORKLOADS, workload
+        assert precision in ("fp32", "fp64"), precision
+        assert traffic > 0
+        src = bench.SWEEP_DRAM_SOURCE[(workload, precision)].split(" ")[0]
+        assert os.path.exists(os.path.join(root, src)), src
+    for name in os.listdir(os.path.join(root, "profiles")):
+        text = open(os.path.join(root, "profiles", name)).read()
+        assert "Command" in text and "ncu " in text, name
