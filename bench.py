@@ -181,7 +181,8 @@ def run_serve(args, dev, world, rank, local):
     # GPU-slot threads sleep while their solve runs instead of spinning on a core: the cores go to the
     # threads that build and upload the next requests' plans
     os.environ["OBTE_BLOCKING_SYNC"] = "1"
-    pool = dict(device=local, slots=args.slots, builders=args.builders, preparers=args.preparers)
+    pool = dict(device=local, slots=args.slots, builders=args.builders, preparers=args.preparers,
+                restart=args.serve_restart)
     t0 = time.time()
     reqs = serving_stream(n_req)
     mesh_s = time.time() - t0
@@ -928,6 +929,7 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-7)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-restart", type=int, default=30, help="GMRES restart length of served solves")
     ap.add_argument("--serve-rtol", type=float, default=1e-5,
                     help="serving stream: residual tolerance of each request (FP32+refine and one-at-a-time FP64)")
     ap.add_argument("--slots", type=int, default=12, help="serving stream: concurrent GPU solves")
