@@ -1,5 +1,6 @@
 """Host side of the inverse-design solver (no GPU)."""
 import numpy as np
+import pytest
 
 
 def test_reversed_material_and_closure():
@@ -90,3 +91,50 @@ def test_dsa_operator_matches_its_restatement():
     np.testing.assert_allclose(Mgot, Mexp, rtol=1e-12, atol=1e-12 * np.abs(Mexp).max())
     # the pore pixel's row is the floor (its sides' conductances are ~1e-12)
     assert Mgot[5, 5] > 1e6 * np.abs(np.delete(Mgot[5], 5)).max()
+
+
+@pytest.mark.parametrize("name", ["a600", "cube1k5"])
+def test_dsa_operator_on_unstructured_meshes(case, name):
+    """The acceleration's operator on triangles and tetrahedra (host-only plan): per internal side
+    A sum_m D_m / d with d = sum over the side's two elements of dim V / (sides x A) (exact for simplices),
+    the floor and the shift, against a numpy restatement; symmetric, with the source projected (no
+    isothermal walls)."""
+    import ctypes as C
+    from openbte_gb300 import _lib
+    from openbte_gb300.runtime import HostProblem, Plan
+    geo, mat, bcs, ek, _ = case(name)
+    hp = HostProblem(geo, mat, bcs, ek)
+    plan = Plan(hp, host_only=True)
+    n = hp.n_elems
+    nnz, proj = C.c_int64(0), C.c_int32()
+    _lib.check(plan.lib.obte_bte_dsa_operator(plan.handle, C.byref(nnz), None, None, None, C.byref(proj)), "size")
+    rp, ci, val = np.zeros(n + 1, np.int32), np.zeros(nnz.value, np.int32), np.zeros(nnz.value)
+    _lib.check(plan.lib.obte_bte_dsa_operator(plan.handle, C.byref(nnz), rp.ctypes.data_as(C.c_void_p),
+                                              ci.ctypes.data_as(C.c_void_p), val.ctypes.data_as(C.c_void_p),
+                                              C.byref(proj)), "operator")
+    assert proj.value == 1
+    M = np.zeros((n, n))
+    for i in range(n):
+        M[i, ci[rp[i]:rp[i + 1]]] = val[rp[i]:rp[i + 1]]
+    np.testing.assert_allclose(M, M.T, rtol=1e-14, atol=0)
+    # restatement
+    dim, nf = hp.dim, hp.elem_nv
+    V = hp.vol
+    tc, L = np.asarray(mat.t_coeff, dtype=np.float64), np.asarray(mat.mfps, dtype=np.float64)
+    v = np.asarray(mat.vmfp, dtype=np.float64)[:, :dim]
+    Dsum = (tc * L[:, None] ** 2 * (v ** 2).sum(axis=1)[None, :]).sum() / dim
+    E = np.zeros((n, n))
+    diag = np.zeros(n)
+    for sd in hp.internal:
+        i, j = hp.sem[sd]
+        A = np.linalg.norm(hp.na[sd])
+        d = dim * V[i] / (nf * A) + dim * V[j] / (nf * A)
+        c = A * Dsum / d
+        diag[i] += c
+        diag[j] += c
+        E[i, j] -= c
+        E[j, i] -= c
+    reg = 1e-6 * diag.max()
+    diag = np.maximum(diag, 0.05 * np.sort(diag / V)[n // 2] * V)
+    E[np.arange(n), np.arange(n)] += diag + reg
+    np.testing.assert_allclose(M, E, rtol=1e-11, atol=1e-11 * np.abs(E).max())
